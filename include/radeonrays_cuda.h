@@ -1,0 +1,128 @@
+/*
+ * radeonrays_cuda.h -- CUDA interop and GB300 extensions of the RadeonRays C API.
+ *
+ * The reference ships Vulkan and D3D12 interop headers
+ * (src/core/include/radeonrays_vlk.h, radeonrays_dx.h).  This header is their
+ * CUDA counterpart: it wraps raw device pointers and CUDA streams as RadeonRays
+ * handles, keeps the API-neutral buffer helpers (rrAllocateDeviceBuffer,
+ * rrMapDevicePtr, rrUnmapDevicePtr) and adds the few controls the GB300 build
+ * needs (node format of a build, traversal kernel selection, device error
+ * word, traversal counters).
+ *
+ * All entry points are plain C: pointers, sizes and 32-bit enums only.  CUDA
+ * handles (cudaStream_t) are passed as void*.
+ */
+#ifndef RADEONRAYS_CUDA_H
+#define RADEONRAYS_CUDA_H
+
+#include "radeonrays.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- node formats of a geometry build ---------------------------------- */
+typedef enum
+{
+    /* Binary 64-byte nodes in the reference layout only ("plain" path). */
+    RR_CUDA_NODE_FORMAT_BINARY = 0,
+    /* Binary nodes plus 8-wide nodes with 8-bit conservatively quantised child
+     * bounds and a 48-byte triangle array (the default). */
+    RR_CUDA_NODE_FORMAT_WIDE8 = 1
+} RRCudaNodeFormat;
+
+/* Passed through RRBuildOptions::backend_specific_info.  A null
+ * backend_specific_info selects the defaults (WIDE8, 30-bit Morton codes). */
+typedef struct
+{
+    uint32_t struct_size;   /* sizeof(RRCudaBuildOptions) */
+    uint32_t node_format;   /* RRCudaNodeFormat */
+    uint32_t morton_bits;   /* 30 (reference) or 63; 0 = 30 */
+    uint32_t reserved;
+} RRCudaBuildOptions;
+
+/* ---- traversal kernel selection ---------------------------------------- */
+typedef enum
+{
+    /* Wide kernel when the buffer holds wide nodes, else the binary kernel. */
+    RR_CUDA_TRAVERSAL_AUTO = 0,
+    /* One thread per ray, 64-byte binary nodes, reference visit order. */
+    RR_CUDA_TRAVERSAL_BINARY = 1,
+    /* Persistent warp-scheduled kernel over 8-wide quantised nodes. */
+    RR_CUDA_TRAVERSAL_WIDE = 2
+} RRCudaTraversal;
+
+typedef struct
+{
+    uint32_t struct_size;     /* sizeof(RRCudaTraversalOptions) */
+    uint32_t traversal;       /* RRCudaTraversal */
+    uint32_t block_size;      /* threads per block, 0 = tuned default */
+    uint32_t blocks_per_sm;   /* persistent kernel occupancy, 0 = tuned default */
+    uint32_t collect_stats;   /* 1 = count node and triangle fetches */
+    uint32_t reserved[3];
+} RRCudaTraversalOptions;
+
+/* Fetch counters accumulated while collect_stats is 1. */
+typedef struct
+{
+    uint64_t rays;
+    uint64_t node_fetches;     /* binary nodes (64 B) or wide nodes (80 B) */
+    uint64_t triangle_fetches; /* wide-path triangles (48 B); 0 on the binary path */
+    uint64_t node_bytes;       /* bytes of one node fetch */
+    uint64_t triangle_bytes;   /* bytes of one triangle fetch */
+} RRCudaTraversalStats;
+
+/* Bits of the sticky device error word (rrCudaGetDeviceErrors). */
+typedef enum
+{
+    RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW   = 1, /* a ray needed more stack than its scratch slot */
+    RR_CUDA_DEVICE_ERROR_BAD_BUFFER       = 2, /* the BVH buffer header did not match */
+    RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH   = 4, /* wide collapse ran out of levels */
+    RR_CUDA_DEVICE_ERROR_NODE_RANGE       = 8, /* a node index left the node array */
+    RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT     = 16 /* a bounded device wait ran out (result invalid) */
+} RRCudaDeviceError;
+
+/* Wrap a CUDA device pointer (plus byte offset) as an RRDevicePtr.  The caller
+ * keeps ownership of the memory; rrReleaseDevicePtr frees only the handle.
+ * Replaces rrGetDevicePtrFromVkBuffer (reference radeonrays_vlk.h:38). */
+RR_API RRError rrGetDevicePtrFromCudaPtr(RRContext context, void* cuda_ptr, size_t offset, RRDevicePtr* device_ptr);
+
+/* Device address (base + offset) behind an RRDevicePtr. */
+RR_API RRError rrGetCudaPtrFromDevicePtr(RRContext context, RRDevicePtr device_ptr, void** cuda_ptr);
+
+/* Wrap a cudaStream_t: rrCmd* calls on the returned stream enqueue at once on
+ * that CUDA stream (no rrSumbitCommandStream needed).  Release it with
+ * rrReleaseExternalCommandStream.
+ * Replaces rrGetCommandStreamFromVkCommandBuffer (reference radeonrays_vlk.h:64). */
+RR_API RRError rrGetCommandStreamFromCudaStream(RRContext context, void* cuda_stream, RRCommandStream* command_stream);
+
+/* Allocate a buffer the host can map (CUDA managed memory).
+ * reference radeonrays_vlk.h:77 */
+RR_API RRError rrAllocateDeviceBuffer(RRContext context, size_t size, RRDevicePtr* device_ptr);
+/* reference radeonrays_vlk.h:86.  Only buffers from rrAllocateDeviceBuffer map. */
+RR_API RRError rrMapDevicePtr(RRContext context, RRDevicePtr device_ptr, void** mapping_ptr);
+/* reference radeonrays_vlk.h:95 */
+RR_API RRError rrUnmapDevicePtr(RRContext context, RRDevicePtr device_ptr, void** mapping_ptr);
+
+/* Select the traversal kernel and its launch shape for later rrCmdIntersect
+ * calls on this context (no reference counterpart: the reference has one
+ * kernel per variant). */
+RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversalOptions* options);
+RR_API RRError rrCudaGetTraversalOptions(RRContext context, RRCudaTraversalOptions* options);
+
+/* Read and clear the context's sticky device error word (RRCudaDeviceError
+ * bits).  Synchronises the context's internal stream. */
+RR_API RRError rrCudaGetDeviceErrors(RRContext context, uint32_t* error_bits);
+
+/* Read and clear the traversal counters (collect_stats = 1). */
+RR_API RRError rrCudaGetTraversalStats(RRContext context, RRCudaTraversalStats* stats);
+
+/* Milliseconds rrWaitEvent polls before it gives up with RR_ERROR_INTERNAL
+ * (default 600000).  The reference waits forever (vlk/device.cpp:249-272). */
+RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RADEONRAYS_CUDA_H */

@@ -1,0 +1,841 @@
+// api.cu -- the C-ABI of the GB300 RadeonRays build (librr.so).
+//
+// Mirrors the reference's API shim (src/core/src/radeonrays.cpp) and its
+// Vulkan intersector facade (src/core/src/vlk/intersector.cpp): the same entry
+// points, argument checks and error codes, with one backend (CUDA) and no
+// virtual dispatch.  Execution model:
+//   * a command stream from rrAllocateCommandStream records operations; the
+//     first rrSumbitCommandStream captures them into a CUDA graph that later
+//     submissions replay (falls back to direct launches if capture fails);
+//   * a command stream from rrGetCommandStreamFromCudaStream enqueues each
+//     operation immediately on the caller's CUDA stream;
+//   * RREvent wraps a cudaEvent_t; rrWaitEvent polls it with a timeout.
+// No exception crosses the C boundary; CUDA allocation failures map to
+// RR_ERROR_OUT_OF_DEVICE_MEMORY, other failures to RR_ERROR_INTERNAL.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "rr_internal.h"
+
+using namespace rr;
+
+// ---------------------------------------------------------------------------
+// Logging (the reference wraps spdlog, utils/logger.h:33-110; this is a
+// level-filtered stderr/file logger with the same two controls).
+namespace
+{
+std::mutex g_log_mu;
+int        g_log_level = RR_LOG_LEVEL_WARN;
+FILE*      g_log_file  = nullptr;
+
+void logf(int level, const char* fmt, ...)
+{
+    if (level < g_log_level || g_log_level >= RR_LOG_LEVEL_OFF) return;
+    static const char* names[] = {"", "debug", "info", "warn", "error"};
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    FILE*                       f = g_log_file ? g_log_file : stderr;
+    std::fprintf(f, "[rr %s] ", names[std::min(level, 4)]);
+    va_list ap;
+    va_start(ap, fmt);
+    std::vfprintf(f, fmt, ap);
+    va_end(ap);
+    std::fputc('\n', f);
+    std::fflush(f);
+}
+#define RR_LOG_INFO(...) logf(RR_LOG_LEVEL_INFO, __VA_ARGS__)
+#define RR_LOG_ERROR(...) logf(RR_LOG_LEVEL_ERROR, __VA_ARGS__)
+
+struct CudaFail : std::runtime_error
+{
+    cudaError_t code;
+    CudaFail(cudaError_t c, const char* what) : std::runtime_error(what), code(c) {}
+};
+inline void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw CudaFail(e, what);
+}
+
+RRError map_error(const CudaFail& f)
+{
+    RR_LOG_ERROR("%s: %s", f.what(), cudaGetErrorString(f.code));
+    return f.code == cudaErrorMemoryAllocation ? RR_ERROR_OUT_OF_DEVICE_MEMORY : RR_ERROR_INTERNAL;
+}
+
+// ---------------------------------------------------------------------------
+struct BufInfo
+{
+    uint32_t kind   = 0;
+    uint32_t n      = 0;
+    uint32_t format = RR_CUDA_NODE_FORMAT_BINARY;
+    size_t   trailer_off = 0, wide_off = 0, tris_off = 0, xforms_off = 0, inst_off = 0;
+    bool     scene_wide = false;
+};
+
+struct Context;
+
+using Op = std::function<cudaError_t(cudaStream_t)>;
+
+struct CommandStream
+{
+    Context*        ctx      = nullptr;
+    bool            external = false;
+    cudaStream_t    stream   = nullptr;
+    std::vector<Op> ops;
+    cudaGraphExec_t graph      = nullptr;
+    size_t          graph_ops  = 0;
+    bool            graph_failed = false;
+    ~CommandStream()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+struct Event
+{
+    cudaEvent_t ev = nullptr;
+};
+
+struct DevicePtr
+{
+    uint8_t* base    = nullptr;
+    size_t   offset  = 0;
+    bool     managed = false;  // allocated by rrAllocateDeviceBuffer (owned)
+    size_t   size    = 0;
+    uint8_t* addr() const { return base + offset; }
+};
+
+struct Context
+{
+    int                    device   = 0;
+    int                    sm_count = 1;
+    cudaStream_t           stream   = nullptr;
+    DeviceWords*           words    = nullptr;
+    RRCudaTraversalOptions topts{};
+    uint32_t               wait_ms  = 600000;
+    bool                   graphs   = true;
+    std::map<uintptr_t, BufInfo> registry;
+    ~Context()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        if (words) cudaFree(words);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct DeviceGuard
+{
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+inline Context*       C(RRContext c) { return reinterpret_cast<Context*>(c); }
+inline CommandStream* S(RRCommandStream s) { return reinterpret_cast<CommandStream*>(s); }
+inline DevicePtr*     P(RRDevicePtr p) { return reinterpret_cast<DevicePtr*>(p); }
+inline Event*         E(RREvent e) { return reinterpret_cast<Event*>(e); }
+
+void record(CommandStream* cs, Op op)
+{
+    if (cs->external)
+    {
+        check(op(cs->stream), "enqueue");
+        return;
+    }
+    cs->ops.push_back(std::move(op));
+}
+
+struct BuildParams
+{
+    uint32_t format = RR_CUDA_NODE_FORMAT_WIDE8;
+    uint32_t bits   = 30;
+};
+
+// RRBuildOptions::backend_specific_info -> node format and key width.
+bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
+{
+    if (!o || !o->backend_specific_info) return true;
+    const RRCudaBuildOptions* c = reinterpret_cast<const RRCudaBuildOptions*>(o->backend_specific_info);
+    if (c->struct_size < sizeof(RRCudaBuildOptions)) return false;
+    if (c->node_format != RR_CUDA_NODE_FORMAT_BINARY && c->node_format != RR_CUDA_NODE_FORMAT_WIDE8) return false;
+    if (c->morton_bits != 0 && c->morton_bits != 30 && c->morton_bits != 63) return false;
+    bp.format = c->node_format;
+    bp.bits   = c->morton_bits == 63 ? 63 : 30;
+    return true;
+}
+
+// Validation of a triangle-mesh build input (reference radeonrays.cpp:242-299,
+// vlk/intersector.cpp:137-175).
+RRError check_mesh_input(const RRGeometryBuildInput* in, const RRTriangleMeshPrimitive** out, bool need_buffers)
+{
+    if (in->primitive_type != RR_PRIMITIVE_TYPE_TRIANGLE_MESH) return RR_ERROR_NOT_IMPLEMENTED;
+    if (in->primitive_count != 1 || !in->triangle_mesh_primitives) return RR_ERROR_INVALID_PARAMETER;
+    const RRTriangleMeshPrimitive* m = in->triangle_mesh_primitives;
+    if (need_buffers && m->triangle_count > 0 && (!m->vertices || !m->triangle_indices))
+        return RR_ERROR_INVALID_PARAMETER;
+    if (m->vertex_stride < 12 || (m->vertex_stride & 3u)) return RR_ERROR_INVALID_PARAMETER;
+    if (m->index_type != RR_INDEX_TYPE_UINT32 && m->index_type != RR_INDEX_TYPE_UINT16)
+        return RR_ERROR_INVALID_PARAMETER;
+    if (m->triangle_count >= (1u << 30)) return RR_ERROR_INVALID_PARAMETER;
+    *out = m;
+    return RR_SUCCESS;
+}
+
+// 3x4 affine inverse in double, rounded once to float.
+void inverse34(const float* m, float* out)
+{
+    double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    double A = e * i - f * h, B = -(d * i - f * g), Cc = d * h - e * g;
+    double det = a * A + b * B + c * Cc;
+    if (det == 0.0)
+    {
+        for (int k = 0; k < 12; ++k) out[k] = 0.f;
+        return;
+    }
+    double r = 1.0 / det;
+    double inv[9];
+    inv[0] = A * r;
+    inv[1] = -(b * i - c * h) * r;
+    inv[2] = (b * f - c * e) * r;
+    inv[3] = B * r;
+    inv[4] = (a * i - c * g) * r;
+    inv[5] = -(a * f - c * d) * r;
+    inv[6] = Cc * r;
+    inv[7] = -(a * h - b * g) * r;
+    inv[8] = (a * e - b * d) * r;
+    double tx = m[3], ty = m[7], tz = m[11];
+    for (int row = 0; row < 3; ++row)
+    {
+        out[row * 4 + 0] = (float)inv[row * 3 + 0];
+        out[row * 4 + 1] = (float)inv[row * 3 + 1];
+        out[row * 4 + 2] = (float)inv[row * 3 + 2];
+        out[row * 4 + 3] = (float)(-(inv[row * 3 + 0] * tx + inv[row * 3 + 1] * ty + inv[row * 3 + 2] * tz));
+    }
+}
+
+struct PinnedBlock
+{
+    void*  p = nullptr;
+    size_t n = 0;
+    explicit PinnedBlock(size_t bytes) : n(bytes)
+    {
+        if (bytes) check(cudaMallocHost(&p, bytes), "cudaMallocHost");
+    }
+    ~PinnedBlock()
+    {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+}  // namespace
+
+#define RR_TRY(...)                                                  \
+    try                                                              \
+    {                                                                \
+        __VA_ARGS__                                                  \
+    }                                                                \
+    catch (const CudaFail& f)                                        \
+    {                                                                \
+        return map_error(f);                                         \
+    }                                                                \
+    catch (const std::bad_alloc&)                                    \
+    {                                                                \
+        RR_LOG_ERROR("out of host memory");                          \
+        return RR_ERROR_OUT_OF_HOST_MEMORY;                          \
+    }                                                                \
+    catch (const std::exception& ex)                                 \
+    {                                                                \
+        RR_LOG_ERROR("%s", ex.what());                               \
+        return RR_ERROR_INTERNAL;                                    \
+    }                                                                \
+    catch (...)                                                      \
+    {                                                                \
+        return RR_ERROR_INTERNAL;                                    \
+    }
+
+extern "C" {
+
+RR_API RRError rrSetLogLevel(RRLogLevel log_level)
+{
+    if (log_level < RR_LOG_LEVEL_DEBUG || log_level > RR_LOG_LEVEL_OFF) return RR_ERROR_INVALID_PARAMETER;
+    g_log_level = log_level;
+    RR_LOG_INFO("rrSetLogLevel(%d)", (int)log_level);
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrSetLogFile(char const* filename)
+{
+    if (!filename) return RR_ERROR_INVALID_PARAMETER;
+    FILE* f = std::fopen(filename, "a");
+    if (!f) return RR_ERROR_INTERNAL;
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    if (g_log_file) std::fclose(g_log_file);
+    g_log_file = f;
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrCreateContext(uint32_t api_version, RRApi api, RRContext* context)
+{
+    RR_LOG_INFO("rrCreateContext(%u)", api_version);
+    if (!context) return RR_ERROR_INVALID_PARAMETER;
+    if (api != RR_API_CUDA) return RR_ERROR_UNSUPPORTED_API;
+    RR_TRY({
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        {
+            cudaGetLastError();
+            RR_LOG_ERROR("no CUDA device");
+            return RR_ERROR_INTERNAL;
+        }
+        std::unique_ptr<Context> c(new Context);
+        check(cudaGetDevice(&c->device), "cudaGetDevice");
+        check(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device), "sm count");
+        check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+        check(cudaMalloc(&c->words, sizeof(DeviceWords)), "cudaMalloc words");
+        check(cudaMemset(c->words, 0, sizeof(DeviceWords)), "memset words");
+        c->topts.struct_size = sizeof(RRCudaTraversalOptions);
+        c->topts.traversal   = RR_CUDA_TRAVERSAL_AUTO;
+        const char* g        = std::getenv("RR_CUDA_GRAPHS");
+        c->graphs            = !(g && g[0] == '0');
+        *context             = reinterpret_cast<RRContext>(c.release());
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrDestroyContext(RRContext context)
+{
+    if (!context) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        delete C(context);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrGetGeometryBuildMemoryRequirements(RRContext                   context,
+                                                    const RRGeometryBuildInput* build_input,
+                                                    const RRBuildOptions*       build_options,
+                                                    RRMemoryRequirements*       memory_requirements)
+{
+    if (!context || !build_input || !memory_requirements) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        const RRTriangleMeshPrimitive* m = nullptr;
+        RRError                        e = check_mesh_input(build_input, &m, false);
+        if (e != RR_SUCCESS) return e;
+        BuildParams bp;
+        if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
+        GeomLayout L                                      = geom_layout(m->triangle_count, bp.format, bp.bits);
+        memory_requirements->result_buffer_size           = L.total;
+        memory_requirements->temporary_build_buffer_size  = L.s_total;
+        memory_requirements->temporary_update_buffer_size = 0;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCmdBuildGeometry(RRContext                   context,
+                                  RRBuildOperation            build_operation,
+                                  const RRGeometryBuildInput* build_input,
+                                  const RRBuildOptions*       build_options,
+                                  RRDevicePtr                 temporary_buffer,
+                                  RRDevicePtr                 geometry_buffer,
+                                  RRCommandStream             command_stream)
+{
+    RR_LOG_INFO("rrCmdBuildGeometry");
+    if (!context || !command_stream || !build_input) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        const RRTriangleMeshPrimitive* m = nullptr;
+        RRError                        e = check_mesh_input(build_input, &m, true);
+        if (e != RR_SUCCESS) return e;
+        if (build_operation == RR_BUILD_OPERATION_UPDATE) return RR_ERROR_NOT_IMPLEMENTED;
+        if (build_operation != RR_BUILD_OPERATION_BUILD) return RR_ERROR_INVALID_PARAMETER;
+        if (!geometry_buffer || (!temporary_buffer && m->triangle_count > 0)) return RR_ERROR_INVALID_PARAMETER;
+        BuildParams bp;
+        if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
+        Context*   ctx = C(context);
+        DeviceGuard g(ctx->device);
+        GeomLayout L   = geom_layout(m->triangle_count, bp.format, bp.bits);
+        MeshArgs   ma;
+        ma.vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
+        ma.stride_floats = m->vertex_stride >> 2;
+        ma.indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
+        ma.index16       = m->index_type == RR_INDEX_TYPE_UINT16;
+        ma.n             = m->triangle_count;
+        uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
+        uint8_t*     result  = P(geometry_buffer)->addr();
+        DeviceWords* words   = ctx->words;
+        const int    sms     = ctx->sm_count;
+        record(S(command_stream), [=](cudaStream_t s) { return launch_build_mesh(ma, L, scratch, result, words, sms, s); });
+        BufInfo bi;
+        bi.kind        = kKindGeom;
+        bi.n           = L.n;
+        bi.format      = L.format;
+        bi.trailer_off = L.trailer_off;
+        bi.wide_off    = L.wide_off;
+        bi.tris_off    = L.tris_off;
+        ctx->registry[(uintptr_t)result] = bi;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrGetSceneBuildMemoryRequirements(RRContext                context,
+                                                 const RRSceneBuildInput* build_input,
+                                                 const RRBuildOptions*    build_options,
+                                                 RRMemoryRequirements*    memory_requirements)
+{
+    (void)build_options;
+    if (!context || !build_input || !memory_requirements) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        SceneLayout L                                     = scene_layout(build_input->instance_count);
+        memory_requirements->result_buffer_size           = L.total;
+        memory_requirements->temporary_build_buffer_size  = L.s_total;
+        memory_requirements->temporary_update_buffer_size = 0;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCmdBuildScene(RRContext                context,
+                               const RRSceneBuildInput* build_input,
+                               const RRBuildOptions*    build_options,
+                               RRDevicePtr              temporary_buffer,
+                               RRDevicePtr              scene_buffer,
+                               RRCommandStream          command_stream)
+{
+    (void)build_options;
+    RR_LOG_INFO("rrCmdBuildScene");
+    if (!context || !command_stream || !build_input) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        const uint32_t n = build_input->instance_count;
+        if (n > 0 && !build_input->instances) return RR_ERROR_INVALID_PARAMETER;
+        if (n >= (1u << 24)) return RR_ERROR_INVALID_PARAMETER;
+        if (!scene_buffer || (!temporary_buffer && n > 0)) return RR_ERROR_INVALID_PARAMETER;
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        SceneLayout L = scene_layout(n);
+        for (uint32_t i = 0; i < n; ++i)
+            if (!build_input->instances[i].geometry) return RR_ERROR_INVALID_PARAMETER;
+        // Host staging: [xforms 2n x 12 floats: inverse, forward][InstanceDesc n].
+        const size_t xbytes = (size_t)n * 2 * 48, ibytes = (size_t)n * sizeof(InstanceDesc);
+        auto         stage  = std::make_shared<PinnedBlock>(xbytes + ibytes);
+        float*       xf     = reinterpret_cast<float*>(stage->p);
+        InstanceDesc* id    = reinterpret_cast<InstanceDesc*>(reinterpret_cast<uint8_t*>(stage->p) + xbytes);
+        bool          all_wide = n > 0;
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            const RRInstance& in = build_input->instances[i];
+            inverse34(&in.transform[0][0], xf + 24ull * i);
+            std::memcpy(xf + 24ull * i + 12, &in.transform[0][0], 48);
+            uint8_t* blas = P(in.geometry)->addr();
+            auto     it   = ctx->registry.find((uintptr_t)blas);
+            InstanceDesc d{};
+            d.blas = (uint64_t)(uintptr_t)blas;
+            if (it != ctx->registry.end() && it->second.kind == kKindGeom)
+            {
+                d.leaf_count = it->second.n;
+                if (it->second.format == RR_CUDA_NODE_FORMAT_WIDE8 && it->second.n > 0)
+                {
+                    d.wide_nodes = (uint64_t)(uintptr_t)(blas + it->second.wide_off);
+                    d.wide_tris  = (uint64_t)(uintptr_t)(blas + it->second.tris_off);
+                }
+                else
+                    all_wide = false;
+                d.flags = 1;  // known geometry
+            }
+            else
+            {
+                d.leaf_count = 0xffffffffu;  // unknown: traverse binary nodes from the root
+                all_wide     = false;
+            }
+            id[i] = d;
+        }
+        uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
+        uint8_t*     result  = P(scene_buffer)->addr();
+        DeviceWords* words   = ctx->words;
+        record(S(command_stream), [=](cudaStream_t s) -> cudaError_t {
+            cudaError_t e = cudaSuccess;
+            if (n > 0)
+            {
+                e = cudaMemcpyAsync(result + L.xforms_off, stage->p, xbytes, cudaMemcpyHostToDevice, s);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(result + L.inst_off, reinterpret_cast<uint8_t*>(stage->p) + xbytes, ibytes,
+                                        cudaMemcpyHostToDevice, s);
+                if (e != cudaSuccess) return e;
+            }
+            SceneBuildArgs sa;
+            sa.inst    = reinterpret_cast<const InstanceDesc*>(result + L.inst_off);
+            sa.forward = reinterpret_cast<const float*>(result + L.xforms_off);
+            sa.n       = n;
+            return launch_build_scene(sa, L, scratch, result, words, s);
+        });
+        BufInfo bi;
+        bi.kind        = kKindScene;
+        bi.n           = n;
+        bi.trailer_off = L.trailer_off;
+        bi.xforms_off  = L.xforms_off;
+        bi.inst_off    = L.inst_off;
+        bi.scene_wide  = all_wide;
+        ctx->registry[(uintptr_t)result] = bi;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCmdIntersect(RRContext              context,
+                              RRDevicePtr            scene_buffer,
+                              RRIntersectQuery       query,
+                              RRDevicePtr            rays,
+                              uint32_t               ray_count,
+                              RRDevicePtr            indirect_ray_count,
+                              RRIntersectQueryOutput query_output,
+                              RRDevicePtr            hits,
+                              RRDevicePtr            scratch,
+                              RRCommandStream        command_stream)
+{
+    RR_LOG_INFO("rrCmdIntersect");
+    if (!context || !scene_buffer || !rays || !hits || !scratch || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    if (query != RR_INTERSECT_QUERY_CLOSEST && query != RR_INTERSECT_QUERY_ANY) return RR_ERROR_INVALID_PARAMETER;
+    if (query_output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && query_output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+        return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        uint8_t*    bvh = P(scene_buffer)->addr();
+        TraceArgs   a{};
+        a.bvh           = bvh;
+        a.rays          = P(rays)->addr();
+        a.ray_count     = ray_count;
+        a.indirect      = indirect_ray_count ? reinterpret_cast<const uint32_t*>(P(indirect_ray_count)->addr()) : nullptr;
+        a.hits          = P(hits)->addr();
+        a.scratch       = P(scratch)->addr();
+        a.scratch_bytes = trace_scratch_bytes(ray_count);
+        a.query         = query;
+        a.output        = query_output;
+        a.words         = ctx->words;
+        a.collect_stats = ctx->topts.collect_stats ? 1 : 0;
+        a.block_size    = (int)ctx->topts.block_size;
+        a.blocks_per_sm = (int)ctx->topts.blocks_per_sm;
+        a.sm_count      = ctx->sm_count;
+        auto     it     = ctx->registry.find((uintptr_t)bvh);
+        BufInfo  bi;
+        if (it != ctx->registry.end()) bi = it->second;
+        const uint32_t trav = ctx->topts.traversal;
+        if (bi.kind == kKindScene)
+        {
+            SceneTraceArgs sa;
+            sa.base       = a;
+            sa.base.empty = bi.n == 0;
+            sa.xforms     = reinterpret_cast<const float*>(bvh + bi.xforms_off);
+            sa.inst       = reinterpret_cast<const InstanceDesc*>(bvh + bi.inst_off);
+            sa.inst_count = bi.n;
+            sa.use_wide   = bi.scene_wide && trav != RR_CUDA_TRAVERSAL_BINARY;
+            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_scene(sa, s); });
+            return RR_SUCCESS;
+        }
+        // Geometry (registered) or an unknown buffer, traversed as binary nodes
+        // from the root like the reference (vlk/intersector.cpp:290).
+        a.empty             = (bi.kind == kKindGeom && bi.n == 0);
+        const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
+        if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
+        {
+            a.wide_nodes = reinterpret_cast<const WideNode*>(bvh + bi.wide_off);
+            a.wide_tris  = reinterpret_cast<const WideTri*>(bvh + bi.tris_off);
+            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_wide(a, s); });
+        }
+        else
+            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_binary(a, s); });
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrGetTraceMemoryRequirements(RRContext context, uint32_t ray_count, size_t* scratch_size)
+{
+    if (!context || !scratch_size || !ray_count) return RR_ERROR_INVALID_PARAMETER;
+    *scratch_size = trace_scratch_bytes(ray_count);
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrAllocateCommandStream(RRContext context, RRCommandStream* command_stream)
+{
+    if (!context || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        CommandStream* cs = new CommandStream;
+        cs->ctx           = C(context);
+        cs->stream        = C(context)->stream;
+        *command_stream   = reinterpret_cast<RRCommandStream>(cs);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrReleaseCommandStream(RRContext context, RRCommandStream command_stream)
+{
+    if (!context || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    if (S(command_stream)->external) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        delete S(command_stream);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrSumbitCommandStream(RRContext context, RRCommandStream command_stream, RREvent wait_event,
+                                     RREvent* out_event)
+{
+    RR_LOG_INFO("rrSumbitCommandStream");
+    if (!context || !command_stream || !out_event) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*       ctx = C(context);
+        CommandStream* cs  = S(command_stream);
+        DeviceGuard    g(ctx->device);
+        cudaStream_t   st = cs->stream;
+        if (wait_event) check(cudaStreamWaitEvent(st, E(wait_event)->ev, 0), "cudaStreamWaitEvent");
+        if (!cs->external)
+        {
+            bool done = false;
+            if (ctx->graphs && !cs->graph_failed && cs->ops.size() > 1)
+            {
+                if (!cs->graph || cs->graph_ops != cs->ops.size())
+                {
+                    if (cs->graph)
+                    {
+                        cudaGraphExecDestroy(cs->graph);
+                        cs->graph = nullptr;
+                    }
+                    cudaGraph_t graph = nullptr;
+                    bool        ok    = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+                    for (auto& op : cs->ops)
+                        if (ok && op(st) != cudaSuccess) ok = false;
+                    cudaError_t ec = cudaStreamEndCapture(st, &graph);
+                    ok             = ok && ec == cudaSuccess && graph;
+                    if (ok && cudaGraphInstantiate(&cs->graph, graph, 0) != cudaSuccess) ok = false;
+                    if (graph) cudaGraphDestroy(graph);
+                    cudaGetLastError();
+                    if (!ok)
+                    {
+                        cs->graph_failed = true;
+                        if (cs->graph) cudaGraphExecDestroy(cs->graph);
+                        cs->graph = nullptr;
+                    }
+                    else
+                        cs->graph_ops = cs->ops.size();
+                }
+                if (cs->graph)
+                {
+                    check(cudaGraphLaunch(cs->graph, st), "cudaGraphLaunch");
+                    done = true;
+                }
+            }
+            if (!done)
+                for (auto& op : cs->ops) check(op(st), "command");
+        }
+        std::unique_ptr<Event> ev(new Event);
+        check(cudaEventCreateWithFlags(&ev->ev, cudaEventDisableTiming), "cudaEventCreate");
+        check(cudaEventRecord(ev->ev, st), "cudaEventRecord");
+        *out_event = reinterpret_cast<RREvent>(ev.release());
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrReleaseEvent(RRContext context, RREvent event)
+{
+    if (!context || !event) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        cudaEventDestroy(E(event)->ev);
+        delete E(event);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrWaitEvent(RRContext context, RREvent event)
+{
+    if (!context || !event) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        const auto  t0 = std::chrono::steady_clock::now();
+        for (uint64_t spin = 0;; ++spin)
+        {
+            cudaError_t e = cudaEventQuery(E(event)->ev);
+            if (e == cudaSuccess) return RR_SUCCESS;
+            if (e != cudaErrorNotReady) throw CudaFail(e, "cudaEventQuery");
+            const auto ms =
+                std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if ((uint64_t)ms > ctx->wait_ms)
+            {
+                RR_LOG_ERROR("rrWaitEvent: timed out after %u ms", ctx->wait_ms);
+                return RR_ERROR_INTERNAL;
+            }
+            if (spin < 2000)
+                std::this_thread::yield();
+            else
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    })
+}
+
+RR_API RRError rrReleaseDevicePtr(RRContext context, RRDevicePtr ptr)
+{
+    if (!context || !ptr) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        DevicePtr* p = P(ptr);
+        if (p->managed && p->base) cudaFree(p->base);
+        delete p;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrReleaseExternalCommandStream(RRContext context, RRCommandStream command_stream)
+{
+    if (!context || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    delete S(command_stream);
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrGetDevicePtrFromCudaPtr(RRContext context, void* cuda_ptr, size_t offset, RRDevicePtr* device_ptr)
+{
+    if (!context || !cuda_ptr || !device_ptr) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DevicePtr* p = new DevicePtr;
+        p->base      = reinterpret_cast<uint8_t*>(cuda_ptr);
+        p->offset    = offset;
+        *device_ptr  = reinterpret_cast<RRDevicePtr>(p);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrGetCudaPtrFromDevicePtr(RRContext context, RRDevicePtr device_ptr, void** cuda_ptr)
+{
+    if (!context || !device_ptr || !cuda_ptr) return RR_ERROR_INVALID_PARAMETER;
+    *cuda_ptr = P(device_ptr)->addr();
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrGetCommandStreamFromCudaStream(RRContext context, void* cuda_stream, RRCommandStream* command_stream)
+{
+    if (!context || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        CommandStream* cs = new CommandStream;
+        cs->ctx           = C(context);
+        cs->external      = true;
+        cs->stream        = reinterpret_cast<cudaStream_t>(cuda_stream);
+        *command_stream   = reinterpret_cast<RRCommandStream>(cs);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrAllocateDeviceBuffer(RRContext context, size_t size, RRDevicePtr* device_ptr)
+{
+    if (!context || !size || !device_ptr) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        void*       mem = nullptr;
+        check(cudaMallocManaged(&mem, size), "cudaMallocManaged");
+        DevicePtr* p = new DevicePtr;
+        p->base      = reinterpret_cast<uint8_t*>(mem);
+        p->managed   = true;
+        p->size      = size;
+        *device_ptr  = reinterpret_cast<RRDevicePtr>(p);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrMapDevicePtr(RRContext context, RRDevicePtr device_ptr, void** mapping_ptr)
+{
+    if (!context || !device_ptr || !mapping_ptr) return RR_ERROR_INVALID_PARAMETER;
+    DevicePtr* p = P(device_ptr);
+    if (!p->managed) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        DeviceGuard g(C(context)->device);
+        // Managed memory: make prior device work visible before the host reads.
+        check(cudaStreamSynchronize(C(context)->stream), "sync");
+        check(cudaDeviceSynchronize(), "sync");
+        *mapping_ptr = p->addr();
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrUnmapDevicePtr(RRContext context, RRDevicePtr device_ptr, void** mapping_ptr)
+{
+    if (!context || !device_ptr) return RR_ERROR_INVALID_PARAMETER;
+    if (!P(device_ptr)->managed) return RR_ERROR_INVALID_PARAMETER;
+    if (mapping_ptr) *mapping_ptr = nullptr;
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversalOptions* options)
+{
+    if (!context || !options || options->struct_size < sizeof(RRCudaTraversalOptions)) return RR_ERROR_INVALID_PARAMETER;
+    if (options->traversal > RR_CUDA_TRAVERSAL_WIDE) return RR_ERROR_INVALID_PARAMETER;
+    if (options->block_size && (options->block_size % 32 || options->block_size > 1024)) return RR_ERROR_INVALID_PARAMETER;
+    C(context)->topts = *options;
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaGetTraversalOptions(RRContext context, RRCudaTraversalOptions* options)
+{
+    if (!context || !options) return RR_ERROR_INVALID_PARAMETER;
+    *options = C(context)->topts;
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaGetDeviceErrors(RRContext context, uint32_t* error_bits)
+{
+    if (!context || !error_bits) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        check(cudaDeviceSynchronize(), "sync");
+        uint32_t v = 0;
+        check(cudaMemcpy(&v, &ctx->words->error_bits, 4, cudaMemcpyDeviceToHost), "read error word");
+        check(cudaMemset(&ctx->words->error_bits, 0, 4), "clear error word");
+        *error_bits = v;
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCudaGetTraversalStats(RRContext context, RRCudaTraversalStats* stats)
+{
+    if (!context || !stats) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        check(cudaDeviceSynchronize(), "sync");
+        DeviceWords w;
+        check(cudaMemcpy(&w, ctx->words, sizeof(w), cudaMemcpyDeviceToHost), "read stats");
+        check(cudaMemset(&ctx->words->rays, 0, 3 * sizeof(unsigned long long)), "clear stats");
+        stats->rays             = w.rays;
+        stats->node_fetches     = w.node_fetches;
+        stats->triangle_fetches = w.tri_fetches;
+        stats->node_bytes       = 0;
+        stats->triangle_bytes   = sizeof(WideTri);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds)
+{
+    if (!context) return RR_ERROR_INVALID_PARAMETER;
+    C(context)->wait_ms = milliseconds;
+    return RR_SUCCESS;
+}
+
+}  // extern "C"

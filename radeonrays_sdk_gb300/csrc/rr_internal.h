@@ -1,0 +1,212 @@
+// rr_internal.h -- data layouts and kernel entry points shared by the host
+// runtime (api.cu) and the CUDA kernels of the GB300 RadeonRays build.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/radeonrays.h"
+#include "../../include/radeonrays_cuda.h"
+
+namespace rr
+{
+constexpr uint32_t kInvalid     = 0xffffffffu;  // vlk/kernels/common.h:20 RR_INVALID_ADDR
+constexpr uint32_t kSentinel    = 0xfffffffeu;  // vlk/kernels/isect_2l.comp:28
+constexpr uint32_t kMagic       = 0x52524742u;  // "RRGB": trailer tag of a result buffer
+constexpr uint32_t kVersion     = 1;
+constexpr uint32_t kKindGeom    = 1;
+constexpr uint32_t kKindScene   = 2;
+constexpr size_t   kAlign       = 256;
+constexpr uint32_t kMaxInstancesRef = 2048;  // vlk/intersector.cpp:38 (accepted; larger counts also work)
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// 64-byte binary node in the reference layout (vlk/kernels/bvh2.h:25-35).
+// Internal nodes [0, N-2], leaves [N-1, 2N-2]; a leaf has child0 = invalid,
+// child1 = primitive id and its triangle's vertices in the first three vec3.
+struct __align__(16) BvhNode
+{
+    float    a0[3];  // aabb0_min_or_v0
+    uint32_t child0;
+    float    a1[3];  // aabb0_max_or_v1
+    uint32_t child1;
+    float    b0[3];  // aabb1_min_or_v2
+    uint32_t parent;
+    float    b1[3];  // aabb1_max_or_v3
+    uint32_t update;
+};
+static_assert(sizeof(BvhNode) == 64, "node layout");
+
+// 8-wide node with 8-bit child bounds (80 bytes, five 16-byte words).
+// Child box of slot i on axis a: [fma(qlo, 2^e, p), fma(qhi, 2^e, p)], rounded
+// outward at build time so it contains the exact child box.
+struct __align__(16) WideNode
+{
+    float    p[3];       // quantisation origin
+    uint8_t  e[3];       // biased exponents: scale = 2^(e - 127)
+    uint8_t  imask;      // bit i: slot i is an internal child
+    uint32_t child_base; // index of the first internal child (children are contiguous)
+    uint32_t tri_base;   // index of the first triangle of this node's leaf slots
+    uint8_t  meta[8];    // internal: child offset; leaf: (count << 5) | tri offset; empty: 0
+    uint8_t  qlo[3][8];  // [axis][slot]
+    uint8_t  qhi[3][8];
+};
+static_assert(sizeof(WideNode) == 80, "wide node layout");
+
+// Triangle of the wide path: three float4 with the primitive id in v0.w.
+struct __align__(16) WideTri
+{
+    float v0[3];
+    uint32_t prim;
+    float v1[3];
+    uint32_t pad1;
+    float v2[3];
+    uint32_t pad2;
+};
+static_assert(sizeof(WideTri) == 48, "triangle layout");
+
+// Trailer written after the binary node array of every result buffer; it
+// makes the buffer self-describing (kind, counts, section offsets).
+struct __align__(16) Trailer
+{
+    uint32_t magic;
+    uint32_t version;
+    uint32_t kind;          // kKindGeom / kKindScene
+    uint32_t node_format;   // RRCudaNodeFormat
+    uint32_t leaf_count;    // triangles (geometry) or instances (scene)
+    uint32_t node_count;    // binary nodes
+    uint32_t wide_count;    // wide nodes written (device)
+    uint32_t wide_tri_count;// wide triangles written (device)
+    uint64_t wide_nodes_off;
+    uint64_t wide_tris_off;
+    uint64_t wide_capacity;
+    uint64_t tri_capacity;
+    uint32_t bounds[8];     // mesh/scene box in the order-preserving uint encoding
+    uint32_t morton_bits;
+    uint32_t pad[3];
+    uint64_t xforms_off;    // scene: transforms [inverse, forward] per instance
+    uint64_t inst_off;      // scene: InstanceDesc per instance
+    uint64_t reserved[16];
+};
+static_assert(sizeof(Trailer) == 256, "trailer layout");
+
+// Per-instance record of a scene buffer: where the instance's BLAS lives.
+struct __align__(16) InstanceDesc
+{
+    uint64_t blas;       // device address of the BLAS result buffer (binary nodes at offset 0)
+    uint64_t wide_nodes; // device address of its wide nodes, 0 if it has none
+    uint64_t wide_tris;  // device address of its wide triangles
+    uint32_t leaf_count;
+    uint32_t flags;
+};
+static_assert(sizeof(InstanceDesc) == 32, "instance layout");
+
+// Result-buffer layout of a geometry build with N triangles.
+struct GeomLayout
+{
+    uint32_t n;
+    uint32_t format;
+    uint32_t morton_bits;
+    size_t   nodes_bytes;
+    size_t   trailer_off;
+    size_t   wide_off;
+    size_t   wide_capacity;
+    size_t   tris_off;
+    size_t   tri_capacity;
+    size_t   total;
+    // scratch
+    size_t   s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_queue, s_queue_bytes,
+        s_total;
+    uint32_t sort_tiles, sort_passes;
+};
+GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits);
+
+struct SceneLayout
+{
+    uint32_t n;
+    size_t   nodes_bytes;
+    size_t   xforms_off;
+    size_t   trailer_off;
+    size_t   inst_off;
+    size_t   total;
+    size_t   s_bounds, s_boxes, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_total;
+    uint32_t sort_tiles, sort_passes;
+};
+SceneLayout scene_layout(uint32_t n);
+
+// Context-wide device words.
+struct DeviceWords
+{
+    uint32_t error_bits;
+    uint32_t pad[3];
+    unsigned long long rays;
+    unsigned long long node_fetches;
+    unsigned long long tri_fetches;
+};
+
+// ---- kernel launchers (all enqueue on `s`, return the launch error) ------
+struct MeshArgs
+{
+    const float* vertices;
+    uint64_t     stride_floats;
+    const void*  indices;
+    int          index16;
+    uint32_t     n;
+};
+
+cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
+                              DeviceWords* words, int sm_count, cudaStream_t s);
+
+// Sort (codes, identity values) stably; bits = 30 (uint32 keys) or 63 (uint64).
+// Returns in *sorted_in_alt whether the result is in the alt buffers.
+cudaError_t launch_radix_sort(void* codes, void* codes_alt, uint32_t* idx, uint32_t* idx_alt, uint32_t n,
+                              int key_bits, uint8_t* sort_scratch, uint32_t tiles, DeviceWords* words,
+                              cudaStream_t s, bool* sorted_in_alt);
+size_t   radix_sort_scratch_bytes(uint32_t n, int key_bits, uint32_t* tiles, uint32_t* passes);
+
+struct TraceArgs
+{
+    const uint8_t*  bvh;          // result buffer base (binary nodes at offset 0)
+    const WideNode* wide_nodes;   // wide path
+    const WideTri*  wide_tris;
+    const uint8_t*  rays;         // RRRay[]
+    uint32_t        ray_count;
+    const uint32_t* indirect;     // optional device count
+    void*           hits;
+    uint8_t*        scratch;
+    size_t          scratch_bytes;
+    int             query;        // RRIntersectQuery
+    int             output;       // RRIntersectQueryOutput
+    int             empty;        // geometry with no triangles
+    DeviceWords*    words;
+    int             collect_stats;
+    int             block_size;
+    int             blocks_per_sm;
+    int             sm_count;
+};
+cudaError_t launch_trace_binary(const TraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_wide(const TraceArgs& a, cudaStream_t s);
+
+struct SceneTraceArgs
+{
+    TraceArgs           base;       // bvh = TLAS buffer
+    const float*        xforms;     // [inverse, forward] 12 floats each
+    const InstanceDesc* inst;
+    uint32_t            inst_count;
+    int                 use_wide;
+};
+cudaError_t launch_trace_scene(const SceneTraceArgs& a, cudaStream_t s);
+
+struct SceneBuildArgs
+{
+    const InstanceDesc* inst;      // device: per instance BLAS pointers
+    const float*        forward;   // device: 12 floats per instance
+    uint32_t            n;
+};
+cudaError_t launch_build_scene(const SceneBuildArgs& a, const SceneLayout& L, uint8_t* scratch, uint8_t* result,
+                               DeviceWords* words, cudaStream_t s);
+
+size_t trace_scratch_bytes(uint32_t ray_count);
+
+}  // namespace rr

@@ -1,0 +1,370 @@
+// wide.cu -- collapse of the binary LBVH into 8-wide nodes with 8-bit child
+// bounds (the "chosen" traversal format; no reference counterpart: the
+// reference traverses its binary nodes only, vlk/kernels/isect.comp).
+//
+// Collapse: top-down and level-synchronous.  A work item is (binary node b,
+// wide slot w).  The children of w start as b's two children; the internal
+// child with the largest surface area is replaced by its two children until
+// there are 8 children or only triangles remain.  Internal children become
+// the next level's work items; triangle children are written to a contiguous
+// 48-byte triangle array.  Every level is one launch whose item count is read
+// on the device, so the whole build records into a stream without a host
+// round trip.
+//
+// Quantisation: per node, origin p = union box minimum; per axis the smallest
+// power of two 2^e with ceil((hi - p) / 2^e) <= 255.  Child bounds are
+// qlo = floor(rd(lo - p) / 2^e), qhi = ceil(ru(hi - p) / 2^e), so the decoded
+// box fma(q, 2^e, p) contains the exact fp32 child box (round-to-nearest is
+// monotonic and the bounds are floats).  A traversal slab test on the decoded
+// box therefore never rejects a ray that the exact box accepts.
+#include <algorithm>
+
+#include "rr_internal.h"
+
+namespace rr
+{
+namespace
+{
+constexpr int kMaxLevels = 66;
+
+struct CollapseCtl
+{
+    uint32_t wide_count;
+    uint32_t tri_count;
+    uint32_t pad[2];
+    uint32_t level_count[kMaxLevels + 2];
+};
+
+struct Item
+{
+    uint32_t b, w;
+};
+
+struct Bx
+{
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Bx node_union(const BvhNode& nd)
+{
+    Bx r;
+    if (nd.child0 != kInvalid)
+    {
+        r.lo[0] = fminf(nd.a0[0], nd.b0[0]);
+        r.lo[1] = fminf(nd.a0[1], nd.b0[1]);
+        r.lo[2] = fminf(nd.a0[2], nd.b0[2]);
+        r.hi[0] = fmaxf(nd.a1[0], nd.b1[0]);
+        r.hi[1] = fmaxf(nd.a1[1], nd.b1[1]);
+        r.hi[2] = fmaxf(nd.a1[2], nd.b1[2]);
+    }
+    else
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            r.lo[k] = fminf(fminf(nd.a0[k], nd.a1[k]), nd.b0[k]);
+            r.hi[k] = fmaxf(fmaxf(nd.a0[k], nd.a1[k]), nd.b0[k]);
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ float half_area(const Bx& b)
+{
+    float x = b.hi[0] - b.lo[0], y = b.hi[1] - b.lo[1], z = b.hi[2] - b.lo[2];
+    return x * y + y * z + z * x;
+}
+
+__device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
+{
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    float4        a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+    BvhNode       n;
+    n.a0[0] = a.x;
+    n.a0[1] = a.y;
+    n.a0[2] = a.z;
+    n.child0 = __float_as_uint(a.w);
+    n.a1[0] = b.x;
+    n.a1[1] = b.y;
+    n.a1[2] = b.z;
+    n.child1 = __float_as_uint(b.w);
+    n.b0[0] = c.x;
+    n.b0[1] = c.y;
+    n.b0[2] = c.z;
+    n.parent = __float_as_uint(c.w);
+    n.b1[0] = d.x;
+    n.b1[1] = d.y;
+    n.b1[2] = d.z;
+    n.update = __float_as_uint(d.w);
+    return n;
+}
+
+// Warp-aggregated atomicAdd over a full warp (all 32 lanes must call it):
+// every lane adds v and gets its own offset.
+__device__ __forceinline__ uint32_t warp_add(uint32_t* ctr, uint32_t v)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t  x    = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+    uint32_t       base  = 0;
+    if (lane == 31 && total) base = atomicAdd(ctr, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + x - v;
+}
+
+// Exponent e (biased) of the smallest power of two s with ceil(ext / s) <= 255.
+__device__ __forceinline__ int pick_exp(float lo, float hi)
+{
+    float    ext = __fsub_ru(hi, lo);
+    float    s   = __fdiv_ru(ext, 255.f);
+    uint32_t u   = __float_as_uint(s);
+    int      ex  = (int)((u >> 23) & 0xffu);
+    if (ex == 0) ex = 1;  // zero or subnormal extent: 2^-126
+    else if (u & 0x7fffffu) ex += 1;
+    while (ex < 253)
+    {
+        float inv = __uint_as_float((uint32_t)(254 - ex) << 23);  // 2^(127-ex)
+        if (ceilf(__fmul_ru(ext, inv)) <= 255.f) break;
+        ++ex;
+    }
+    return ex;
+}
+
+__global__ void k_collapse_init(const BvhNode* nodes, uint32_t n, CollapseCtl* ctl, Item* q0, WideNode* wn,
+                                WideTri* wt)
+{
+    if (threadIdx.x != 0) return;
+    for (int i = 0; i < kMaxLevels + 2; ++i) ctl->level_count[i] = 0;
+    if (n == 1)
+    {
+        // A one-triangle mesh: one wide node with a single triangle slot.
+        BvhNode  lf = nodes[0];
+        WideNode w{};
+        Bx       b = node_union(lf);
+        for (int k = 0; k < 3; ++k)
+        {
+            w.p[k] = b.lo[k];
+            int e  = pick_exp(b.lo[k], b.hi[k]);
+            w.e[k] = (uint8_t)e;
+            float inv = __uint_as_float((uint32_t)(254 - e) << 23);
+            w.qlo[k][0] = 0;
+            w.qhi[k][0] = (uint8_t)min(255.f, ceilf(__fmul_ru(__fsub_ru(b.hi[k], b.lo[k]), inv)));
+        }
+        w.imask      = 0;
+        w.child_base = 0;
+        w.tri_base   = 0;
+        w.meta[0]    = (uint8_t)((1u << 5) | 0u);
+        wn[0]        = w;
+        WideTri t;
+        t.v0[0] = lf.a0[0];
+        t.v0[1] = lf.a0[1];
+        t.v0[2] = lf.a0[2];
+        t.prim  = lf.child1;
+        t.v1[0] = lf.a1[0];
+        t.v1[1] = lf.a1[1];
+        t.v1[2] = lf.a1[2];
+        t.pad1  = 0;
+        t.v2[0] = lf.b0[0];
+        t.v2[1] = lf.b0[1];
+        t.v2[2] = lf.b0[2];
+        t.pad2  = 0;
+        wt[0]   = t;
+        ctl->wide_count = 1;
+        ctl->tri_count  = 1;
+        return;
+    }
+    q0[0]              = Item{0u, 0u};
+    ctl->level_count[0] = 1;
+    ctl->wide_count    = 1;
+    ctl->tri_count     = 0;
+}
+
+__global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restrict__ nodes, int level,
+                                                        CollapseCtl* ctl, const Item* __restrict__ qin,
+                                                        Item* __restrict__ qout, WideNode* wn, WideTri* wt,
+                                                        uint32_t wide_capacity, uint32_t tri_capacity,
+                                                        DeviceWords* words)
+{
+    const uint32_t count = *((volatile uint32_t*)&ctl->level_count[level]);
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < ((count + 31u) & ~31u);
+         it += gridDim.x * blockDim.x)
+    {
+        const bool active = it < count;
+        uint32_t   ch[8];
+        Bx         cb[8];
+        bool       cint[8];
+        int        nc = 0;
+        Item       item{0, 0};
+        if (active)
+        {
+            item          = qin[it];
+            BvhNode root  = load_node(nodes, item.b);
+            ch[0]         = root.child0;
+            ch[1]         = root.child1;
+            nc            = 2;
+            for (int k = 0; k < 2; ++k)
+            {
+                BvhNode c = load_node(nodes, ch[k]);
+                cb[k]     = node_union(c);
+                cint[k]   = c.child0 != kInvalid;
+            }
+            while (nc < 8)
+            {
+                int   best = -1;
+                float ba   = -1.f;
+                for (int k = 0; k < nc; ++k)
+                    if (cint[k])
+                    {
+                        float a = half_area(cb[k]);
+                        if (a > ba)
+                        {
+                            ba   = a;
+                            best = k;
+                        }
+                    }
+                if (best < 0) break;
+                BvhNode  nd = load_node(nodes, ch[best]);
+                uint32_t l = nd.child0, r = nd.child1;
+                BvhNode  ln = load_node(nodes, l), rn = load_node(nodes, r);
+                ch[best]   = l;
+                cb[best]   = node_union(ln);
+                cint[best] = ln.child0 != kInvalid;
+                ch[nc]     = r;
+                cb[nc]     = node_union(rn);
+                cint[nc]   = rn.child0 != kInvalid;
+                ++nc;
+            }
+        }
+        uint32_t n_int = 0, n_leaf = 0;
+        for (int k = 0; k < nc; ++k) (cint[k] ? n_int : n_leaf) += 1;
+        // Allocate (warp-aggregated over the full warp; inactive lanes add 0).
+        __syncwarp();
+        const uint32_t child_base = warp_add(&ctl->wide_count, n_int);
+        const uint32_t tri_base   = warp_add(&ctl->tri_count, n_leaf);
+        const uint32_t qpos       = warp_add(&ctl->level_count[level + 1], n_int);
+        if (!active) continue;
+        if (child_base + n_int > wide_capacity || tri_base + n_leaf > tri_capacity)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            continue;
+        }
+        // Quantisation frame.
+        WideNode w;
+        Bx       u = cb[0];
+        for (int k = 1; k < nc; ++k)
+            for (int a = 0; a < 3; ++a)
+            {
+                u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+                u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+            }
+        float inv[3];
+        for (int a = 0; a < 3; ++a)
+        {
+            w.p[a] = u.lo[a];
+            int e  = pick_exp(u.lo[a], u.hi[a]);
+            w.e[a] = (uint8_t)e;
+            inv[a] = __uint_as_float((uint32_t)(254 - e) << 23);
+        }
+        w.child_base = child_base;
+        w.tri_base   = tri_base;
+        uint8_t  imask = 0;
+        uint32_t ri = 0, rl = 0;
+        for (int k = 0; k < 8; ++k)
+        {
+            if (k < nc)
+            {
+                for (int a = 0; a < 3; ++a)
+                {
+                    float ql = floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], w.p[a]), inv[a]));
+                    float qh = ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], w.p[a]), inv[a]));
+                    w.qlo[a][k] = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
+                    w.qhi[a][k] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
+                }
+                if (cint[k])
+                {
+                    imask |= (uint8_t)(1u << k);
+                    w.meta[k] = (uint8_t)(0x80u | ri);
+                    qout[qpos + ri] = Item{ch[k], child_base + ri};
+                    ++ri;
+                }
+                else
+                {
+                    w.meta[k] = (uint8_t)((1u << 5) | rl);
+                    BvhNode lf = load_node(nodes, ch[k]);
+                    WideTri t;
+                    t.v0[0] = lf.a0[0];
+                    t.v0[1] = lf.a0[1];
+                    t.v0[2] = lf.a0[2];
+                    t.prim  = lf.child1;
+                    t.v1[0] = lf.a1[0];
+                    t.v1[1] = lf.a1[1];
+                    t.v1[2] = lf.a1[2];
+                    t.pad1  = 0;
+                    t.v2[0] = lf.b0[0];
+                    t.v2[1] = lf.b0[1];
+                    t.v2[2] = lf.b0[2];
+                    t.pad2  = 0;
+                    wt[tri_base + rl] = t;
+                    ++rl;
+                }
+            }
+            else
+            {
+                w.meta[k] = 0;
+                for (int a = 0; a < 3; ++a)
+                {
+                    w.qlo[a][k] = 0;
+                    w.qhi[a][k] = 0;
+                }
+            }
+        }
+        w.imask       = imask;
+        wn[item.w]    = w;
+    }
+}
+
+__global__ void k_collapse_finish(CollapseCtl* ctl, Trailer* tr, DeviceWords* words)
+{
+    if (threadIdx.x != 0) return;
+    if (ctl->level_count[kMaxLevels] != 0) atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH);
+    tr->wide_count     = ctl->wide_count;
+    tr->wide_tri_count = ctl->tri_count;
+}
+
+}  // namespace
+
+cudaError_t launch_collapse_wide(const GeomLayout& L, uint8_t* scratch, uint8_t* result, DeviceWords* words,
+                                 int sm_count, cudaStream_t s)
+{
+    if (L.n == 0) return cudaSuccess;
+    CollapseCtl*    ctl   = reinterpret_cast<CollapseCtl*>(scratch + L.s_queue);
+    Item*           q0    = reinterpret_cast<Item*>(scratch + L.s_queue + 2 * kAlign);
+    Item*           q1    = q0 + L.n;
+    const BvhNode*  nodes = reinterpret_cast<const BvhNode*>(result);
+    WideNode*       wn    = reinterpret_cast<WideNode*>(result + L.wide_off);
+    WideTri*        wt    = reinterpret_cast<WideTri*>(result + L.tris_off);
+    Trailer*        tr    = reinterpret_cast<Trailer*>(result + L.trailer_off);
+    static_assert(sizeof(CollapseCtl) <= 2 * kAlign, "collapse control block");
+    k_collapse_init<<<1, 32, 0, s>>>(nodes, L.n, ctl, q0, wn, wt);
+    if (L.n > 1)
+    {
+        uint64_t bound = 1;
+        for (int level = 0; level < kMaxLevels; ++level)
+        {
+            const uint64_t cap    = std::min<uint64_t>(bound, (uint64_t)L.n);
+            const int      blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((cap + 127) / 128, (uint64_t)sm_count * 16));
+            k_collapse_level<<<blocks, 128, 0, s>>>(nodes, level, ctl, (level & 1) ? q1 : q0, (level & 1) ? q0 : q1,
+                                                    wn, wt, (uint32_t)L.wide_capacity, (uint32_t)L.tri_capacity,
+                                                    words);
+            bound = std::min<uint64_t>(bound * 8, (uint64_t)L.n);
+        }
+    }
+    k_collapse_finish<<<1, 32, 0, s>>>(ctl, tr, words);
+    return cudaGetLastError();
+}
+
+}  // namespace rr

@@ -1,0 +1,106 @@
+"""CPU tests of the C-ABI library: it loads, exports every entry point the
+headers declare, and the host-side argument checks return the reference's
+error codes (radeonrays.cpp) without touching a GPU."""
+import ctypes as C
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        names |= set(re.findall(r"RR_API\s+RRError\s+(\w+)\s*\(", h.read_text()))
+    return names
+
+
+def test_library_exports_every_declared_symbol(rrlib):
+    from radeonrays_sdk_gb300 import rr
+    names = declared_symbols()
+    assert len(names) >= 28
+    for n in names:
+        assert hasattr(rrlib, n), n
+    assert names <= set(rr.PROTOTYPES), names - set(rr.PROTOTYPES)
+
+
+def test_reference_spellings_kept(rrlib):
+    text = (ROOT / "include" / "radeonrays.h").read_text()
+    assert "rrSumbitCommandStream" in text and "RR_INAVLID_VALUE" in text
+    assert hasattr(rrlib, "rrSumbitCommandStream")
+
+
+def test_create_context_argument_checks(rrlib):
+    from radeonrays_sdk_gb300 import rr
+    ctx = C.c_void_p()
+    assert rrlib.rrCreateContext(rr.RR_API_VERSION, rr.RR_API_CUDA, None) == rr.RR_ERROR_INVALID_PARAMETER
+    assert rrlib.rrCreateContext(rr.RR_API_VERSION, rr.RR_API_VK, C.byref(ctx)) == rr.RR_ERROR_UNSUPPORTED_API
+    assert rrlib.rrCreateContext(rr.RR_API_VERSION, rr.RR_API_DX, C.byref(ctx)) == rr.RR_ERROR_UNSUPPORTED_API
+    assert rrlib.rrDestroyContext(None) == rr.RR_ERROR_INVALID_PARAMETER
+
+
+def test_null_arguments_rejected(rrlib):
+    from radeonrays_sdk_gb300 import rr
+    E = rr.RR_ERROR_INVALID_PARAMETER
+    fake = C.c_void_p(0x1000)  # never dereferenced: every call below fails its null checks first
+    assert rrlib.rrCmdBuildGeometry(None, 1, None, None, None, None, None) == E
+    assert rrlib.rrCmdBuildGeometry(fake, 1, None, None, None, None, fake) == E
+    assert rrlib.rrCmdBuildScene(fake, None, None, None, None, fake) == E
+    assert rrlib.rrCmdIntersect(fake, None, 0, fake, 1, None, 0, fake, fake, fake) == E
+    assert rrlib.rrCmdIntersect(fake, fake, 0, fake, 1, None, 0, fake, None, fake) == E
+    assert rrlib.rrGetTraceMemoryRequirements(None, 1, None) == E
+    sz = C.c_size_t()
+    assert rrlib.rrGetTraceMemoryRequirements(fake, 0, C.byref(sz)) == E  # radeonrays.cpp:741-745
+    assert rrlib.rrAllocateCommandStream(fake, None) == E
+    assert rrlib.rrSumbitCommandStream(fake, fake, None, None) == E
+    assert rrlib.rrWaitEvent(fake, None) == E
+    assert rrlib.rrReleaseEvent(None, fake) == E
+    assert rrlib.rrReleaseDevicePtr(fake, None) == E
+    assert rrlib.rrGetDevicePtrFromCudaPtr(fake, None, 0, None) == E
+    assert rrlib.rrSetLogLevel(99) == E
+    assert rrlib.rrSetLogFile(None) == E
+
+
+def test_memory_requirements_host_logic(rrlib, tmp_path):
+    """Sizes come from the host layout code only (no device access)."""
+    from radeonrays_sdk_gb300 import rr
+    fake = C.c_void_p(0x1000)
+    mesh = rr.RRTriangleMeshPrimitive(None, 0, 12, None, 1000, rr.RR_INDEX_TYPE_UINT32)
+    bi = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_TRIANGLE_MESH, 1, C.pointer(mesh))
+    req = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), None, C.byref(req)) == rr.RR_SUCCESS
+    plain_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_BINARY, 30, 0)
+    opts = rr.RRBuildOptions(1, C.cast(C.pointer(plain_opts), C.c_void_p))
+    req_b = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts), C.byref(req_b)) == 0
+    nodes = (2 * 1000 - 1) * 64
+    assert req_b.result_buffer_size == (nodes + 255) // 256 * 256 + 256
+    assert req.result_buffer_size > req_b.result_buffer_size  # wide nodes + triangles appended
+    assert req.temporary_update_buffer_size == 0
+    # Unsupported primitive type / bad input.
+    bi2 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1, C.pointer(mesh))
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi2), None, C.byref(req)) == \
+        rr.RR_ERROR_NOT_IMPLEMENTED
+    bi3 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_TRIANGLE_MESH, 2, C.pointer(mesh))
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi3), None, C.byref(req)) == \
+        rr.RR_ERROR_INVALID_PARAMETER
+    bad = rr.RRTriangleMeshPrimitive(None, 0, 10, None, 10, rr.RR_INDEX_TYPE_UINT32)
+    bi4 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_TRIANGLE_MESH, 1, C.pointer(bad))
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi4), None, C.byref(req)) == \
+        rr.RR_ERROR_INVALID_PARAMETER
+    # Trace scratch: 256 bytes per ray (reference geometry_trace.cpp:169), at least 4096 rays' worth.
+    sz = C.c_size_t()
+    assert rrlib.rrGetTraceMemoryRequirements(fake, 1 << 20, C.byref(sz)) == 0
+    assert sz.value == 256 + (1 << 20) * 256
+    # Scene sizes: nodes + [inverse, forward] transforms + trailer + instance records.
+    sbi = rr.RRSceneBuildInput(None, 2048)
+    assert rrlib.rrGetSceneBuildMemoryRequirements(fake, C.byref(sbi), None, C.byref(req)) == 0
+    assert req.result_buffer_size >= (2 * 2048 - 1) * 64 + 2 * 2048 * 48 + 256 + 2048 * 32
+
+
+def test_log_controls(rrlib, tmp_path):
+    from radeonrays_sdk_gb300 import rr
+    assert rrlib.rrSetLogLevel(rr.RR_LOG_LEVEL_ERROR) == 0
+    assert rrlib.rrSetLogFile(str(tmp_path / "rr.log").encode()) == 0
+    assert rrlib.rrSetLogLevel(rr.RR_LOG_LEVEL_WARN) == 0
