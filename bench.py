@@ -1,0 +1,378 @@
+"""Benchmark of the RadeonRays GB300 intersection path.
+
+Workload (one GPU): the 1449 x 1449-vertex heightfield (4,193,408 triangles,
+z = 0.1 * sum of 8 seeded sinusoids) and 16,777,216 incoherent rays (origins
+uniform in its bounding box, directions uniform on the sphere), closest hit,
+full RRHit output.  A step is one rrCmdIntersect over all rays.
+
+Reported (one JSON line on rank 0):
+  value        chosen path (8-wide quantised nodes, persistent kernel) Mrays/s,
+               rays and BVH resident in HBM, CUDA events on the launch stream
+  plain        the plain binary-node kernel on the same rays (reference order)
+  latency_ms   p50 / p99 of the per-step (per-batch) latency of the chosen path
+  e2e          the same metric through the C-ABI with pinned host buffers:
+               H2D of the rays, trace, D2H of the hits inside the timed region
+  roofline     algorithmic bytes of the chosen kernel per launch (ray + hit +
+               80 B per wide node fetch + 48 B per triangle fetch, counted by
+               the kernel's own counters) / mean launch time, against the
+               measured HBM copy bandwidth
+  build        LBVH + wide collapse of the mesh through rrCmdBuildGeometry
+  cpu_baseline the oracle's C++ restatement of the reference traversal on the
+               host cores, on a bounded sample of the same rays
+With --gpus N under torchrun every rank traces its own 16,777,216 rays against
+its own replica of the BVH (replicas only: the path has no exchange step).
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port of isect.comp; the reference's own bvh_analyzer cannot be built
+on the GPU host) on the host cores, on a bounded sample of each step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "incoherent closest-hit Mrays/s + p99 batch latency, chosen vs plain on same GB300"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=1449)
+    ap.add_argument("--rays", type=int, default=16_777_216)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--only", default="", help="profiling aid: 'chosen' or 'plain' runs only that kernel")
+    return ap.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        tdist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.lines, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(args, rank):
+    from radeonrays_sdk_gb300 import scenes
+    g = scenes.rng(1)
+    v, i = scenes.heightfield(args.grid, g)
+    lo, hi = v.min(axis=0), v.max(axis=0)
+    rays = scenes.incoherent_rays(args.rays, lo, hi, scenes.rng(1, 1 + rank))
+    return v, i, rays
+
+
+def describe(args, ntri):
+    return {"workload": f"heightfield {args.grid}x{args.grid} vertices ({ntri:,} triangles), {args.rays:,} incoherent "
+                        "rays per GPU (origins uniform in the mesh box, directions uniform on the sphere), "
+                        "closest hit, full RRHit output",
+            "triangles": ntri, "rays_per_gpu": args.rays, "query": "closest", "output": "full_hit",
+            "chosen": "8-wide nodes, 8-bit conservative child bounds, persistent warp-scheduled kernel",
+            "plain": "64-byte binary nodes, one thread per ray, reference visit order",
+            "l2": "inputs larger than L2 (rays 32 B x rays, BVH > 129 MB); no flush needed",
+            "parallelism": "replicas (rays sharded per GPU, BVH replicated)"}
+
+
+def cpu_baseline(v, i, rays, seconds, threads=None):
+    """Oracle port of isect.comp on the host cores over a bounded ray sample."""
+    import oracle
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    nodes, _, _ = oracle.build_mesh(v, i, threads=threads)
+    n = 1 << 14
+    t0 = time.perf_counter()
+    oracle.trace(nodes, rays[:n], threads=threads)
+    dt = time.perf_counter() - t0
+    target = int(min(rays.shape[0], max(n, n * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    oracle.trace(nodes, rays[:target], threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": target / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"first {target:,} rays of the workload, closest hit, binary nodes built by the oracle"}, nodes
+
+
+def run_reference(args):
+    """--impl reference: the reference's traversal (oracle port) on the host cores."""
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    v, i, rays = workload(args, 0)
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    nodes, _, _ = oracle.build_mesh(v, i, threads=threads)
+    # Size a step so the whole run stays within a few minutes.
+    n = 1 << 14
+    t0 = time.perf_counter()
+    oracle.trace(nodes, rays[:n], threads=threads)
+    per_ray = (time.perf_counter() - t0) / n
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    sample = int(max(n, min(rays.shape[0], budget / per_ray)))
+    for k in range(args.warmup):
+        oracle.trace(nodes, rays[:sample], threads=threads)
+    times = []
+    for k in range(args.steps):
+        off = (k * sample) % max(1, rays.shape[0] - sample + 1)
+        t0 = time.perf_counter()
+        oracle.trace(nodes, rays[off:off + sample], threads=threads)
+        times.append(time.perf_counter() - t0)
+    value = sample * len(times) / sum(times) / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": describe(args, i.shape[0]), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample:,} rays per step of the same workload (oracle restatement of "
+                                       "isect.comp; bvh_analyzer is not buildable on the GPU host)"},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * float(np.percentile(times, 99))}}
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(step, K, W, ws, stream):
+    import torch
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for s, e in ev:
+        s.record(stream)
+        step()
+        e.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    per = [s.elapsed_time(e) for s, e in ev]
+    total = ev[0][0].elapsed_time(ev[-1][1])
+    return per, total
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    from radeonrays_sdk_gb300 import rr
+    v, i, rays = workload(args, rank)
+    R, ntri = rays.shape[0], i.shape[0]
+    ctx = rr.Context()
+    stream = torch.cuda.current_stream()
+    ext = ctx.external_stream(stream)
+    v_d = torch.from_numpy(v).cuda()
+    i_d = torch.from_numpy(i.view(np.int32)).cuda()
+
+    # ---- build (LBVH + wide collapse) through rrCmdBuildGeometry
+    s_bytes, r_bytes = ctx.geometry_requirements(ntri, rr.RR_CUDA_NODE_FORMAT_WIDE8, 30, v.shape[0], 12)
+    scratch_b = torch.empty(s_bytes, dtype=torch.uint8, device="cuda")
+    bvh = torch.empty(r_bytes, dtype=torch.uint8, device="cuda")
+
+    def build_step():
+        ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_WIDE8, stream=ext, scratch=scratch_b,
+                           result=bvh)
+        ctx.release_ptrs()
+    b_per, b_total = time_steps(build_step, 5, 2, 1, stream)
+    build = {"ms": statistics.median(b_per), "mtris_s": ntri / statistics.median(b_per) / 1e3,
+             "format": "binary + wide8", "triangles": ntri}
+
+    rays_d = torch.from_numpy(rays).cuda()
+    hits_d = torch.empty((R, 4), dtype=torch.int32, device="cuda")
+    scratch_t = torch.empty(ctx.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda")
+    hb, rb, hitb = ctx.ptr(bvh), ctx.ptr(rays_d), ctx.ptr(hits_d)
+    sb = ctx.ptr(scratch_t)
+    L = ctx.L
+
+    def trace_step():
+        rr.check(L.rrCmdIntersect(ctx.ctx, hb, rr.RR_INTERSECT_QUERY_CLOSEST, rb, R, None,
+                                  rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hitb, sb, ext), "rrCmdIntersect")
+
+    out = {}
+    # Fetch counters of each kernel (untimed run) -> algorithmic bytes.
+    for name, trav in (("chosen", rr.RR_CUDA_TRAVERSAL_WIDE), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
+        if args.only and args.only != name:
+            continue
+        if name == "plain" and args.no_plain:
+            continue
+        ctx.set_traversal(trav, collect_stats=1)
+        trace_step()
+        torch.cuda.synchronize()
+        st = ctx.stats()
+        ctx.set_traversal(trav)
+        node_b = 80 if name == "chosen" else 64
+        alg = R * (32 + 16) + st["node_fetches"] * node_b + st["triangle_fetches"] * 48
+        clocks = Clocks(local)
+        with clocks:
+            per, total = time_steps(trace_step, args.steps, args.warmup, ws, stream)
+        total = max_over_ranks(total, ws)
+        out[name] = {"per": per, "total": total, "alg_bytes": alg, "stats": st, "clocks": clocks.summary(),
+                     "hits": hits_d[: 1 << 16].cpu().numpy().copy()}
+    assert ctx.device_errors() == 0, "device error word set during the benchmark"
+
+    # ---- end to end through the C-ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e and not args.only:
+        ctx.set_traversal(rr.RR_CUDA_TRAVERSAL_AUTO)
+        rays_h = torch.from_numpy(rays).pin_memory()
+        hits_h = torch.empty((R, 4), dtype=torch.int32).pin_memory()
+
+        def e2e_step():
+            rays_d.copy_(rays_h, non_blocking=True)
+            trace_step()
+            hits_h.copy_(hits_d, non_blocking=True)
+        per_e, total_e = time_steps(e2e_step, args.steps, args.warmup, ws, stream)
+        total_e = max_over_ranks(total_e, ws)
+        e2e = {"value": R * ws * args.steps / (total_e / 1e3) / 1e6, "unit": "Mrays/s",
+               "h2d_bytes_per_step": int(rays_h.numel() * 4), "d2h_bytes_per_step": int(hits_h.numel() * 4),
+               "ms_per_step": total_e / args.steps}
+
+    if rank != 0:
+        ctx.close()
+        return
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    key = "chosen" if "chosen" in out else "plain"
+    c = out[key]
+    value = R * ws * args.steps / (c["total"] / 1e3) / 1e6
+    mean_launch_s = statistics.mean(c["per"]) / 1e3
+    achieved = c["alg_bytes"] / mean_launch_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text()).get(f"trace_{key}")
+        if t and t.get("dram_bytes_per_ray"):
+            traffic = t["dram_bytes_per_ray"] * R
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": c["total"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded heightfield + incoherent rays)",
+        "config": describe(args, ntri),
+        "latency_ms": {"p50": statistics.median(c["per"]), "p99": float(np.percentile(c["per"], 99)),
+                       "max": max(c["per"])},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else
+                     "fallback 6800 GB/s",
+                     "alg_bytes_per_ray": c["alg_bytes"] / R,
+                     "node_fetches_per_ray": c["stats"]["node_fetches"] / R,
+                     "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R},
+        "clocks": c["clocks"], "gpu_launches": args.steps, "build": build, "traversal": key,
+    }
+    if "plain" in out and "chosen" in out:
+        p = out["plain"]
+        pv = R * ws * args.steps / (p["total"] / 1e3) / 1e6
+        line["plain"] = {"value": pv, "unit": "Mrays/s", "ms_per_step": p["total"] / args.steps,
+                         "latency_ms": {"p50": statistics.median(p["per"]), "p99": float(np.percentile(p["per"], 99))},
+                         "alg_bytes_per_ray": p["alg_bytes"] / R, "node_fetches_per_ray": p["stats"]["node_fetches"] / R,
+                         "achieved_gbs": p["alg_bytes"] / (statistics.mean(p["per"]) / 1e3) / 1e9}
+        line["speedup_vs_plain"] = value / pv
+        ch, ph = out["chosen"]["hits"], out["plain"]["hits"]
+        line["hit_id_identity_first_65536"] = float(np.mean(ch[:, 3] == ph[:, 3]))
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu:
+        cb, _ = cpu_baseline(v, i, rays, args.cpu_seconds)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -558,13 +558,18 @@ static void trace_scene_one(const rro_node*         tlas,
         }
         else if (inst == kInvalid)
         {
-            inst = nd.child1;
-            r    = xform_ray(xforms + 24ull * inst, r);
-            inv  = safe_invdir(r.d);
-            oxi  = f3(-r.o.x * inv.x, -r.o.y * inv.y, -r.o.z * inv.z);
-            stack.push_back(kSentinel);
-            addr = 0;
-            continue;
+            // A TLAS leaf whose BLAS is empty (null here) is a miss; the
+            // reference would traverse an undefined buffer.
+            if (blas[nd.child1] != nullptr)
+            {
+                inst = nd.child1;
+                r    = xform_ray(xforms + 24ull * inst, r);
+                inv  = safe_invdir(r.d);
+                oxi  = f3(-r.o.x * inv.x, -r.o.y * inv.y, -r.o.z * inv.z);
+                stack.push_back(kSentinel);
+                addr = 0;
+                continue;
+            }
         }
         else
         {

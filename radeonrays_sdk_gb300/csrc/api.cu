@@ -537,6 +537,10 @@ RR_API RRError rrCmdIntersect(RRContext              context,
         BufInfo  bi;
         if (it != ctx->registry.end()) bi = it->second;
         const uint32_t trav = ctx->topts.traversal;
+        const uint32_t nodes = bi.n == 0 ? 0u : 2u * bi.n - 1u;
+        a.node_limit         = bi.kind == 0 ? kInvalid : nodes;
+        a.wide_limit         = bi.n > 1 ? bi.n - 1 : 1u;
+        a.tri_limit          = bi.n;
         if (bi.kind == kKindScene)
         {
             SceneTraceArgs sa;

@@ -239,7 +239,8 @@ __device__ __forceinline__ void child_box(const BvhNode* nodes, uint32_t c, F3& 
     }
 }
 
-__global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __restrict__ sorted_idx, BvhNode* nodes)
+__global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __restrict__ sorted_idx, BvhNode* nodes,
+                                               DeviceWords* words)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m.n) return;
@@ -255,15 +256,29 @@ __global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __res
     __stcg(dst + 2, make_float4(c.x, c.y, c.z, __uint_as_float(parent)));
     __stcg(dst + 3, make_float4(0.f, 0.f, 0.f, __uint_as_float(0u)));
     uint32_t addr = parent;
-    while (addr != kInvalid)
+    // A Karras tree over 2^30 leaves with 32-bit index tie-breaks is at most
+    // 64 levels deep; the bound and the range check only guard against a
+    // corrupted tree (they raise NODE_RANGE instead of faulting or spinning).
+    for (int level = 0; addr != kInvalid; ++level)
     {
+        if (addr >= n - 1 || level > 96)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
         __threadfence();
         if (atomicExch(&nodes[addr].update, 1u) == 0u) return;
         __threadfence();
-        BvhNode* nd = nodes + addr;
-        F3       lo0, hi0, lo1, hi1;
-        child_box(nodes, __ldcg(&nd->child0), lo0, hi0);
-        child_box(nodes, __ldcg(&nd->child1), lo1, hi1);
+        BvhNode*       nd = nodes + addr;
+        const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
+        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
+        F3 lo0, hi0, lo1, hi1;
+        child_box(nodes, c0, lo0, hi0);
+        child_box(nodes, c1, lo1, hi1);
         __stcg(&nd->a0[0], lo0.x);
         __stcg(&nd->a0[1], lo0.y);
         __stcg(&nd->a0[2], lo0.z);
@@ -283,7 +298,7 @@ __global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __res
 __global__ void k_init_trailer(Trailer* t, Trailer v) { *t = v; }
 __global__ void k_copy_bounds(const uint32_t* b, Trailer* t)
 {
-    if (threadIdx.x < 8) t->bounds[threadIdx.x] = b[threadIdx.x];
+    if (threadIdx.x < 8) t->bounds[threadIdx.x] = (threadIdx.x & 3) == 3 ? 0u : b[threadIdx.x];
 }
 
 inline int grid_for(uint64_t n, int block) { return (int)std::max<uint64_t>(1, (n + block - 1) / block); }
@@ -377,7 +392,7 @@ cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* s
     const uint32_t* sidx = alt ? idx_alt : idx;
     BvhNode*        nodes = reinterpret_cast<BvhNode*>(result);
     if ((e = launch_emit(sc, (int)L.morton_bits, L.n, nodes, s)) != cudaSuccess) return e;
-    k_refit<<<grid_for(L.n, 256), 256, 0, s>>>(m, sidx, nodes);
+    k_refit<<<grid_for(L.n, 256), 256, 0, s>>>(m, sidx, nodes, words);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (L.format == RR_CUDA_NODE_FORMAT_WIDE8) return launch_collapse_wide(L, scratch, result, words, sm_count, s);
     return cudaSuccess;

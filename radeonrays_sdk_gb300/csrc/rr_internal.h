@@ -179,6 +179,9 @@ struct TraceArgs
     int             query;        // RRIntersectQuery
     int             output;       // RRIntersectQueryOutput
     int             empty;        // geometry with no triangles
+    uint32_t        node_limit;   // binary nodes in the buffer (kInvalid: unknown)
+    uint32_t        wide_limit;   // wide-node capacity
+    uint32_t        tri_limit;    // wide-triangle capacity
     DeviceWords*    words;
     int             collect_stats;
     int             block_size;

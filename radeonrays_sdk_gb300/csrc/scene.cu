@@ -143,7 +143,8 @@ __device__ __forceinline__ void slots_union(const BvhNode* nodes, uint32_t c, F3
     hi = vmax3(b, q);
 }
 
-__global__ void k_scene_refit(const float* boxes, const uint32_t* sorted_idx, uint32_t n, BvhNode* nodes)
+__global__ void k_scene_refit(const float* boxes, const uint32_t* sorted_idx, uint32_t n, BvhNode* nodes,
+                              DeviceWords* words)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -157,15 +158,26 @@ __global__ void k_scene_refit(const float* boxes, const uint32_t* sorted_idx, ui
     __stcg(dst + 2, make_float4(b[0], b[1], b[2], __uint_as_float(parent)));
     __stcg(dst + 3, make_float4(b[3], b[4], b[5], __uint_as_float(0u)));
     uint32_t addr = parent;
-    while (addr != kInvalid)
+    for (int level = 0; addr != kInvalid; ++level)
     {
+        if (addr >= n - 1 || level > 96)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
         __threadfence();
         if (atomicExch(&nodes[addr].update, 1u) == 0u) return;
         __threadfence();
-        BvhNode* nd = nodes + addr;
-        F3       l0, h0, l1, h1;
-        slots_union(nodes, __ldcg(&nd->child0), l0, h0);
-        slots_union(nodes, __ldcg(&nd->child1), l1, h1);
+        BvhNode*       nd = nodes + addr;
+        const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
+        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
+        F3 l0, h0, l1, h1;
+        slots_union(nodes, c0, l0, h0);
+        slots_union(nodes, c1, l1, h1);
         __stcg(&nd->a0[0], l0.x); __stcg(&nd->a0[1], l0.y); __stcg(&nd->a0[2], l0.z);
         __stcg(&nd->a1[0], h0.x); __stcg(&nd->a1[1], h0.y); __stcg(&nd->a1[2], h0.z);
         __stcg(&nd->b0[0], l1.x); __stcg(&nd->b0[1], l1.y); __stcg(&nd->b0[2], l1.z);
@@ -178,7 +190,7 @@ __global__ void k_scene_trailer(Trailer* t, Trailer v, const uint32_t* bounds)
 {
     if (threadIdx.x == 0) *t = v;
     __syncthreads();
-    if (bounds && threadIdx.x < 8) t->bounds[threadIdx.x] = bounds[threadIdx.x];
+    if (bounds && threadIdx.x < 8) t->bounds[threadIdx.x] = (threadIdx.x & 3) == 3 ? 0u : bounds[threadIdx.x];
 }
 
 // ---- two-level traversal -------------------------------------------------
@@ -240,8 +252,15 @@ __global__ void __launch_bounds__(kBlock) k_trace_scene_binary(SceneTraceArgs sa
         return v;
     };
 
+    uint32_t blas_lim = kInvalid;
     while (addr != kInvalid)
     {
+        if (addr >= (inst == kInvalid ? a.node_limit : blas_lim) || fetches >= kFetchCap)
+        {
+            raise_error(a.words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            caddr = kInvalid;
+            break;
+        }
         const NodeView nd = load_binary_node(inst == kInvalid ? tlas : blas, addr);
         ++fetches;
         bool descend = false;
@@ -274,8 +293,9 @@ __global__ void __launch_bounds__(kBlock) k_trace_scene_binary(SceneTraceArgs sa
             const InstanceDesc d  = sa.inst[id];
             if (d.leaf_count != 0)
             {
-                inst = id;
-                blas = reinterpret_cast<const BvhNode*>(d.blas);
+                inst     = id;
+                blas     = reinterpret_cast<const BvhNode*>(d.blas);
+                blas_lim = d.leaf_count == kInvalid ? kInvalid : 2 * d.leaf_count - 1;
                 ray  = xray(sa.xforms + 24ull * inst, world);
                 inv  = safe_invdir(ray.d);
                 oxi  = f3(-ray.o.x * inv.x, -ray.o.y * inv.y, -ray.o.z * inv.z);
@@ -371,6 +391,12 @@ __global__ void k_trace_scene_wide(SceneTraceArgs sa, uint32_t gcap)
                     if (sp == 0) break;
                     addr = stack[--sp];
                 }
+                if (addr >= a.node_limit || nf >= kFetchCap)
+                {
+                    raise_error(a.words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+                    cbest = kInvalid;
+                    break;
+                }
                 const NodeView nd = load_binary_node(tlas, addr);
                 ++nf;
                 addr = kInvalid;
@@ -407,13 +433,12 @@ __global__ void k_trace_scene_wide(SceneTraceArgs sa, uint32_t gcap)
                     const uint32_t     id = nd.child1;
                     const InstanceDesc d  = sa.inst[id];
                     if (d.leaf_count == 0) continue;
-                    const Ray lr   = xray(sa.xforms + 24ull * id, world);
-                    const F3  linv = safe_invdir(lr.d);
-                    const F3  loxi = f3(-lr.o.x * linv.x, -lr.o.y * linv.y, -lr.o.z * linv.z);
-                    uint32_t  best = kInvalid;
-                    const bool hit = wide_traverse<kAny>(lr, linv, loxi, reinterpret_cast<const WideNode*>(d.wide_nodes),
-                                                         reinterpret_cast<const WideTri*>(d.wide_tris), ct, best, st,
-                                                         a.words, nf, tf);
+                    const Ray      lr   = xray(sa.xforms + 24ull * id, world);
+                    uint32_t       best = kInvalid;
+                    const uint32_t wlim = d.leaf_count > 1 ? d.leaf_count - 1 : 1;
+                    const bool hit = wide_traverse<kAny>(lr, reinterpret_cast<const WideNode*>(d.wide_nodes),
+                                                         reinterpret_cast<const WideTri*>(d.wide_tris), wlim,
+                                                         d.leaf_count, ct, best, st, a.words, nf, tf);
                     if (best != kInvalid)
                     {
                         cinst = id;
@@ -541,7 +566,7 @@ cudaError_t launch_build_scene(const SceneBuildArgs& a, const SceneLayout& L, ui
         e = launch_emit(alt ? codes_alt : codes, 30, a.n, nodes, s);
         if (e != cudaSuccess) return e;
     }
-    k_scene_refit<<<grid_for(a.n, 128), 128, 0, s>>>(boxes, alt ? idx_alt : idx, a.n, nodes);
+    k_scene_refit<<<grid_for(a.n, 128), 128, 0, s>>>(boxes, alt ? idx_alt : idx, a.n, nodes, words);
     k_scene_trailer<<<1, 32, 0, s>>>(dtr, tr, bounds);
     return cudaGetLastError();
 }

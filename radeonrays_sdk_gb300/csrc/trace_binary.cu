@@ -50,6 +50,12 @@ __global__ void __launch_bounds__(kBlock) k_trace_binary(TraceArgs a)
 
     while (addr != kInvalid)
     {
+        if (addr >= a.node_limit || fetches >= kFetchCap)
+        {
+            raise_error(a.words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            caddr = kInvalid;
+            break;
+        }
         const NodeView nd = load_binary_node(nodes, addr);
         ++fetches;
         if (nd.child0 != kInvalid)

@@ -10,6 +10,13 @@ namespace rr
 {
 constexpr size_t kTraceScratchHeader = 256;  // control words at the start of the trace scratch
 
+// Node visits after which a ray is abandoned with RR_CUDA_DEVICE_ERROR_NODE_RANGE
+// (a well-formed BVH needs a few thousand at most; the cap only stops a
+// corrupted, cyclic buffer from spinning a warp forever).
+constexpr uint32_t kFetchCap = 1u << 22;
+
+__device__ __forceinline__ void raise_error(DeviceWords* w, uint32_t bits) { atomicOr(&w->error_bits, bits); }
+
 struct F3
 {
     float x, y, z;

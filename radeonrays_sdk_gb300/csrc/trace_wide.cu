@@ -13,9 +13,14 @@
 // wide.cu), and the slab test is the reference's, so no hit that the exact
 // box admits is culled.
 //
-// Scheduling: persistent blocks (SM count x blocks_per_sm); each warp takes
-// 32 rays at a time from a counter in the scratch header.  Every node is five
-// 128-bit read-only loads, every triangle three.
+// Scheduling: a persistent grid (SM count x resident blocks).  Every lane owns
+// one ray at a time and advances it one node per loop iteration
+// (trace_wide.cuh, wide_step); when a lane's ray finishes, it writes the hit
+// and takes the next ray from a counter in the scratch header in the same
+// iteration (one warp-aggregated atomic per refill).  Incoherent rays finish
+// at very different times, so refilling keeps the warp's lanes busy instead of
+// idling until the warp's longest ray ends.  Every node is five 128-bit
+// read-only loads, every triangle three.
 #include "rr_internal.h"
 #include "trace_wide.cuh"
 
@@ -23,6 +28,21 @@ namespace rr
 {
 namespace
 {
+template <bool kAny, bool kFull>
+__device__ __forceinline__ void finish(const TraceArgs& a, uint32_t gid, const WideRay& s)
+{
+    if (s.best != kInvalid)
+    {
+        const float4*  tp   = reinterpret_cast<const float4*>(a.wide_tris + s.best);
+        const float4   A = __ldg(tp), B = __ldg(tp + 1), C = __ldg(tp + 2);
+        const uint32_t prim = __float_as_uint(A.w);
+        write_hit<kFull>(a.hits, gid, s.ray, s.ct, f3(A.x, A.y, A.z), f3(B.x, B.y, B.z), f3(C.x, C.y, C.z), 0u, prim,
+                         prim);
+    }
+    else
+        write_miss<kFull>(a.hits, gid);
+}
+
 template <bool kAny, bool kFull, bool kStats>
 __global__ void k_trace_wide(TraceArgs a, uint32_t gcap)
 {
@@ -32,49 +52,60 @@ __global__ void k_trace_wide(TraceArgs a, uint32_t gcap)
     st.s    = s_stack + threadIdx.x * kWideShortStack;
     st.g    = reinterpret_cast<WideEntry*>(a.scratch + kTraceScratchHeader) + (uint64_t)tglob * gcap;
     st.gcap = gcap;
-    uint32_t* ray_ctr = reinterpret_cast<uint32_t*>(a.scratch);
-    const int lane    = threadIdx.x & 31;
-    uint32_t  count   = a.ray_count;
+    uint32_t*      ray_ctr = reinterpret_cast<uint32_t*>(a.scratch);
+    const uint32_t lane    = threadIdx.x & 31;
+    const uint32_t lt      = (1u << lane) - 1u;
+    uint32_t       count   = a.ray_count;
     if (a.indirect) count = min(count, __ldg(a.indirect));
 
+    WideRay  s;
+    uint32_t gid = kInvalid, nf = 0, tf = 0;
+    bool     active = false, exhausted = false;
     for (;;)
     {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(ray_ctr, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) return;
-        const uint32_t gid = base + lane;
-        if (gid < count)
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (idle && !exhausted)
         {
-            const Ray ray = load_ray(a.rays, gid);
-            const F3  inv = safe_invdir(ray.d);
-            const F3  oxi = f3(-ray.o.x * inv.x, -ray.o.y * inv.y, -ray.o.z * inv.z);
-            float     ct  = ray.tmax;
-            uint32_t  best = kInvalid, nf = 0, tf = 0;
-            if (!a.empty) wide_traverse<kAny>(ray, inv, oxi, a.wide_nodes, a.wide_tris, ct, best, st, a.words, nf, tf);
-            if (best != kInvalid)
+            const uint32_t n      = __popc(idle);
+            const int      leader = __ffs(idle) - 1;
+            uint32_t       base   = 0;
+            if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+            base      = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base + n >= count;
+            if (!active)
             {
-                const float4*  tp   = reinterpret_cast<const float4*>(a.wide_tris + best);
-                const float4   A = __ldg(tp), B = __ldg(tp + 1), C = __ldg(tp + 2);
-                const uint32_t prim = __float_as_uint(A.w);
-                write_hit<kFull>(a.hits, gid, ray, ct, f3(A.x, A.y, A.z), f3(B.x, B.y, B.z), f3(C.x, C.y, C.z), 0u,
-                                 prim, prim);
+                const uint32_t my = base + __popc(idle & lt);
+                if (my < count)
+                {
+                    gid    = my;
+                    active = true;
+                    nf = tf = 0;
+                    wide_begin(s, load_ray(a.rays, gid), a.empty != 0);
+                }
             }
-            else
-                write_miss<kFull>(a.hits, gid);
-            if (kStats) add_stats(a.words, nf, tf);
         }
-        __syncwarp();
+        if (__ballot_sync(0xffffffffu, active) == 0) break;
+        if (active && wide_step<kAny>(s, a.wide_nodes, a.wide_tris, a.wide_limit, a.tri_limit, st, a.words, nf, tf))
+        {
+            finish<kAny, kFull>(a, gid, s);
+            if (kStats)
+            {
+                atomicAdd(&a.words->rays, 1ull);
+                atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
+                atomicAdd(&a.words->tri_fetches, (unsigned long long)tf);
+            }
+            active = false;
+        }
     }
 }
 
 template <bool kAny, bool kFull, bool kStats>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
-    auto      kern  = k_trace_wide<kAny, kFull, kStats>;
-    const int block = a.block_size > 0 ? a.block_size : 128;
-    const size_t smem = (size_t)block * kWideShortStack * sizeof(WideEntry);
-    int       per_sm = a.blocks_per_sm;
+    auto         kern  = k_trace_wide<kAny, kFull, kStats>;
+    const int    block = a.block_size > 0 ? a.block_size : 128;
+    const size_t smem  = (size_t)block * kWideShortStack * sizeof(WideEntry);
+    int          per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem) != cudaSuccess) per_sm = 1;

@@ -1,6 +1,16 @@
 // trace_wide.cuh -- traversal of one ray through an 8-wide BVH (device code
 // shared by the single-level kernel, trace_wide.cu, and the two-level kernel,
 // scene.cu).  Node format and conservativeness argument: wide.cu.
+//
+// Per node: the 8 child boxes are decoded to fp32 (fma(q, 2^e, p), exact
+// byte -> float via a PRMT-built 2^23 + q) and slab-tested with the
+// reference's formula (vlk/kernels/common.h:150-164), evaluating only the
+// near plane and the far plane of each axis (chosen by the sign of the
+// inverse direction, which yields exactly the reference's min/max result).
+// Children are visited in the order i = 0..7 of slot i ^ octant(ray): the
+// build places children in octant slots, so this order is roughly front to
+// back.  The traversal stack holds node groups (first child index, internal
+// slot mask, remaining hit mask), one entry per visited node, not per child.
 #pragma once
 #include "trace_common.cuh"
 
@@ -10,153 +20,239 @@ constexpr int kWideShortStack = 16;
 
 struct WideEntry
 {
-    uint32_t node;
-    float    t0;
+    uint32_t base;  // index of the group's first internal child
+    uint32_t bits;  // [7:0] internal-slot mask of the parent, [15:8] remaining hits (visit order)
 };
-
-__device__ __forceinline__ uint32_t ord_f(float f)
-{
-    uint32_t u = __float_as_uint(f);
-    return u ^ ((1u + ~(u >> 31)) | 0x80000000u);
-}
-__device__ __forceinline__ float unord_f(uint32_t v) { return __uint_as_float(v ^ (((v >> 31) - 1u) | 0x80000000u)); }
-__device__ __forceinline__ float byte_f(uint32_t w, int byte) { return (float)((w >> (8 * byte)) & 0xffu); }
-
-__device__ __forceinline__ void cmpx(unsigned long long& a, unsigned long long& b)
-{
-    const unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
-    a = lo;
-    b = hi;
-}
 
 // Per-thread traversal stack: a short stack in shared memory that spills
 // kWideShortStack entries at a time to a per-thread global region.
 struct WideStack
 {
-    WideEntry* s;        // kWideShortStack entries (shared)
-    WideEntry* g;        // gcap entries (global scratch)
+    WideEntry* s;    // kWideShortStack entries (shared)
+    WideEntry* g;    // gcap entries (global scratch)
     uint32_t   gcap;
 };
 
-// Traverse the wide BVH (root = node 0) for `ray`.  Closest hit: shrinks `ct`
-// and sets `best` (triangle index) for every accepted triangle.  Any hit
-// (kAny): returns true at the first accepted triangle.  Returns false when the
-// traversal completes.
-template <bool kAny>
-__device__ __forceinline__ bool wide_traverse(const Ray& ray, const F3 inv, const F3 oxi, const WideNode* __restrict__ wn,
-                                              const WideTri* __restrict__ wt, float& ct, uint32_t& best,
-                                              const WideStack& st, DeviceWords* words, uint32_t& nfetch,
-                                              uint32_t& tfetch)
+// Exact float of byte b (compile-time index) of w: bits of 2^23 + q, minus 2^23.
+template <int b>
+__device__ __forceinline__ float qbyte(uint32_t w)
 {
-    int      sp   = 0;
-    uint32_t gsp  = 0;
-    uint32_t node = 0;
-    for (;;)
-    {
-        if (node == kInvalid)
-        {
-            for (;;)
-            {
-                if (sp == 0)
-                {
-                    if (gsp == 0) return false;
-                    gsp -= kWideShortStack;
-                    for (int i = 0; i < kWideShortStack; ++i) st.s[i] = st.g[gsp + i];
-                    sp = kWideShortStack;
-                }
-                const WideEntry e = st.s[--sp];
-                if (e.t0 <= ct)
-                {
-                    node = e.node;
-                    break;
-                }
-            }
-        }
-
-        const uint4* np = reinterpret_cast<const uint4*>(wn + node);
-        const uint4  w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-        ++nfetch;
-        const F3       p  = f3(__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z));
-        const float    sx = __uint_as_float((w0.w & 0xffu) << 23);
-        const float    sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
-        const float    sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
-        const uint32_t imask      = w0.w >> 24;
-        const uint32_t child_base = w1.x, tri_base = w1.y;
-        node                      = kInvalid;
-
-        unsigned long long key[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-        {
-            const uint32_t meta = ((k < 4 ? w1.z : w1.w) >> (8 * (k & 3))) & 0xffu;
-            key[k]              = ~0ull;
-            if (meta == 0) continue;
-            const uint32_t qlx = k < 4 ? w2.x : w2.y, qly = k < 4 ? w2.z : w2.w, qlz = k < 4 ? w3.x : w3.y;
-            const uint32_t qhx = k < 4 ? w3.z : w3.w, qhy = k < 4 ? w4.x : w4.y, qhz = k < 4 ? w4.z : w4.w;
-            const int      b   = k & 3;
-            const F3 lo = f3(fmaf(byte_f(qlx, b), sx, p.x), fmaf(byte_f(qly, b), sy, p.y), fmaf(byte_f(qlz, b), sz, p.z));
-            const F3 hi = f3(fmaf(byte_f(qhx, b), sx, p.x), fmaf(byte_f(qhy, b), sy, p.y), fmaf(byte_f(qhz, b), sz, p.z));
-            float    t0, t1;
-            isect_box(lo, hi, inv, oxi, ct, ray.tmin, t0, t1);
-            if (t0 > t1) continue;
-            if (imask & (1u << k))
-                key[k] = ((unsigned long long)ord_f(t0) << 32) | (child_base + (meta & 0x7fu));
-            else
-            {
-                const uint32_t cnt = meta >> 5, off = meta & 31u;
-                for (uint32_t j = 0; j < cnt; ++j)
-                {
-                    const uint32_t ti = tri_base + off + j;
-                    const float4*  tp = reinterpret_cast<const float4*>(wt + ti);
-                    const float4   A = __ldg(tp), B = __ldg(tp + 1), C = __ldg(tp + 2);
-                    ++tfetch;
-                    const float t = isect_tri(ray, f3(A.x, A.y, A.z), f3(B.x, B.y, B.z), f3(C.x, C.y, C.z), ct);
-                    if (t < ct)
-                    {
-                        ct   = t;
-                        best = ti;
-                        if (kAny) return true;
-                    }
-                }
-            }
-        }
-
-        // Nearest internal child next; the others pushed farthest-first.
-        cmpx(key[0], key[1]); cmpx(key[2], key[3]); cmpx(key[4], key[5]); cmpx(key[6], key[7]);
-        cmpx(key[0], key[2]); cmpx(key[1], key[3]); cmpx(key[4], key[6]); cmpx(key[5], key[7]);
-        cmpx(key[1], key[2]); cmpx(key[5], key[6]); cmpx(key[0], key[4]); cmpx(key[3], key[7]);
-        cmpx(key[1], key[5]); cmpx(key[2], key[6]);
-        cmpx(key[1], key[4]); cmpx(key[3], key[6]);
-        cmpx(key[2], key[4]); cmpx(key[3], key[5]);
-        cmpx(key[3], key[4]);
-#pragma unroll
-        for (int k = 7; k >= 1; --k)
-        {
-            if (key[k] == ~0ull) continue;
-            if (sp == kWideShortStack)
-            {
-                if (gsp + kWideShortStack > st.gcap)
-                {
-                    atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
-                    continue;
-                }
-                for (int i = 0; i < kWideShortStack; ++i) st.g[gsp + i] = st.s[i];
-                gsp += kWideShortStack;
-                sp = 0;
-            }
-            st.s[sp++] = WideEntry{(uint32_t)key[k], unord_f((uint32_t)(key[k] >> 32))};
-        }
-        if (key[0] != ~0ull) node = (uint32_t)key[0];
-    }
+    return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | b)) - 8388608.0f;
 }
 
-// Persistent-grid sizing shared by the wide kernels: threads never exceed the
-// 32-ray batches; every thread gets an equal share of the scratch for spills.
-struct WideLaunch
+// Traversal state of one ray (kept in registers between steps so that a
+// persistent kernel can retire finished rays and start new ones per lane).
+struct WideRay
 {
-    int      blocks;
-    int      block;
-    uint32_t gcap;
+    Ray      ray;
+    F3       inv, oxi;
+    float    ct;     // closest hit distance so far
+    uint32_t best;   // triangle index of the closest hit
+    uint32_t node;   // next node to fetch (kInvalid: pop a group)
+    uint32_t gbase;  // current node group
+    uint32_t gbits;
+    uint32_t gsp;    // entries spilled to global
+    uint32_t steps;
+    int      sp;     // entries in the short stack
 };
+
+__device__ __forceinline__ void wide_begin(WideRay& s, const Ray& r, bool empty)
+{
+    s.ray   = r;
+    s.inv   = safe_invdir(r.d);
+    s.oxi   = f3(-r.o.x * s.inv.x, -r.o.y * s.inv.y, -r.o.z * s.inv.z);
+    s.ct    = r.tmax;
+    s.best  = kInvalid;
+    s.node  = empty ? kInvalid : 0u;
+    s.gbase = s.gbits = s.gsp = s.steps = 0;
+    s.sp    = 0;
+}
+
+// One traversal step: fetch and test one node (popping a group first when no
+// node is pending), test the triangles of its hit leaf slots, push the
+// remaining hit internal children as a group.  Returns true when the ray is
+// finished: stack empty (closest hit) or a triangle accepted (any hit).
+template <bool kAny>
+__device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict__ wn, const WideTri* __restrict__ wt,
+                                          uint32_t wlim, uint32_t tlim, const WideStack& st, DeviceWords* words,
+                                          uint32_t& nfetch, uint32_t& tfetch)
+{
+    const bool     bx = s.inv.x < 0.f, by = s.inv.y < 0.f, bz = s.inv.z < 0.f;
+    const uint32_t oct = (bx ? 4u : 0u) | (by ? 2u : 0u) | (bz ? 1u : 0u);
+    const uint32_t o2  = oct & 3u;
+    const uint32_t ps  = (0u ^ o2) | ((1u ^ o2) << 4) | ((2u ^ o2) << 8) | ((3u ^ o2) << 12);
+    const bool     sw  = (oct & 4u) != 0;
+
+    if (s.node == kInvalid)
+    {
+        if ((s.gbits >> 8) == 0)
+        {
+            if (s.sp == 0)
+            {
+                if (s.gsp == 0) return true;
+                s.gsp -= kWideShortStack;
+                for (int k = 0; k < kWideShortStack; ++k) st.s[k] = st.g[s.gsp + k];
+                s.sp = kWideShortStack;
+            }
+            const WideEntry e = st.s[--s.sp];
+            s.gbase           = e.base;
+            s.gbits           = e.bits;
+        }
+        const uint32_t i    = __ffs(s.gbits >> 8) - 1;
+        s.gbits &= ~(0x100u << i);
+        const uint32_t slot = i ^ oct;
+        s.node              = s.gbase + __popc(s.gbits & ((1u << slot) - 1u) & 0xffu);
+    }
+    if (++s.steps > kFetchCap || s.node >= wlim)
+    {
+        raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+        s.best = kInvalid;
+        return true;
+    }
+
+    const uint4* np = reinterpret_cast<const uint4*>(wn + s.node);
+    const uint4  w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    ++nfetch;
+    const float    px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const float    sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float    sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float    sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    const uint32_t imask      = w0.w >> 24;
+    const uint32_t child_base = w1.x, tri_base = w1.y;
+    const F3       inv = s.inv, oxi = s.oxi;
+    const float    tmin = s.ray.tmin, ct = s.ct;
+
+    // Near / far byte arrays per axis, permuted into visit order.
+    auto vis = [&](uint32_t a0, uint32_t a1, uint32_t& o0, uint32_t& o1) {
+        const uint32_t t0 = sw ? a1 : a0, t1 = sw ? a0 : a1;
+        o0 = __byte_perm(t0, 0u, ps);
+        o1 = __byte_perm(t1, 0u, ps);
+    };
+    uint32_t nx0, nx1, fx0, fx1, ny0, ny1, fy0, fy1, nz0, nz1, fz0, fz1, m0, m1;
+    vis(bx ? w3.z : w2.x, bx ? w3.w : w2.y, nx0, nx1);
+    vis(bx ? w2.x : w3.z, bx ? w2.y : w3.w, fx0, fx1);
+    vis(by ? w4.x : w2.z, by ? w4.y : w2.w, ny0, ny1);
+    vis(by ? w2.z : w4.x, by ? w2.w : w4.y, fy0, fy1);
+    vis(bz ? w4.z : w3.x, bz ? w4.w : w3.y, nz0, nz1);
+    vis(bz ? w3.x : w4.z, bz ? w3.y : w4.w, fz0, fz1);
+    vis(w1.z, w1.w, m0, m1);
+
+    uint32_t ihit = 0, lhit = 0;
+#define RR_WIDE_CHILD(i, W)                                                                                         \
+    {                                                                                                               \
+        const uint32_t meta = (W##m >> (8 * ((i) & 3))) & 0xffu;                                                    \
+        const float    tnx  = fmaf(fmaf(qbyte<(i) & 3>(W##nx), sx, px), inv.x, oxi.x);                              \
+        const float    tfx  = fmaf(fmaf(qbyte<(i) & 3>(W##fx), sx, px), inv.x, oxi.x);                              \
+        const float    tny  = fmaf(fmaf(qbyte<(i) & 3>(W##ny), sy, py), inv.y, oxi.y);                              \
+        const float    tfy  = fmaf(fmaf(qbyte<(i) & 3>(W##fy), sy, py), inv.y, oxi.y);                              \
+        const float    tnz  = fmaf(fmaf(qbyte<(i) & 3>(W##nz), sz, pz), inv.z, oxi.z);                              \
+        const float    tfz  = fmaf(fmaf(qbyte<(i) & 3>(W##fz), sz, pz), inv.z, oxi.z);                              \
+        const float    t0   = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));                                             \
+        const float    t1   = fminf(fminf(tfx, tfy), fminf(tfz, ct));                                               \
+        if (meta != 0 && t0 <= t1)                                                                                  \
+        {                                                                                                           \
+            if (meta & 0x80u)                                                                                       \
+                ihit |= 1u << (i);                                                                                  \
+            else                                                                                                    \
+                lhit |= 1u << (i);                                                                                  \
+        }                                                                                                           \
+    }
+    {
+        const uint32_t lo_nx = nx0, lo_fx = fx0, lo_ny = ny0, lo_fy = fy0, lo_nz = nz0, lo_fz = fz0, lo_m = m0;
+        const uint32_t hi_nx = nx1, hi_fx = fx1, hi_ny = ny1, hi_fy = fy1, hi_nz = nz1, hi_fz = fz1, hi_m = m1;
+        RR_WIDE_CHILD(0, lo_)
+        RR_WIDE_CHILD(1, lo_)
+        RR_WIDE_CHILD(2, lo_)
+        RR_WIDE_CHILD(3, lo_)
+        RR_WIDE_CHILD(4, hi_)
+        RR_WIDE_CHILD(5, hi_)
+        RR_WIDE_CHILD(6, hi_)
+        RR_WIDE_CHILD(7, hi_)
+    }
+#undef RR_WIDE_CHILD
+
+    // Leaf slots: test their triangles in visit order.
+    while (lhit)
+    {
+        const uint32_t i    = __ffs(lhit) - 1;
+        lhit &= lhit - 1;
+        const uint32_t meta = ((i < 4 ? m0 : m1) >> (8 * (i & 3))) & 0xffu;
+        const uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+        if (tri_base + off + cnt > tlim)
+        {
+            raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            continue;
+        }
+        for (uint32_t j = 0; j < cnt; ++j)
+        {
+            const uint32_t ti = tri_base + off + j;
+            const float4*  tp = reinterpret_cast<const float4*>(wt + ti);
+            const float4   A = __ldg(tp), B = __ldg(tp + 1), C = __ldg(tp + 2);
+            ++tfetch;
+            const float t = isect_tri(s.ray, f3(A.x, A.y, A.z), f3(B.x, B.y, B.z), f3(C.x, C.y, C.z), s.ct);
+            if (t < s.ct)
+            {
+                s.ct   = t;
+                s.best = ti;
+                if (kAny) return true;
+            }
+        }
+    }
+
+    if (ihit)
+    {
+        if (s.gbits >> 8)
+        {
+            if (s.sp == kWideShortStack)
+            {
+                if (s.gsp + kWideShortStack > st.gcap)
+                {
+                    raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
+                    s.sp = kWideShortStack - 1;  // overwrite the top entry: result flagged invalid
+                }
+                else
+                {
+                    for (int k = 0; k < kWideShortStack; ++k) st.g[s.gsp + k] = st.s[k];
+                    s.gsp += kWideShortStack;
+                    s.sp = 0;
+                }
+            }
+            st.s[s.sp++] = WideEntry{s.gbase, s.gbits};
+        }
+        s.gbase             = child_base;
+        s.gbits             = imask | (ihit << 8);
+        const uint32_t i    = __ffs(ihit) - 1;
+        s.gbits &= ~(0x100u << i);
+        const uint32_t slot = i ^ oct;
+        s.node              = s.gbase + __popc(s.gbits & ((1u << slot) - 1u) & 0xffu);
+    }
+    else
+        s.node = kInvalid;
+    return false;
+}
+
+// Whole traversal of one ray (used where a thread owns its ray to the end).
+// Closest hit: shrinks `ct` and sets `best` (triangle index).  Any hit (kAny):
+// returns true at the first accepted triangle.
+template <bool kAny>
+__device__ __forceinline__ bool wide_traverse(const Ray& ray, const WideNode* __restrict__ wn,
+                                              const WideTri* __restrict__ wt, uint32_t wlim, uint32_t tlim, float& ct,
+                                              uint32_t& best, const WideStack& st, DeviceWords* words,
+                                              uint32_t& nfetch, uint32_t& tfetch)
+{
+    WideRay s;
+    wide_begin(s, ray, false);
+    s.ct = ct;
+    while (!wide_step<kAny>(s, wn, wt, wlim, tlim, st, words, nfetch, tfetch))
+    {
+    }
+    const bool hit = kAny && s.best != kInvalid;
+    if (s.best != kInvalid)
+    {
+        ct   = s.ct;
+        best = s.best;
+    }
+    return hit;
+}
 
 }  // namespace rr

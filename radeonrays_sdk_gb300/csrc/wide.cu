@@ -271,29 +271,66 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
         }
         w.child_base = child_base;
         w.tri_base   = tri_base;
+        // Octant slot order: slot s holds a child on the + side of the node
+        // centre along x if s & 4, y if s & 2, z if s & 1 (greedy assignment,
+        // smallest cost first).  A ray with direction octant o visits slots
+        // i ^ o for i = 0..7, which is then roughly front to back.
+        int slot_child[8];
+        {
+            float dc[8][3];
+            for (int k = 0; k < nc; ++k)
+                for (int a = 0; a < 3; ++a)
+                    dc[k][a] = 0.5f * (cb[k].lo[a] + cb[k].hi[a]) - 0.5f * (u.lo[a] + u.hi[a]);
+            for (int s2 = 0; s2 < 8; ++s2) slot_child[s2] = -1;
+            uint32_t used = 0;
+            for (int round = 0; round < nc; ++round)
+            {
+                float bc = INFINITY;
+                int   bk = -1, bs = -1;
+                for (int k = 0; k < nc; ++k)
+                {
+                    if (used >> k & 1u) continue;
+                    for (int s2 = 0; s2 < 8; ++s2)
+                    {
+                        if (slot_child[s2] >= 0) continue;
+                        const float cost = ((s2 & 4) ? -dc[k][0] : dc[k][0]) + ((s2 & 2) ? -dc[k][1] : dc[k][1]) +
+                                           ((s2 & 1) ? -dc[k][2] : dc[k][2]);
+                        if (cost < bc || bk < 0)
+                        {
+                            bc = cost;
+                            bk = k;
+                            bs = s2;
+                        }
+                    }
+                }
+                slot_child[bs] = bk;
+                used |= 1u << bk;
+            }
+        }
         uint8_t  imask = 0;
         uint32_t ri = 0, rl = 0;
-        for (int k = 0; k < 8; ++k)
+        for (int slot = 0; slot < 8; ++slot)
         {
-            if (k < nc)
+            const int k = slot_child[slot];
+            if (k >= 0)
             {
                 for (int a = 0; a < 3; ++a)
                 {
                     float ql = floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], w.p[a]), inv[a]));
                     float qh = ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], w.p[a]), inv[a]));
-                    w.qlo[a][k] = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
-                    w.qhi[a][k] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
+                    w.qlo[a][slot] = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
+                    w.qhi[a][slot] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
                 }
                 if (cint[k])
                 {
-                    imask |= (uint8_t)(1u << k);
-                    w.meta[k] = (uint8_t)(0x80u | ri);
+                    imask |= (uint8_t)(1u << slot);
+                    w.meta[slot] = (uint8_t)(0x80u | ri);
                     qout[qpos + ri] = Item{ch[k], child_base + ri};
                     ++ri;
                 }
                 else
                 {
-                    w.meta[k] = (uint8_t)((1u << 5) | rl);
+                    w.meta[slot] = (uint8_t)((1u << 5) | rl);
                     BvhNode lf = load_node(nodes, ch[k]);
                     WideTri t;
                     t.v0[0] = lf.a0[0];
@@ -314,11 +351,11 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
             }
             else
             {
-                w.meta[k] = 0;
+                w.meta[slot] = 0;
                 for (int a = 0; a < 3; ++a)
                 {
-                    w.qlo[a][k] = 0;
-                    w.qhi[a][k] = 0;
+                    w.qlo[a][slot] = 0;
+                    w.qhi[a][slot] = 0;
                 }
             }
         }
