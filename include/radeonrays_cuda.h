@@ -121,6 +121,33 @@ RR_API RRError rrCudaGetTraversalStats(RRContext context, RRCudaTraversalStats* 
  * (default 600000).  The reference waits forever (vlk/device.cpp:249-272). */
 RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
 
+/* Intersect without allocating anything and without a caller scratch buffer.
+ * No counterpart in the reference API.
+ *
+ * For callers that cannot call cudaMalloc at the point where they trace rays:
+ * a serving loop with a hard latency budget (cudaMalloc may block and
+ * synchronise the device), or a host whose device memory is owned by another
+ * allocator or pool (an extra cudaMalloc would fail or break its accounting).
+ * The caller passes its own BVH, rays and hit buffer (device pointers) and a
+ * cudaStream_t as void* (0 = default stream); no RRContext is needed.
+ *
+ * Runs the plain binary-node traversal (the rrCmdIntersect plain kernel, same
+ * hits) over `geometry`, a non-empty geometry result buffer written by
+ * rrCmdBuildGeometry (binary nodes at offset 0).  Its traversal scratch is a
+ * fixed device array of about 32 MiB inside librr.so, which every GPU that
+ * loads the library keeps until the process exits; a call takes at most
+ * 131072 rays (more returns RR_ERROR_INVALID_PARAMETER).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress): make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU race with each other. */
+RR_API RRError rrCudaIntersectNoAlloc(const void*            geometry,
+                                      RRIntersectQuery       query,
+                                      const void*            rays,
+                                      uint32_t               ray_count,
+                                      RRIntersectQueryOutput query_output,
+                                      void*                  hits,
+                                      void*                  cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -151,6 +151,7 @@ PROTOTYPES = {
     "rrCudaGetDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaGetTraversalStats": [_P, C.POINTER(RRCudaTraversalStats)],
     "rrCudaSetWaitTimeout": [_P, C.c_uint32],
+    "rrCudaIntersectNoAlloc": [_P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
 }
 
 _LIB = None
