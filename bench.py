@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--only", default="", help="profiling aid: 'chosen' or 'plain' runs only that kernel")
+    ap.add_argument("--block", type=int, default=0, help="chosen kernel threads per block (0: library default)")
+    ap.add_argument("--per-sm", type=int, default=0, help="chosen kernel resident blocks per SM (0: occupancy)")
+    ap.add_argument("--ray-order", type=int, default=0, help="chosen kernel: 0 default, 1 given order, 2 sorted")
+    ap.add_argument("--chosen", type=int, default=2, help="chosen traversal: 2 wide (8-wide nodes), 3 binary persistent")
     return ap.parse_args()
 
 
@@ -279,17 +283,19 @@ def run_ours(args):
 
     out = {}
     # Fetch counters of each kernel (untimed run) -> algorithmic bytes.
-    for name, trav in (("chosen", rr.RR_CUDA_TRAVERSAL_WIDE), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
+    for name, trav in (("chosen", args.chosen), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
         if args.only and args.only != name:
             continue
         if name == "plain" and args.no_plain:
             continue
-        ctx.set_traversal(trav, collect_stats=1)
+        shape = (args.block, args.per_sm) if name == "chosen" else (0, 0)
+        order = args.ray_order if name == "chosen" else 0
+        ctx.set_traversal(trav, *shape, collect_stats=1, ray_order=order)
         trace_step()
         torch.cuda.synchronize()
         st = ctx.stats()
-        ctx.set_traversal(trav)
-        node_b = 80 if name == "chosen" else 64
+        ctx.set_traversal(trav, *shape, ray_order=order)
+        node_b = 80 if trav == rr.RR_CUDA_TRAVERSAL_WIDE else 64
         alg = R * (32 + 16) + st["node_fetches"] * node_b + st["triangle_fetches"] * 48
         clocks = Clocks(local)
         with clocks:

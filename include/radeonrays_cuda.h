@@ -49,7 +49,10 @@ typedef enum
     /* One thread per ray, 64-byte binary nodes, reference visit order. */
     RR_CUDA_TRAVERSAL_BINARY = 1,
     /* Persistent warp-scheduled kernel over 8-wide quantised nodes. */
-    RR_CUDA_TRAVERSAL_WIDE = 2
+    RR_CUDA_TRAVERSAL_WIDE = 2,
+    /* Persistent warp-scheduled kernel over the binary nodes, reference visit
+     * order (hits bit-identical to RR_CUDA_TRAVERSAL_BINARY). */
+    RR_CUDA_TRAVERSAL_BINARY_PERSISTENT = 3
 } RRCudaTraversal;
 
 typedef struct
@@ -59,7 +62,9 @@ typedef struct
     uint32_t block_size;      /* threads per block, 0 = tuned default */
     uint32_t blocks_per_sm;   /* persistent kernel occupancy, 0 = tuned default */
     uint32_t collect_stats;   /* 1 = count node and triangle fetches */
-    uint32_t reserved[3];
+    uint32_t ray_order;       /* wide kernel: 0 = default, 1 = trace in the given order, 2 = sort rays by
+                                 direction octant and origin first (batches of 2^20 rays or more) */
+    uint32_t reserved[2];
 } RRCudaTraversalOptions;
 
 /* Fetch counters accumulated while collect_stats is 1. */

@@ -532,6 +532,7 @@ RR_API RRError rrCmdIntersect(RRContext              context,
         a.collect_stats = ctx->topts.collect_stats ? 1 : 0;
         a.block_size    = (int)ctx->topts.block_size;
         a.blocks_per_sm = (int)ctx->topts.blocks_per_sm;
+        a.ray_order     = (int)ctx->topts.ray_order;
         a.sm_count      = ctx->sm_count;
         auto     it     = ctx->registry.find((uintptr_t)bvh);
         BufInfo  bi;
@@ -557,10 +558,13 @@ RR_API RRError rrCmdIntersect(RRContext              context,
         // from the root like the reference (vlk/intersector.cpp:290).
         a.empty             = (bi.kind == kKindGeom && bi.n == 0);
         const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
-        if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
+        if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT)
+            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_persistent(a, s); });
+        else if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
         {
             a.wide_nodes = reinterpret_cast<const WideNode*>(bvh + bi.wide_off);
             a.wide_tris  = reinterpret_cast<const WideTri*>(bvh + bi.tris_off);
+            a.bounds     = reinterpret_cast<const uint32_t*>(bvh + bi.trailer_off + offsetof(Trailer, bounds));
             record(S(command_stream), [=](cudaStream_t s) { return launch_trace_wide(a, s); });
         }
         else
@@ -788,7 +792,8 @@ RR_API RRError rrUnmapDevicePtr(RRContext context, RRDevicePtr device_ptr, void*
 RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversalOptions* options)
 {
     if (!context || !options || options->struct_size < sizeof(RRCudaTraversalOptions)) return RR_ERROR_INVALID_PARAMETER;
-    if (options->traversal > RR_CUDA_TRAVERSAL_WIDE) return RR_ERROR_INVALID_PARAMETER;
+    if (options->traversal > RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || options->ray_order > 2)
+        return RR_ERROR_INVALID_PARAMETER;
     if (options->block_size && (options->block_size % 32 || options->block_size > 1024)) return RR_ERROR_INVALID_PARAMETER;
     C(context)->topts = *options;
     return RR_SUCCESS;

@@ -182,6 +182,8 @@ struct TraceArgs
     uint32_t        node_limit;   // binary nodes in the buffer (kInvalid: unknown)
     uint32_t        wide_limit;   // wide-node capacity
     uint32_t        tri_limit;    // wide-triangle capacity
+    const uint32_t* bounds;       // mesh box (order-preserving uint encoding) for ray ordering; may be null
+    int             ray_order;    // RRCudaTraversalOptions::ray_order
     DeviceWords*    words;
     int             collect_stats;
     int             block_size;
@@ -190,6 +192,7 @@ struct TraceArgs
 };
 cudaError_t launch_trace_binary(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_wide(const TraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_persistent(const TraceArgs& a, cudaStream_t s);
 
 struct SceneTraceArgs
 {

@@ -357,7 +357,7 @@ __global__ void k_trace_scene_wide(SceneTraceArgs sa, uint32_t gcap)
     extern __shared__ WideEntry s_stack[];
     const uint32_t tglob = blockIdx.x * blockDim.x + threadIdx.x;
     WideStack      st;
-    st.s    = s_stack + threadIdx.x * kWideShortStack;
+    st.s    = s_stack + threadIdx.x;
     st.g    = reinterpret_cast<WideEntry*>(a.scratch + kTraceScratchHeader) + (uint64_t)tglob * gcap;
     st.gcap = gcap;
     uint32_t* ray_ctr = reinterpret_cast<uint32_t*>(a.scratch);
@@ -480,7 +480,7 @@ cudaError_t go(const SceneTraceArgs& sa, cudaStream_t s)
         return cudaGetLastError();
     }
     auto         kern  = k_trace_scene_wide<kAny, kFull, kStats>;
-    const int    block = a.block_size > 0 ? a.block_size : 128;
+    const int    block = kWideBlock;
     const size_t smem  = (size_t)block * kWideShortStack * sizeof(WideEntry);
     int          per_sm = a.blocks_per_sm;
     if (per_sm <= 0)

@@ -26,11 +26,15 @@ struct WideEntry
 
 // Per-thread traversal stack: a short stack in shared memory that spills
 // kWideShortStack entries at a time to a per-thread global region.
+constexpr int kWideBlock = 128;  // threads per block of the wide kernels
+
 struct WideStack
 {
-    WideEntry* s;    // kWideShortStack entries (shared)
-    WideEntry* g;    // gcap entries (global scratch)
+    WideEntry* s;  // this thread's first short-stack entry (shared); entries are
+                   // interleaved across the block (kWideBlock apart): no bank conflicts
+    WideEntry* g;  // gcap entries (global scratch)
     uint32_t   gcap;
+    __device__ __forceinline__ WideEntry& at(int k) const { return s[k * kWideBlock]; }
 };
 
 // Exact float of byte b (compile-time index) of w: bits of 2^23 + q, minus 2^23.
@@ -39,6 +43,23 @@ __device__ __forceinline__ float qbyte(uint32_t w)
 {
     return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | b)) - 8388608.0f;
 }
+
+// Three-input min / max (one instruction each on sm_100 and later).
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Bit 7 of each byte of w gathered into bits 0..3.
+__device__ __forceinline__ uint32_t byte_msbs(uint32_t w) { return (((w >> 7) & 0x01010101u) * 0x01020408u) >> 24; }
 
 // Traversal state of one ray (kept in registers between steps so that a
 // persistent kernel can retire finished rays and start new ones per lane).
@@ -75,7 +96,7 @@ __device__ __forceinline__ void wide_begin(WideRay& s, const Ray& r, bool empty)
 template <bool kAny>
 __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict__ wn, const WideTri* __restrict__ wt,
                                           uint32_t wlim, uint32_t tlim, const WideStack& st, DeviceWords* words,
-                                          uint32_t& nfetch, uint32_t& tfetch)
+                                          uint32_t& nfetch, uint32_t& tfetch, uint32_t amask = 0u)
 {
     const bool     bx = s.inv.x < 0.f, by = s.inv.y < 0.f, bz = s.inv.z < 0.f;
     const uint32_t oct = (bx ? 4u : 0u) | (by ? 2u : 0u) | (bz ? 1u : 0u);
@@ -83,32 +104,49 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
     const uint32_t ps  = (0u ^ o2) | ((1u ^ o2) << 4) | ((2u ^ o2) << 8) | ((3u ^ o2) << 12);
     const bool     sw  = (oct & 4u) != 0;
 
+    // Pick the node to fetch.  Written without early exits so that lanes that
+    // pop and lanes that already have a node reconverge before the node test
+    // (an exit inside this branch would let the two groups run it separately).
+    bool done = false;
     if (s.node == kInvalid)
     {
         if ((s.gbits >> 8) == 0)
         {
-            if (s.sp == 0)
+            if (s.sp == 0 && s.gsp == 0)
+                done = true;
+            else
             {
-                if (s.gsp == 0) return true;
-                s.gsp -= kWideShortStack;
-                for (int k = 0; k < kWideShortStack; ++k) st.s[k] = st.g[s.gsp + k];
-                s.sp = kWideShortStack;
+                if (s.sp == 0)
+                {
+                    s.gsp -= kWideShortStack;
+                    for (int k = 0; k < kWideShortStack; ++k) st.at(k) = st.g[s.gsp + k];
+                    s.sp = kWideShortStack;
+                }
+                const WideEntry e = st.at(--s.sp);
+                s.gbase           = e.base;
+                s.gbits           = e.bits;
             }
-            const WideEntry e = st.s[--s.sp];
-            s.gbase           = e.base;
-            s.gbits           = e.bits;
         }
-        const uint32_t i    = __ffs(s.gbits >> 8) - 1;
-        s.gbits &= ~(0x100u << i);
-        const uint32_t slot = i ^ oct;
-        s.node              = s.gbase + __popc(s.gbits & ((1u << slot) - 1u) & 0xffu);
+        if (!done)
+        {
+            const uint32_t i    = __ffs(s.gbits >> 8) - 1;
+            s.gbits &= ~(0x100u << i);
+            const uint32_t slot = i ^ oct;
+            s.node              = s.gbase + __popc(s.gbits & ((1u << slot) - 1u) & 0xffu);
+        }
     }
-    if (++s.steps > kFetchCap || s.node >= wlim)
+    if (!done && (++s.steps > kFetchCap || s.node >= wlim))
     {
         raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
         s.best = kInvalid;
-        return true;
+        done   = true;
     }
+    // amask (when given) holds every lane of the warp that is in this step:
+    // the lanes that go on to the node test wait for each other here so that
+    // the node test runs once for all of them.
+    const uint32_t go = amask ? __ballot_sync(amask, !done) : 0u;
+    if (done) return true;
+    if (amask) __syncwarp(go);
 
     const uint4* np = reinterpret_cast<const uint4*>(wn + s.node);
     const uint4  w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
@@ -137,29 +175,51 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
     vis(bz ? w3.x : w4.z, bz ? w3.y : w4.w, fz0, fz1);
     vis(w1.z, w1.w, m0, m1);
 
-    uint32_t ihit = 0, lhit = 0;
+    // Slab distances in quantised space.  For a plane at byte q of axis a the
+    // reference evaluates fma(c, inv, oxi) on the child coordinate c; here
+    //   t = fma(2^23 + q, A, B -+ eps),  A = 2^e * inv (exact),
+    //   B = fma(p, inv, oxi) - 2^23 * A (rounded),
+    // with eps = 1.25 |A| + 2^-20 |B| on the near (-) and far (+) planes.  eps
+    // bounds the rounding of B, of B - 2^23 A and of B -+ eps (each at most
+    // |A| / 2 + 2^-24 |B|); as the decoded coordinate lies outside the exact
+    // child bound and rounding is monotone, the near distance never exceeds
+    // the reference's on the exact box and the far distance is never below it.
+    // A ray the reference's test admits is therefore always admitted.
+    float An[3], Bn[3], Bf[3];
+    {
+        const float s3[3] = {sx, sy, sz}, p3[3] = {px, py, pz}, i3[3] = {inv.x, inv.y, inv.z},
+                    o3[3] = {oxi.x, oxi.y, oxi.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const float A   = s3[k] * i3[k];
+            const float B   = fmaf(p3[k], i3[k], o3[k]);
+            const float eps = fmaf(fabsf(A), 1.25f, fabsf(B) * 9.5367431640625e-07f);
+            const float M   = fmaf(-8388608.0f, A, B);
+            An[k]           = A;
+            Bn[k]           = M - eps;
+            Bf[k]           = M + eps;
+        }
+    }
+    // Hit bits per visit position; empty slots are masked out below through
+    // the meta bytes (internal: bit 7; leaf: bit 7 clear, count in bits 5-6).
+    uint32_t hits = 0;
+#define RR_WIDE_Q(w, b) __int_as_float((int)__byte_perm((w), 0x4B000000u, 0x7540u | (b)))
 #define RR_WIDE_CHILD(i, W)                                                                                         \
     {                                                                                                               \
-        const uint32_t meta = (W##m >> (8 * ((i) & 3))) & 0xffu;                                                    \
-        const float    tnx  = fmaf(fmaf(qbyte<(i) & 3>(W##nx), sx, px), inv.x, oxi.x);                              \
-        const float    tfx  = fmaf(fmaf(qbyte<(i) & 3>(W##fx), sx, px), inv.x, oxi.x);                              \
-        const float    tny  = fmaf(fmaf(qbyte<(i) & 3>(W##ny), sy, py), inv.y, oxi.y);                              \
-        const float    tfy  = fmaf(fmaf(qbyte<(i) & 3>(W##fy), sy, py), inv.y, oxi.y);                              \
-        const float    tnz  = fmaf(fmaf(qbyte<(i) & 3>(W##nz), sz, pz), inv.z, oxi.z);                              \
-        const float    tfz  = fmaf(fmaf(qbyte<(i) & 3>(W##fz), sz, pz), inv.z, oxi.z);                              \
-        const float    t0   = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));                                             \
-        const float    t1   = fminf(fminf(tfx, tfy), fminf(tfz, ct));                                               \
-        if (meta != 0 && t0 <= t1)                                                                                  \
-        {                                                                                                           \
-            if (meta & 0x80u)                                                                                       \
-                ihit |= 1u << (i);                                                                                  \
-            else                                                                                                    \
-                lhit |= 1u << (i);                                                                                  \
-        }                                                                                                           \
+        const float tnx = fmaf(RR_WIDE_Q(W##nx, (i) & 3), An[0], Bn[0]);                                            \
+        const float tfx = fmaf(RR_WIDE_Q(W##fx, (i) & 3), An[0], Bf[0]);                                            \
+        const float tny = fmaf(RR_WIDE_Q(W##ny, (i) & 3), An[1], Bn[1]);                                            \
+        const float tfy = fmaf(RR_WIDE_Q(W##fy, (i) & 3), An[1], Bf[1]);                                            \
+        const float tnz = fmaf(RR_WIDE_Q(W##nz, (i) & 3), An[2], Bn[2]);                                            \
+        const float tfz = fmaf(RR_WIDE_Q(W##fz, (i) & 3), An[2], Bf[2]);                                            \
+        const float t0  = fmaxf(max3f(tnx, tny, tnz), tmin);                                                        \
+        const float t1  = fminf(min3f(tfx, tfy, tfz), ct);                                                          \
+        hits |= (t0 <= t1) ? (1u << (i)) : 0u;                                                                      \
     }
     {
-        const uint32_t lo_nx = nx0, lo_fx = fx0, lo_ny = ny0, lo_fy = fy0, lo_nz = nz0, lo_fz = fz0, lo_m = m0;
-        const uint32_t hi_nx = nx1, hi_fx = fx1, hi_ny = ny1, hi_fy = fy1, hi_nz = nz1, hi_fz = fz1, hi_m = m1;
+        const uint32_t lo_nx = nx0, lo_fx = fx0, lo_ny = ny0, lo_fy = fy0, lo_nz = nz0, lo_fz = fz0;
+        const uint32_t hi_nx = nx1, hi_fx = fx1, hi_ny = ny1, hi_fy = fy1, hi_nz = nz1, hi_fz = fz1;
         RR_WIDE_CHILD(0, lo_)
         RR_WIDE_CHILD(1, lo_)
         RR_WIDE_CHILD(2, lo_)
@@ -170,6 +230,11 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
         RR_WIDE_CHILD(7, hi_)
     }
 #undef RR_WIDE_CHILD
+#undef RR_WIDE_Q
+    const uint32_t int_mask  = byte_msbs(m0) | (byte_msbs(m1) << 4);
+    const uint32_t leaf_mask = byte_msbs(((m0 << 1) | (m0 << 2)) & ~m0) | (byte_msbs(((m1 << 1) | (m1 << 2)) & ~m1) << 4);
+    const uint32_t ihit      = hits & int_mask;
+    uint32_t       lhit      = hits & leaf_mask;
 
     // Leaf slots: test their triangles in visit order.
     while (lhit)
@@ -177,11 +242,12 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
         const uint32_t i    = __ffs(lhit) - 1;
         lhit &= lhit - 1;
         const uint32_t meta = ((i < 4 ? m0 : m1) >> (8 * (i & 3))) & 0xffu;
-        const uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+        uint32_t       cnt = (meta >> 5) & 3u;
+        const uint32_t off = meta & 31u;
         if (tri_base + off + cnt > tlim)
         {
             raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
-            continue;
+            cnt = 0;
         }
         for (uint32_t j = 0; j < cnt; ++j)
         {
@@ -194,10 +260,12 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
             {
                 s.ct   = t;
                 s.best = ti;
-                if (kAny) return true;
+                if (kAny) done = true;
             }
         }
+        if (kAny && done) break;
     }
+    if (kAny && done) return true;
 
     if (ihit)
     {
@@ -212,12 +280,12 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
                 }
                 else
                 {
-                    for (int k = 0; k < kWideShortStack; ++k) st.g[s.gsp + k] = st.s[k];
+                    for (int k = 0; k < kWideShortStack; ++k) st.g[s.gsp + k] = st.at(k);
                     s.gsp += kWideShortStack;
                     s.sp = 0;
                 }
             }
-            st.s[s.sp++] = WideEntry{s.gbase, s.gbits};
+            st.at(s.sp++) = WideEntry{s.gbase, s.gbits};
         }
         s.gbase             = child_base;
         s.gbits             = imask | (ihit << 8);

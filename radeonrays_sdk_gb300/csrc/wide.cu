@@ -98,6 +98,34 @@ __device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
     return n;
 }
 
+constexpr uint32_t kLeafMax = 1;  // triangles per leaf slot (2-bit count in the meta byte)
+
+// Leaves (binary leaf node indices, left to right) of the subtree at `root`,
+// stopping as soon as there are more than kLeafMax; returns their count or
+// kLeafMax + 1.
+__device__ __forceinline__ uint32_t collect_leaves(const BvhNode* nodes, uint32_t root, uint32_t* out)
+{
+    uint32_t stack[kLeafMax + 1];
+    int      sp  = 0;
+    uint32_t cnt = 0;
+    stack[sp++]  = root;
+    while (sp > 0)
+    {
+        const uint32_t a  = stack[--sp];
+        const uint32_t c0 = __ldg(&nodes[a].child0);
+        if (c0 == kInvalid)
+        {
+            if (cnt == kLeafMax) return kLeafMax + 1;
+            out[cnt++] = a;
+            continue;
+        }
+        if (sp + 2 > (int)kLeafMax + 1) return kLeafMax + 1;
+        stack[sp++] = __ldg(&nodes[a].child1);
+        stack[sp++] = c0;
+    }
+    return cnt;
+}
+
 // Warp-aggregated atomicAdd over a full warp (all 32 lanes must call it):
 // every lane adds v and gets its own offset.
 __device__ __forceinline__ uint32_t warp_add(uint32_t* ctr, uint32_t v)
@@ -239,8 +267,30 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
                 ++nc;
             }
         }
+        // Leaf clusters: an internal child left over with at most kLeafMax
+        // triangles becomes one leaf slot holding them (a wide node for it
+        // would cost a fetch for a few triangle slots).
+        uint32_t ctri[8][kLeafMax];
+        uint32_t ccnt[8];
+        for (int k = 0; k < nc; ++k)
+        {
+            if (!cint[k])
+            {
+                ctri[k][0] = ch[k];
+                ccnt[k]    = 1;
+                continue;
+            }
+            ccnt[k] = collect_leaves(nodes, ch[k], ctri[k]);
+            if (ccnt[k] <= kLeafMax) cint[k] = false;
+        }
         uint32_t n_int = 0, n_leaf = 0;
-        for (int k = 0; k < nc; ++k) (cint[k] ? n_int : n_leaf) += 1;
+        for (int k = 0; k < nc; ++k)
+        {
+            if (cint[k])
+                ++n_int;
+            else
+                n_leaf += ccnt[k];
+        }
         // Allocate (warp-aggregated over the full warp; inactive lanes add 0).
         __syncwarp();
         const uint32_t child_base = warp_add(&ctl->wide_count, n_int);
@@ -330,23 +380,26 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
                 }
                 else
                 {
-                    w.meta[slot] = (uint8_t)((1u << 5) | rl);
-                    BvhNode lf = load_node(nodes, ch[k]);
-                    WideTri t;
-                    t.v0[0] = lf.a0[0];
-                    t.v0[1] = lf.a0[1];
-                    t.v0[2] = lf.a0[2];
-                    t.prim  = lf.child1;
-                    t.v1[0] = lf.a1[0];
-                    t.v1[1] = lf.a1[1];
-                    t.v1[2] = lf.a1[2];
-                    t.pad1  = 0;
-                    t.v2[0] = lf.b0[0];
-                    t.v2[1] = lf.b0[1];
-                    t.v2[2] = lf.b0[2];
-                    t.pad2  = 0;
-                    wt[tri_base + rl] = t;
-                    ++rl;
+                    w.meta[slot] = (uint8_t)((ccnt[k] << 5) | rl);
+                    for (uint32_t j = 0; j < ccnt[k]; ++j)
+                    {
+                        BvhNode lf = load_node(nodes, ctri[k][j]);
+                        WideTri t;
+                        t.v0[0] = lf.a0[0];
+                        t.v0[1] = lf.a0[1];
+                        t.v0[2] = lf.a0[2];
+                        t.prim  = lf.child1;
+                        t.v1[0] = lf.a1[0];
+                        t.v1[1] = lf.a1[1];
+                        t.v1[2] = lf.a1[2];
+                        t.pad1  = 0;
+                        t.v2[0] = lf.b0[0];
+                        t.v2[1] = lf.b0[1];
+                        t.v2[2] = lf.b0[2];
+                        t.pad2  = 0;
+                        wt[tri_base + rl] = t;
+                        ++rl;
+                    }
                 }
             }
             else

@@ -107,7 +107,8 @@ class RRSceneBuildInput(C.Structure):
 
 class RRCudaTraversalOptions(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
-                ("blocks_per_sm", C.c_uint32), ("collect_stats", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("blocks_per_sm", C.c_uint32), ("collect_stats", C.c_uint32), ("ray_order", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class RRCudaTraversalStats(C.Structure):
@@ -331,9 +332,10 @@ class Context:
         return hits
 
     # -- options and diagnostics
-    def set_traversal(self, traversal=RR_CUDA_TRAVERSAL_AUTO, block_size=0, blocks_per_sm=0, collect_stats=0):
+    def set_traversal(self, traversal=RR_CUDA_TRAVERSAL_AUTO, block_size=0, blocks_per_sm=0, collect_stats=0,
+                      ray_order=0):
         o = RRCudaTraversalOptions(C.sizeof(RRCudaTraversalOptions), traversal, block_size, blocks_per_sm,
-                                   collect_stats)
+                                   collect_stats, ray_order)
         check(self.L.rrCudaSetTraversalOptions(self.ctx, C.byref(o)), "rrCudaSetTraversalOptions")
 
     def device_errors(self) -> int:

@@ -14,16 +14,19 @@ from gpu_util import INVALID, build, tie_only_mismatch, to_dev, trace
 
 pytestmark = pytest.mark.gpu
 
-BINARY, WIDE = 1, 2
+BINARY, WIDE, PERSISTENT = 1, 2, 3
 
 
 @pytest.mark.parametrize("name", MESH_FIXTURES)
-def test_binary_trace_bit_exact_on_fixtures(ctx, orc, name):
+@pytest.mark.parametrize("trav", [BINARY, PERSISTENT])
+def test_binary_trace_bit_exact_on_fixtures(ctx, orc, name, trav):
+    """Both binary-node kernels (one thread per ray, and persistent refill)
+    visit nodes in the reference order: bit-identical records."""
     g = golden(name)
     res = build(ctx, g["vertices"], g["indices"], node_format=1)
     for q in (0, 1):
         for o in (0, 1):
-            got = trace(ctx, res, g["rays"], query=q, output=o, traversal=BINARY)
+            got = trace(ctx, res, g["rays"], query=q, output=o, traversal=trav)
             assert np.array_equal(got, g[f"hits_q{q}_o{o}"]), (q, o)
     assert ctx.device_errors() == 0
 
@@ -54,6 +57,7 @@ def test_config0_plain_and_wide(ctx, orc):
     want = orc.trace(nodes, rays, threads=16)
     plain = trace(ctx, res, rays, traversal=BINARY)
     assert np.array_equal(plain, want)
+    assert np.array_equal(trace(ctx, res, rays, traversal=PERSISTENT), want)
     wide = trace(ctx, res, rays, traversal=WIDE)
     assert np.array_equal(wide[:, 2] != INVALID, want[:, 2] != INVALID)
     ties = tie_only_mismatch(orc, rays, wide, want, v, i)
@@ -70,6 +74,7 @@ def test_heightfield_incoherent_plain_and_wide(ctx, orc):
     for q in (0, 1):
         want = orc.trace(nodes, rays, query=q, threads=16)
         assert np.array_equal(trace(ctx, res, rays, query=q, traversal=BINARY), want)
+        assert np.array_equal(trace(ctx, res, rays, query=q, traversal=PERSISTENT), want)
     want = orc.trace(nodes, rays, threads=16)
     wide = trace(ctx, res, rays, traversal=WIDE)
     assert np.array_equal(wide[:, 2] != INVALID, want[:, 2] != INVALID)
