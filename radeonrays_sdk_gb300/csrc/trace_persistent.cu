@@ -25,6 +25,7 @@ namespace
 constexpr int      kPBlock    = 128;
 constexpr int      kPShort    = 32;   // shared short-stack entries per thread
 constexpr uint32_t kPSpillCap = 256;  // global spill entries per thread (binary LBVH depth <= 64)
+constexpr uint32_t kPRefillMin = 8;   // idle lanes that trigger a refill
 
 struct PRay
 {
@@ -60,6 +61,8 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
     }
     const NodeView nd = load_binary_node(nodes, s.addr);
     ++nf;
+    // Single exit: the internal-node and leaf paths rejoin before the pop.
+    bool pop = true, done = false;
     if (nd.child0 != kInvalid)
     {
         float a0, a1, b0, b1;
@@ -91,7 +94,7 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
                 st.at(s.sp++) = deferred;
             }
             s.addr = next;
-            return false;
+            pop    = false;
         }
     }
     else
@@ -101,18 +104,25 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
         {
             s.ct    = t;
             s.caddr = s.addr;
-            if (kAny) return true;
+            if (kAny) done = true;
         }
     }
-    if (s.sp == 0)
+    if (pop && !done)
     {
-        if (s.gsp == 0) return true;
-        s.gsp -= kPShort;
-        for (int k = 0; k < kPShort; ++k) st.at(k) = st.g[s.gsp + k];
-        s.sp = kPShort;
+        if (s.sp == 0 && s.gsp == 0)
+            done = true;
+        else
+        {
+            if (s.sp == 0)
+            {
+                s.gsp -= kPShort;
+                for (int k = 0; k < kPShort; ++k) st.at(k) = st.g[s.gsp + k];
+                s.sp = kPShort;
+            }
+            s.addr = st.at(--s.sp);
+        }
     }
-    s.addr = st.at(--s.sp);
-    return false;
+    return done;
 }
 
 template <bool kAny, bool kFull, bool kStats>
@@ -133,22 +143,44 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
 
     PRay     s;
     uint32_t gid = kInvalid, nf = 0;
-    bool     active = false, exhausted = false;
+    bool     active = false, pending = false, exhausted = false;
     for (;;)
     {
+        __syncwarp();
+        // Lanes whose ray finished write its hit and take a new ray together,
+        // once at least kPRefillMin lanes are idle (or no ray is left).
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-        if (idle && !exhausted)
+        if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
         {
-            const uint32_t n      = __popc(idle);
-            const int      leader = __ffs(idle) - 1;
-            uint32_t       base   = 0;
-            if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
-            base      = __shfl_sync(0xffffffffu, base, leader);
-            exhausted = base + n >= count;
+            const uint32_t n    = exhausted ? 0u : __popc(idle);
+            uint32_t       base = 0;
+            if (n)
+            {
+                const int leader = __ffs(idle) - 1;
+                if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+                base      = __shfl_sync(0xffffffffu, base, leader);
+                exhausted = base + n >= count;
+            }
             if (!active)
             {
+                if (pending)
+                {
+                    if (s.caddr != kInvalid)
+                    {
+                        const NodeView nd = load_binary_node(nodes, s.caddr);
+                        write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                    }
+                    else
+                        write_miss<kFull>(a.hits, gid);
+                    if (kStats)
+                    {
+                        atomicAdd(&a.words->rays, 1ull);
+                        atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
+                    }
+                    pending = false;
+                }
                 const uint32_t my = base + __popc(idle & lt);
-                if (my < count)
+                if (n && my < count)
                 {
                     gid = my;
                     if (a.empty)
@@ -169,26 +201,12 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                 }
             }
         }
-        if (__ballot_sync(0xffffffffu, active) == 0)
-        {
-            if (exhausted) break;
-            continue;
-        }
+        const uint32_t amask = __ballot_sync(0xffffffffu, active);
+        if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
         if (active && p_step<kAny>(s, nodes, a.node_limit, st, a.words, nf))
         {
-            if (s.caddr != kInvalid)
-            {
-                const NodeView nd = load_binary_node(nodes, s.caddr);
-                write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
-            }
-            else
-                write_miss<kFull>(a.hits, gid);
-            if (kStats)
-            {
-                atomicAdd(&a.words->rays, 1ull);
-                atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
-            }
-            active = false;
+            active  = false;
+            pending = true;
         }
     }
 }
