@@ -45,6 +45,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "incoherent closest-hit Mrays/s + p99 batch latency, chosen vs plain on same GB300"
+# RRCudaTraversal value -> kernel name (the key of profiles/traffic.json)
+KERNELS = {1: "k_trace_binary", 2: "k_trace_wide", 3: "k_trace_persistent"}
 
 
 def parse():
@@ -63,7 +65,9 @@ def parse():
     ap.add_argument("--block", type=int, default=0, help="chosen kernel threads per block (0: library default)")
     ap.add_argument("--per-sm", type=int, default=0, help="chosen kernel resident blocks per SM (0: occupancy)")
     ap.add_argument("--ray-order", type=int, default=0, help="chosen kernel: 0 default, 1 given order, 2 sorted")
-    ap.add_argument("--chosen", type=int, default=2, help="chosen traversal: 2 wide (8-wide nodes), 3 binary persistent")
+    ap.add_argument("--chosen", type=int, default=0,
+                    help="chosen traversal: 0 autotuned (rrCudaAutotuneTraversal), 2 wide (8-wide nodes), "
+                         "3 binary persistent")
     return ap.parse_args()
 
 
@@ -162,7 +166,9 @@ def describe(args, ntri):
                         "rays per GPU (origins uniform in the mesh box, directions uniform on the sphere), "
                         "closest hit, full RRHit output",
             "triangles": ntri, "rays_per_gpu": args.rays, "query": "closest", "output": "full_hit",
-            "chosen": "8-wide nodes, 8-bit conservative child bounds, persistent warp-scheduled kernel",
+            "chosen": "autotuned (rrCudaAutotuneTraversal) among: plain binary, persistent lane-refill binary "
+                      "(reference visit order), persistent 8-wide nodes with 8-bit conservative child bounds "
+                      "(rays in given or sorted order)",
             "plain": "64-byte binary nodes, one thread per ray, reference visit order",
             "l2": "inputs larger than L2 (rays 32 B x rays, BVH > 129 MB); no flush needed",
             "parallelism": "replicas (rays sharded per GPU, BVH replicated)"}
@@ -282,14 +288,20 @@ def run_ours(args):
                                   rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hitb, sb, ext), "rrCmdIntersect")
 
     out = {}
+    # Chosen path: the autotuner's pick (untimed tuning on the workload's rays)
+    # unless a kernel is forced on the command line.
+    chosen_trav, chosen_order, tuned = args.chosen, args.ray_order, None
+    if args.chosen == 0 and args.only != "plain":
+        tuned = ctx.autotune(bvh, rays_d, hits=hits_d, scratch=scratch_t)
+        chosen_trav, chosen_order = tuned["traversal"], tuned["ray_order"]
     # Fetch counters of each kernel (untimed run) -> algorithmic bytes.
-    for name, trav in (("chosen", args.chosen), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
+    for name, trav in (("chosen", chosen_trav), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
         if args.only and args.only != name:
             continue
         if name == "plain" and args.no_plain:
             continue
         shape = (args.block, args.per_sm) if name == "chosen" else (0, 0)
-        order = args.ray_order if name == "chosen" else 0
+        order = chosen_order if name == "chosen" else 0
         ctx.set_traversal(trav, *shape, collect_stats=1, ray_order=order)
         trace_step()
         torch.cuda.synchronize()
@@ -302,7 +314,7 @@ def run_ours(args):
             per, total = time_steps(trace_step, args.steps, args.warmup, ws, stream)
         total = max_over_ranks(total, ws)
         out[name] = {"per": per, "total": total, "alg_bytes": alg, "stats": st, "clocks": clocks.summary(),
-                     "hits": hits_d[: 1 << 16].cpu().numpy().copy()}
+                     "hits": hits_d[: 1 << 16].cpu().numpy().copy(), "trav": trav, "order": order}
     assert ctx.device_errors() == 0, "device error word set during the benchmark"
 
     # ---- end to end through the C-ABI with pinned host buffers
@@ -333,9 +345,10 @@ def run_ours(args):
     mean_launch_s = statistics.mean(c["per"]) / 1e3
     achieved = c["alg_bytes"] / mean_launch_s / 1e9
     traffic = None
+    kernel = KERNELS.get(c["trav"], "k_trace_binary")
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        t = json.loads(tf.read_text()).get(f"trace_{key}")
+        t = json.loads(tf.read_text()).get(kernel)
         if t and t.get("dram_bytes_per_ray"):
             traffic = t["dram_bytes_per_ray"] * R
     line = {
@@ -352,6 +365,8 @@ def run_ours(args):
                      "node_fetches_per_ray": c["stats"]["node_fetches"] / R,
                      "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R},
         "clocks": c["clocks"], "gpu_launches": args.steps, "build": build, "traversal": key,
+        "chosen_kernel": {"kernel": kernel, "traversal": c["trav"], "ray_order": c["order"],
+                          "selected_by": "rrCudaAutotuneTraversal" if tuned else "command line"},
     }
     if "plain" in out and "chosen" in out:
         p = out["plain"]

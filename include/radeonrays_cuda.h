@@ -126,6 +126,27 @@ RR_API RRError rrCudaGetTraversalStats(RRContext context, RRCudaTraversalStats* 
  * (default 600000).  The reference waits forever (vlk/device.cpp:249-272). */
 RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
 
+/* Pick the fastest traversal for a workload and make it this context's
+ * traversal option (no reference counterpart: the reference has one kernel
+ * per query variant).  Times every applicable kernel -- plain binary, binary
+ * persistent, 8-wide with the rays in the given order and, for batches of
+ * 2^20 rays or more, 8-wide with the rays sorted -- on the caller's rays
+ * (their count is the sample size), three runs each on the context's stream,
+ * and keeps the fastest.  Results are cached per (GPU, buffer kind and size,
+ * query, output, ray-count octave) in the context and, when the environment
+ * variable RR_CUDA_TUNE_CACHE names a file, in that file across processes.
+ * Synchronous; hits and scratch (rrGetTraceMemoryRequirements(ray_count))
+ * are overwritten.  `chosen` (optional) receives the selection. */
+RR_API RRError rrCudaAutotuneTraversal(RRContext               context,
+                                       RRDevicePtr             scene_buffer,
+                                       RRIntersectQuery        query,
+                                       RRDevicePtr             rays,
+                                       uint32_t                ray_count,
+                                       RRIntersectQueryOutput  query_output,
+                                       RRDevicePtr             hits,
+                                       RRDevicePtr             scratch,
+                                       RRCudaTraversalOptions* chosen);
+
 /* Intersect without allocating anything and without a caller scratch buffer.
  * No counterpart in the reference API.
  *

@@ -127,6 +127,8 @@ struct Context
     RRCudaTraversalOptions topts{};
     uint32_t               wait_ms  = 600000;
     bool                   graphs   = true;
+    std::string            gpu_name;
+    std::map<std::string, RRCudaTraversalOptions> tuned;  // autotuner results by workload key
     std::map<uintptr_t, BufInfo> registry;
     ~Context()
     {
@@ -273,6 +275,64 @@ struct PinnedBlock
         return RR_ERROR_INTERNAL;                                    \
     }
 
+namespace
+{
+// The launch of one rrCmdIntersect: arguments from the buffers and the
+// traversal options, kernel chosen by the buffer kind and options.
+Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count, const uint32_t* indirect, void* hits,
+            uint8_t* scratch, int query, int output, const RRCudaTraversalOptions& o)
+{
+    TraceArgs a{};
+    a.bvh           = bvh;
+    a.rays          = rays;
+    a.ray_count     = ray_count;
+    a.indirect      = indirect;
+    a.hits          = hits;
+    a.scratch       = scratch;
+    a.scratch_bytes = trace_scratch_bytes(ray_count);
+    a.query         = query;
+    a.output        = output;
+    a.words         = ctx->words;
+    a.collect_stats = o.collect_stats ? 1 : 0;
+    a.block_size    = (int)o.block_size;
+    a.blocks_per_sm = (int)o.blocks_per_sm;
+    a.ray_order     = (int)o.ray_order;
+    a.sm_count      = ctx->sm_count;
+    auto    it      = ctx->registry.find((uintptr_t)bvh);
+    BufInfo bi;
+    if (it != ctx->registry.end()) bi = it->second;
+    const uint32_t trav  = o.traversal;
+    const uint32_t nodes = bi.n == 0 ? 0u : 2u * bi.n - 1u;
+    a.node_limit         = bi.kind == 0 ? kInvalid : nodes;
+    a.wide_limit         = bi.n > 1 ? bi.n - 1 : 1u;
+    a.tri_limit          = bi.n;
+    if (bi.kind == kKindScene)
+    {
+        SceneTraceArgs sa;
+        sa.base       = a;
+        sa.base.empty = bi.n == 0;
+        sa.xforms     = reinterpret_cast<const float*>(bvh + bi.xforms_off);
+        sa.inst       = reinterpret_cast<const InstanceDesc*>(bvh + bi.inst_off);
+        sa.inst_count = bi.n;
+        sa.use_wide   = bi.scene_wide && trav != RR_CUDA_TRAVERSAL_BINARY;
+        return [=](cudaStream_t s) { return launch_trace_scene(sa, s); };
+    }
+    // Geometry (registered) or an unknown buffer, traversed as binary nodes
+    // from the root like the reference (vlk/intersector.cpp:290).
+    a.empty             = (bi.kind == kKindGeom && bi.n == 0);
+    const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
+    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT) return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
+    if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
+    {
+        a.wide_nodes = reinterpret_cast<const WideNode*>(bvh + bi.wide_off);
+        a.wide_tris  = reinterpret_cast<const WideTri*>(bvh + bi.tris_off);
+        a.bounds     = reinterpret_cast<const uint32_t*>(bvh + bi.trailer_off + offsetof(Trailer, bounds));
+        return [=](cudaStream_t s) { return launch_trace_wide(a, s); };
+    }
+    return [=](cudaStream_t s) { return launch_trace_binary(a, s); };
+}
+}  // namespace
+
 extern "C" {
 
 RR_API RRError rrSetLogLevel(RRLogLevel log_level)
@@ -310,6 +370,11 @@ RR_API RRError rrCreateContext(uint32_t api_version, RRApi api, RRContext* conte
         std::unique_ptr<Context> c(new Context);
         check(cudaGetDevice(&c->device), "cudaGetDevice");
         check(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device), "sm count");
+        {
+            cudaDeviceProp prop{};
+            check(cudaGetDeviceProperties(&prop, c->device), "device properties");
+            c->gpu_name = prop.name;
+        }
         check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
         check(cudaMalloc(&c->words, sizeof(DeviceWords)), "cudaMalloc words");
         check(cudaMemset(c->words, 0, sizeof(DeviceWords)), "memset words");
@@ -517,58 +582,10 @@ RR_API RRError rrCmdIntersect(RRContext              context,
     RR_TRY({
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
-        uint8_t*    bvh = P(scene_buffer)->addr();
-        TraceArgs   a{};
-        a.bvh           = bvh;
-        a.rays          = P(rays)->addr();
-        a.ray_count     = ray_count;
-        a.indirect      = indirect_ray_count ? reinterpret_cast<const uint32_t*>(P(indirect_ray_count)->addr()) : nullptr;
-        a.hits          = P(hits)->addr();
-        a.scratch       = P(scratch)->addr();
-        a.scratch_bytes = trace_scratch_bytes(ray_count);
-        a.query         = query;
-        a.output        = query_output;
-        a.words         = ctx->words;
-        a.collect_stats = ctx->topts.collect_stats ? 1 : 0;
-        a.block_size    = (int)ctx->topts.block_size;
-        a.blocks_per_sm = (int)ctx->topts.blocks_per_sm;
-        a.ray_order     = (int)ctx->topts.ray_order;
-        a.sm_count      = ctx->sm_count;
-        auto     it     = ctx->registry.find((uintptr_t)bvh);
-        BufInfo  bi;
-        if (it != ctx->registry.end()) bi = it->second;
-        const uint32_t trav = ctx->topts.traversal;
-        const uint32_t nodes = bi.n == 0 ? 0u : 2u * bi.n - 1u;
-        a.node_limit         = bi.kind == 0 ? kInvalid : nodes;
-        a.wide_limit         = bi.n > 1 ? bi.n - 1 : 1u;
-        a.tri_limit          = bi.n;
-        if (bi.kind == kKindScene)
-        {
-            SceneTraceArgs sa;
-            sa.base       = a;
-            sa.base.empty = bi.n == 0;
-            sa.xforms     = reinterpret_cast<const float*>(bvh + bi.xforms_off);
-            sa.inst       = reinterpret_cast<const InstanceDesc*>(bvh + bi.inst_off);
-            sa.inst_count = bi.n;
-            sa.use_wide   = bi.scene_wide && trav != RR_CUDA_TRAVERSAL_BINARY;
-            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_scene(sa, s); });
-            return RR_SUCCESS;
-        }
-        // Geometry (registered) or an unknown buffer, traversed as binary nodes
-        // from the root like the reference (vlk/intersector.cpp:290).
-        a.empty             = (bi.kind == kKindGeom && bi.n == 0);
-        const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
-        if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT)
-            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_persistent(a, s); });
-        else if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
-        {
-            a.wide_nodes = reinterpret_cast<const WideNode*>(bvh + bi.wide_off);
-            a.wide_tris  = reinterpret_cast<const WideTri*>(bvh + bi.tris_off);
-            a.bounds     = reinterpret_cast<const uint32_t*>(bvh + bi.trailer_off + offsetof(Trailer, bounds));
-            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_wide(a, s); });
-        }
-        else
-            record(S(command_stream), [=](cudaStream_t s) { return launch_trace_binary(a, s); });
+        const uint32_t* ind =
+            indirect_ray_count ? reinterpret_cast<const uint32_t*>(P(indirect_ray_count)->addr()) : nullptr;
+        record(S(command_stream), trace_op(ctx, P(scene_buffer)->addr(), P(rays)->addr(), ray_count, ind,
+                                           P(hits)->addr(), P(scratch)->addr(), query, query_output, ctx->topts));
         return RR_SUCCESS;
     })
 }
@@ -845,6 +862,122 @@ RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds)
     if (!context) return RR_ERROR_INVALID_PARAMETER;
     C(context)->wait_ms = milliseconds;
     return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
+                                       RRDevicePtr            scene_buffer,
+                                       RRIntersectQuery       query,
+                                       RRDevicePtr            rays,
+                                       uint32_t               ray_count,
+                                       RRIntersectQueryOutput query_output,
+                                       RRDevicePtr            hits,
+                                       RRDevicePtr            scratch,
+                                       RRCudaTraversalOptions* chosen)
+{
+    if (!context || !scene_buffer || !rays || !hits || !scratch || !ray_count) return RR_ERROR_INVALID_PARAMETER;
+    if (query != RR_INTERSECT_QUERY_CLOSEST && query != RR_INTERSECT_QUERY_ANY) return RR_ERROR_INVALID_PARAMETER;
+    if (query_output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && query_output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+        return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        uint8_t*    bvh = P(scene_buffer)->addr();
+        auto        it  = ctx->registry.find((uintptr_t)bvh);
+        BufInfo     bi;
+        if (it != ctx->registry.end()) bi = it->second;
+        const bool has_wide = (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0) ||
+                              (bi.kind == kKindScene && bi.scene_wide);
+        // Workload key: device, buffer kind and size, query, output, ray-count octave.
+        uint32_t octave = 0;
+        while ((1ull << (octave + 1)) <= ray_count) ++octave;
+        const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.n) + "|" +
+                                std::to_string((int)query) + "|" + std::to_string((int)query_output) + "|" +
+                                std::to_string(octave);
+        auto hit = ctx->tuned.find(key);
+        const char* cache_path = std::getenv("RR_CUDA_TUNE_CACHE");
+        if (hit == ctx->tuned.end() && cache_path)
+        {
+            if (FILE* f = std::fopen(cache_path, "r"))
+            {
+                char     line[512];
+                while (std::fgets(line, sizeof(line), f))
+                {
+                    char*    tab = std::strchr(line, '\t');
+                    unsigned t = 0, ro = 0, bps = 0;
+                    if (!tab) continue;
+                    *tab = 0;
+                    if (key == line && std::sscanf(tab + 1, "%u %u %u", &t, &ro, &bps) == 3)
+                    {
+                        RRCudaTraversalOptions o{};
+                        o.struct_size   = sizeof(o);
+                        o.traversal     = t;
+                        o.ray_order     = ro;
+                        o.blocks_per_sm = bps;
+                        ctx->tuned[key] = o;
+                    }
+                }
+                std::fclose(f);
+            }
+            hit = ctx->tuned.find(key);
+        }
+        if (hit == ctx->tuned.end())
+        {
+            std::vector<RRCudaTraversalOptions> cand;
+            auto add = [&](uint32_t trav, uint32_t order) {
+                RRCudaTraversalOptions o{};
+                o.struct_size = sizeof(o);
+                o.traversal   = trav;
+                o.ray_order   = order;
+                cand.push_back(o);
+            };
+            add(RR_CUDA_TRAVERSAL_BINARY, 0);
+            if (bi.kind != kKindScene) add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
+            if (has_wide)
+            {
+                add(RR_CUDA_TRAVERSAL_WIDE, 1);
+                if (bi.kind == kKindGeom && ray_count >= (1u << 20)) add(RR_CUDA_TRAVERSAL_WIDE, 2);
+            }
+            cudaEvent_t e0, e1;
+            check(cudaEventCreate(&e0), "event");
+            check(cudaEventCreate(&e1), "event");
+            float best_ms = 1e30f;
+            RRCudaTraversalOptions best = cand[0];
+            for (const auto& o : cand)
+            {
+                Op op = trace_op(ctx, bvh, P(rays)->addr(), ray_count, nullptr, P(hits)->addr(), P(scratch)->addr(),
+                                 query, query_output, o);
+                check(op(ctx->stream), "tune warm-up");
+                check(cudaEventRecord(e0, ctx->stream), "event");
+                for (int r = 0; r < 3; ++r) check(op(ctx->stream), "tune run");
+                check(cudaEventRecord(e1, ctx->stream), "event");
+                check(cudaEventSynchronize(e1), "event");
+                float ms = 0.f;
+                check(cudaEventElapsedTime(&ms, e0, e1), "event");
+                RR_LOG_INFO("autotune %s: traversal %u order %u -> %.3f ms", key.c_str(), o.traversal, o.ray_order,
+                            ms / 3.f);
+                if (ms < best_ms)
+                {
+                    best_ms = ms;
+                    best    = o;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            ctx->tuned[key] = best;
+            if (cache_path)
+                if (FILE* f = std::fopen(cache_path, "a"))
+                {
+                    std::fprintf(f, "%s\t%u %u %u\n", key.c_str(), best.traversal, best.ray_order, best.blocks_per_sm);
+                    std::fclose(f);
+                }
+            hit = ctx->tuned.find(key);
+        }
+        RRCudaTraversalOptions o = hit->second;
+        o.collect_stats          = 0;
+        ctx->topts               = o;
+        if (chosen) *chosen = o;
+        return RR_SUCCESS;
+    })
 }
 
 }  // extern "C"

@@ -153,6 +153,8 @@ PROTOTYPES = {
     "rrCudaGetTraversalStats": [_P, C.POINTER(RRCudaTraversalStats)],
     "rrCudaSetWaitTimeout": [_P, C.c_uint32],
     "rrCudaIntersectNoAlloc": [_P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
+    "rrCudaAutotuneTraversal": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P,
+                                C.POINTER(RRCudaTraversalOptions)],
 }
 
 _LIB = None
@@ -337,6 +339,23 @@ class Context:
         o = RRCudaTraversalOptions(C.sizeof(RRCudaTraversalOptions), traversal, block_size, blocks_per_sm,
                                    collect_stats, ray_order)
         check(self.L.rrCudaSetTraversalOptions(self.ctx, C.byref(o)), "rrCudaSetTraversalOptions")
+
+    def autotune(self, bvh, rays, query=RR_INTERSECT_QUERY_CLOSEST, output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT,
+                 hits=None, scratch=None) -> dict:
+        """Time the applicable traversal kernels on `rays` and select the
+        fastest for this context (rrCudaAutotuneTraversal)."""
+        torch = _torch()
+        R = rays.shape[0]
+        if hits is None:
+            hits = torch.empty((R, 4) if output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT else (R,), dtype=torch.int32,
+                               device=rays.device)
+        if scratch is None:
+            scratch = torch.empty(self.trace_scratch_bytes(R), dtype=torch.uint8, device=rays.device)
+        o = RRCudaTraversalOptions()
+        check(self.L.rrCudaAutotuneTraversal(self.ctx, self.ptr(bvh), query, self.ptr(rays), R, output,
+                                             self.ptr(hits), self.ptr(scratch), C.byref(o)),
+              "rrCudaAutotuneTraversal")
+        return {"traversal": o.traversal, "ray_order": o.ray_order, "blocks_per_sm": o.blocks_per_sm}
 
     def device_errors(self) -> int:
         v = C.c_uint32()

@@ -192,3 +192,27 @@ def test_argument_errors_with_context(ctx):
         rr.RR_ERROR_INVALID_PARAMETER
     assert L.rrCmdIntersect(ctx.ctx, fake, 5, fake, 1, None, 0, fake, fake, cs) == rr.RR_ERROR_INVALID_PARAMETER
     ctx.release_stream(cs)
+
+
+def test_autotuner_selects_a_kernel_and_results_stay_exact(ctx, orc, tmp_path, monkeypatch):
+    """rrCudaAutotuneTraversal times the candidate kernels, sets the fastest on
+    the context and caches it; the tuned path keeps the parity bar."""
+    from radeonrays_sdk_gb300 import scenes
+    monkeypatch.setenv("RR_CUDA_TUNE_CACHE", str(tmp_path / "tune.tsv"))
+    v, i, rays = scenes.config1(grid=257, nrays=1 << 18)
+    res = build(ctx, v, i, node_format=1)
+    rays_d = to_dev(rays)
+    choice = ctx.autotune(res, rays_d)
+    assert choice["traversal"] in (BINARY, WIDE, PERSISTENT)
+    assert (tmp_path / "tune.tsv").exists()
+    nodes, _, _ = orc.build_mesh(v, i)
+    want = orc.trace(nodes, rays, threads=16)
+    got = hits_np_of(ctx.intersect(res, rays_d))
+    assert np.array_equal(got[:, 2] != INVALID, want[:, 2] != INVALID)
+    tie_only_mismatch(orc, rays, got, want, v, i)
+    assert ctx.autotune(res, rays_d) == choice  # served from the cache
+    ctx.set_traversal(0)
+
+
+def hits_np_of(t):
+    return t.cpu().numpy().view(np.uint32)
