@@ -147,6 +147,63 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext               context,
                                        RRDevicePtr             scratch,
                                        RRCudaTraversalOptions* chosen);
 
+/* Build `count` geometries in one fused set of launches (no counterpart in
+ * the reference API, which records one rrCmdBuildGeometry per geometry,
+ * radeonrays.h:322-328).  Geometry i reads build_inputs[i] and uses
+ * temporary_buffers[i] and geometry_buffers[i], sized by
+ * rrGetGeometryBuildMemoryRequirements for build_inputs[i] alone; all share
+ * build_options.  The results are those of count separate rrCmdBuildGeometry
+ * calls.  Buffers of different geometries must not overlap
+ * (RR_ERROR_INVALID_PARAMETER).  The launch count does not depend on count:
+ * every kernel of the build covers all geometries.
+ *
+ * Consecutive rrCmdBuildGeometry calls recorded into one internal command
+ * stream (rrAllocateCommandStream) with the same options and disjoint buffers
+ * are fused the same way at submission (environment variable
+ * RR_CUDA_FUSE_BUILDS=0 turns that off); on an external stream every call
+ * runs at once. */
+RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
+                                        uint32_t                    count,
+                                        const RRGeometryBuildInput* build_inputs,
+                                        const RRBuildOptions*       build_options,
+                                        const RRDevicePtr*          temporary_buffers,
+                                        const RRDevicePtr*          geometry_buffers,
+                                        RRCommandStream             command_stream);
+
+/* ---- many intersection requests in one launch ---------------------------
+ * No counterpart in the reference API (one rrCmdIntersect dispatches one
+ * query over one buffer, radeonrays.h:391-400).  A serving loop packs the
+ * requests it admits into one call: every request's rays are traced by one
+ * persistent launch whose lanes take rays from all requests.  Each request is
+ * traced exactly like rrCmdIntersect with RR_CUDA_TRAVERSAL_BINARY (the
+ * reference's visit order), so its hits do not depend on what it is packed
+ * with. */
+typedef struct
+{
+    RRDevicePtr            geometry;   /* geometry result buffer (rrCmdBuildGeometry); scenes are not accepted */
+    RRIntersectQuery       query;
+    RRIntersectQueryOutput output;
+    RRDevicePtr            rays;       /* RRRay[ray_count] */
+    uint32_t               ray_count;
+    RRDevicePtr            hits;       /* RRHit[ray_count], or uint32_t[ray_count] for INSTANCE_ID output */
+} RRCudaIntersectRequest;
+
+/* Scratch bytes of rrCudaCmdIntersectBatch for `request_count` requests with
+ * `total_ray_count` rays in all. */
+RR_API RRError rrCudaGetIntersectBatchMemoryRequirements(RRContext context,
+                                                         uint32_t  request_count,
+                                                         uint32_t  total_ray_count,
+                                                         size_t*   scratch_size);
+
+/* Record (or, on an external stream, enqueue) one launch over all requests.
+ * The total ray count must be below 2^32.  A scene buffer as `geometry`
+ * returns RR_ERROR_NOT_IMPLEMENTED. */
+RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
+                                       uint32_t                      request_count,
+                                       const RRCudaIntersectRequest* requests,
+                                       RRDevicePtr                   scratch,
+                                       RRCommandStream               command_stream);
+
 /* Intersect without allocating anything and without a caller scratch buffer.
  * No counterpart in the reference API.
  *

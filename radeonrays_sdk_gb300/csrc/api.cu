@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <map>
 #include <memory>
@@ -89,15 +90,61 @@ struct Context;
 
 using Op = std::function<cudaError_t(cudaStream_t)>;
 
+// Device memory owned by a recorded op (the descriptors of a fused build).
+struct DeviceBlock
+{
+    void* p = nullptr;
+    explicit DeviceBlock(size_t bytes)
+    {
+        if (bytes) check(cudaMalloc(&p, bytes), "cudaMalloc build descriptors");
+    }
+    ~DeviceBlock()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+// A geometry build recorded into a command stream and not yet turned into an
+// op: consecutive ones are fused into one build (build_batch_op).
+struct PendingGeom
+{
+    MeshArgs   ma;
+    GeomLayout L;
+    uint8_t*   scratch;
+    uint8_t*   result;
+};
+
+// Disjoint byte ranges [start, end) of device memory.
+struct RangeSet
+{
+    std::map<uintptr_t, uintptr_t> r;
+    bool overlaps(const uint8_t* p, size_t n) const
+    {
+        if (!p || !n) return false;
+        const uintptr_t s = (uintptr_t)p, e = s + n;
+        auto            it = r.lower_bound(e);  // first range starting at or after e
+        if (it == r.begin()) return false;
+        --it;
+        return it->second > s;
+    }
+    void add(const uint8_t* p, size_t n)
+    {
+        if (p && n) r[(uintptr_t)p] = (uintptr_t)p + n;
+    }
+};
+
 struct CommandStream
 {
-    Context*        ctx      = nullptr;
-    bool            external = false;
-    cudaStream_t    stream   = nullptr;
-    std::vector<Op> ops;
-    cudaGraphExec_t graph      = nullptr;
-    size_t          graph_ops  = 0;
-    bool            graph_failed = false;
+    Context*                 ctx      = nullptr;
+    bool                     external = false;
+    cudaStream_t             stream   = nullptr;
+    std::vector<Op>          ops;
+    std::vector<PendingGeom> pending;
+    RangeSet                 pending_ranges;
+    bool                     want_graph   = false;  // an op enqueues many launches
+    cudaGraphExec_t          graph        = nullptr;
+    size_t                   graph_ops    = 0;
+    bool                     graph_failed = false;
     ~CommandStream()
     {
         if (graph) cudaGraphExecDestroy(graph);
@@ -127,12 +174,51 @@ struct Context
     RRCudaTraversalOptions topts{};
     uint32_t               wait_ms  = 600000;
     bool                   graphs   = true;
+    bool                   fuse_builds = true;  // fuse consecutive geometry builds of a command stream
     std::string            gpu_name;
     std::map<std::string, RRCudaTraversalOptions> tuned;  // autotuner results by workload key
     std::map<uintptr_t, BufInfo> registry;
+    // Ops run at once on external streams, kept (with the memory they own)
+    // until an event after them has completed; ops enqueued into a stream
+    // capture are kept until the context goes.
+    std::deque<std::pair<cudaEvent_t, Op>> retired;
+    std::vector<Op>                        kept;
+    void retire(Op&& op, cudaStream_t s)
+    {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cap);
+        if (cap != cudaStreamCaptureStatusNone)
+        {
+            kept.push_back(std::move(op));
+            return;
+        }
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventRecord(ev, s) != cudaSuccess)
+        {
+            cudaGetLastError();
+            if (ev) cudaEventDestroy(ev);
+            cudaStreamSynchronize(s);
+            return;
+        }
+        retired.emplace_back(ev, std::move(op));
+        while (!retired.empty() && cudaEventQuery(retired.front().first) != cudaErrorNotReady)
+        {
+            cudaEventDestroy(retired.front().first);
+            retired.pop_front();
+        }
+        cudaGetLastError();
+    }
     ~Context()
     {
         if (stream) cudaStreamSynchronize(stream);
+        for (auto& r : retired)
+        {
+            cudaEventSynchronize(r.first);
+            cudaEventDestroy(r.first);
+        }
+        retired.clear();
+        kept.clear();
         if (words) cudaFree(words);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -157,13 +243,99 @@ inline CommandStream* S(RRCommandStream s) { return reinterpret_cast<CommandStre
 inline DevicePtr*     P(RRDevicePtr p) { return reinterpret_cast<DevicePtr*>(p); }
 inline Event*         E(RREvent e) { return reinterpret_cast<Event*>(e); }
 
-void record(CommandStream* cs, Op op)
+// Whether a geometry build touches a byte of scratch or result that builds
+// already in `used` touch (then they cannot run fused: they would overwrite
+// each other's state).  Otherwise its ranges are added.
+bool claim_build_ranges(RangeSet& used, const PendingGeom& g)
+{
+    if (used.overlaps(g.scratch, g.L.s_total) || used.overlaps(g.result, g.L.total)) return false;
+    if (g.scratch && g.result && g.L.s_total && g.scratch < g.result + g.L.total && g.result < g.scratch + g.L.s_total)
+        return false;
+    used.add(g.scratch, g.L.s_total);
+    used.add(g.result, g.L.total);
+    return true;
+}
+
+// The op of a fused build: descriptors of every geometry copied to a device
+// block the op owns, then one launch_build_batch.  A single geometry keeps
+// its descriptor in its own scratch (no allocation).
+Op build_batch_op(Context* ctx, const std::vector<PendingGeom>& geoms, bool* many_launches)
+{
+    DeviceWords* words = ctx->words;
+    const int    sms   = ctx->sm_count;
+    *many_launches     = false;
+    if (geoms.size() == 1)
+    {
+        const PendingGeom pg = geoms[0];
+        return [=](cudaStream_t s) { return launch_build_mesh(pg.ma, pg.L, pg.scratch, pg.result, words, sms, s); };
+    }
+    const uint32_t       count = (uint32_t)geoms.size();
+    const size_t         bytes = batch_desc_bytes(count);
+    std::vector<uint8_t> host(bytes, 0);
+    BuildItem*           hi = nullptr;
+    uint32_t *           htp = nullptr, *hlp = nullptr;
+    BatchCtl*            hctl = nullptr;
+    batch_carve(host.data(), count, &hi, &htp, &hlp, &hctl);
+    uint64_t tiles = 0, prims = 0;
+    uint32_t max_n = 0;
+    for (uint32_t i = 0; i < count; ++i)
+    {
+        const PendingGeom& g = geoms[i];
+        hi[i]  = make_build_item(g.L, g.ma.vertices, g.ma.stride_floats, g.ma.indices, g.ma.index16, g.scratch,
+                                 g.result);
+        htp[i] = (uint32_t)tiles;
+        tiles += g.L.sort_tiles;
+        prims += g.L.n;
+        max_n  = std::max(max_n, g.L.n);
+    }
+    if (tiles >= (1ull << 26)) throw std::runtime_error("fused build too large (more than 2^26 sort tiles)");
+    htp[count] = (uint32_t)tiles;
+    auto dev   = std::make_shared<DeviceBlock>(bytes);
+    check(cudaMemcpy(dev->p, host.data(), bytes, cudaMemcpyHostToDevice), "copy build descriptors");
+    BuildItem* di  = nullptr;
+    uint32_t * dtp = nullptr, *dlp = nullptr;
+    BatchCtl*  dctl = nullptr;
+    batch_carve(reinterpret_cast<uint8_t*>(dev->p), count, &di, &dtp, &dlp, &dctl);
+    BatchArgs b{};
+    b.items        = di;
+    b.tile_prefix  = dtp;
+    b.level_prefix = dlp;
+    b.ctl          = dctl;
+    b.count        = count;
+    b.total_tiles  = (uint32_t)tiles;
+    b.total_prims  = prims;
+    b.max_n        = max_n;
+    b.format       = geoms[0].L.format;
+    b.morton_bits  = geoms[0].L.morton_bits;
+    *many_launches = true;
+    return [=](cudaStream_t s) {
+        (void)dev;  // keeps the descriptors alive as long as the op
+        return launch_build_batch(b, words, sms, s);
+    };
+}
+
+void flush_builds(CommandStream* cs)
+{
+    if (cs->pending.empty()) return;
+    bool many = false;
+    Op   op   = build_batch_op(cs->ctx, cs->pending, &many);
+    cs->pending.clear();
+    cs->pending_ranges.r.clear();
+    cs->want_graph = cs->want_graph || many;
+    cs->ops.push_back(std::move(op));
+}
+
+// Append an op to a command stream, or run it at once on an external one.
+// An op that owns memory (owns = true) is kept until the GPU is past it.
+void record(CommandStream* cs, Op op, bool owns = false)
 {
     if (cs->external)
     {
         check(op(cs->stream), "enqueue");
+        if (owns) cs->ctx->retire(std::move(op), cs->stream);
         return;
     }
+    flush_builds(cs);
     cs->ops.push_back(std::move(op));
 }
 
@@ -201,6 +373,66 @@ RRError check_mesh_input(const RRGeometryBuildInput* in, const RRTriangleMeshPri
     if (m->triangle_count >= (1u << 30)) return RR_ERROR_INVALID_PARAMETER;
     *out = m;
     return RR_SUCCESS;
+}
+
+// Validate one geometry build (reference radeonrays.cpp:242-299) and resolve
+// its buffers.
+RRError prepare_geometry(const RRGeometryBuildInput* in, const BuildParams& bp, RRDevicePtr temporary_buffer,
+                         RRDevicePtr geometry_buffer, PendingGeom* pg)
+{
+    const RRTriangleMeshPrimitive* m = nullptr;
+    RRError                        e = check_mesh_input(in, &m, true);
+    if (e != RR_SUCCESS) return e;
+    if (!geometry_buffer || (!temporary_buffer && m->triangle_count > 0)) return RR_ERROR_INVALID_PARAMETER;
+    pg->L                = geom_layout(m->triangle_count, bp.format, bp.bits);
+    pg->ma.vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
+    pg->ma.stride_floats = m->vertex_stride >> 2;
+    pg->ma.indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
+    pg->ma.index16       = m->index_type == RR_INDEX_TYPE_UINT16;
+    pg->ma.n             = m->triangle_count;
+    pg->scratch          = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
+    pg->result           = P(geometry_buffer)->addr();
+    return RR_SUCCESS;
+}
+
+// Remember what a result buffer holds (scene builds and traversal read it).
+void register_geometry(Context* ctx, const PendingGeom& pg)
+{
+    BufInfo bi;
+    bi.kind                             = kKindGeom;
+    bi.n                                = pg.L.n;
+    bi.format                           = pg.L.format;
+    bi.trailer_off                      = pg.L.trailer_off;
+    bi.wide_off                         = pg.L.wide_off;
+    bi.tris_off                         = pg.L.tris_off;
+    ctx->registry[(uintptr_t)pg.result] = bi;
+}
+
+// Record a geometry build: fused with the builds recorded just before it when
+// they share format and key width and touch disjoint memory.
+void record_build(CommandStream* cs, const PendingGeom& pg)
+{
+    if (cs->external || !cs->ctx->fuse_builds)
+    {
+        std::vector<PendingGeom> one{pg};
+        bool                     many = false;
+        record(cs, build_batch_op(cs->ctx, one, &many));
+        return;
+    }
+    bool fits = true;
+    if (!cs->pending.empty())
+    {
+        const PendingGeom& f = cs->pending.front();
+        fits = f.L.format == pg.L.format && f.L.morton_bits == pg.L.morton_bits && claim_build_ranges(cs->pending_ranges, pg);
+    }
+    if (!fits)
+    {
+        flush_builds(cs);
+        claim_build_ranges(cs->pending_ranges, pg);
+    }
+    else if (cs->pending.empty())
+        claim_build_ranges(cs->pending_ranges, pg);
+    cs->pending.push_back(pg);
 }
 
 // 3x4 affine inverse in double, rounded once to float.
@@ -382,6 +614,8 @@ RR_API RRError rrCreateContext(uint32_t api_version, RRApi api, RRContext* conte
         c->topts.traversal   = RR_CUDA_TRAVERSAL_AUTO;
         const char* g        = std::getenv("RR_CUDA_GRAPHS");
         c->graphs            = !(g && g[0] == '0');
+        const char* fb       = std::getenv("RR_CUDA_FUSE_BUILDS");
+        c->fuse_builds       = !(fb && fb[0] == '0');
         *context             = reinterpret_cast<RRContext>(c.release());
         return RR_SUCCESS;
     })
@@ -428,36 +662,52 @@ RR_API RRError rrCmdBuildGeometry(RRContext                   context,
     RR_LOG_INFO("rrCmdBuildGeometry");
     if (!context || !command_stream || !build_input) return RR_ERROR_INVALID_PARAMETER;
     RR_TRY({
-        const RRTriangleMeshPrimitive* m = nullptr;
-        RRError                        e = check_mesh_input(build_input, &m, true);
-        if (e != RR_SUCCESS) return e;
         if (build_operation == RR_BUILD_OPERATION_UPDATE) return RR_ERROR_NOT_IMPLEMENTED;
         if (build_operation != RR_BUILD_OPERATION_BUILD) return RR_ERROR_INVALID_PARAMETER;
-        if (!geometry_buffer || (!temporary_buffer && m->triangle_count > 0)) return RR_ERROR_INVALID_PARAMETER;
         BuildParams bp;
         if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
-        Context*   ctx = C(context);
+        Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
-        GeomLayout L   = geom_layout(m->triangle_count, bp.format, bp.bits);
-        MeshArgs   ma;
-        ma.vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
-        ma.stride_floats = m->vertex_stride >> 2;
-        ma.indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
-        ma.index16       = m->index_type == RR_INDEX_TYPE_UINT16;
-        ma.n             = m->triangle_count;
-        uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
-        uint8_t*     result  = P(geometry_buffer)->addr();
-        DeviceWords* words   = ctx->words;
-        const int    sms     = ctx->sm_count;
-        record(S(command_stream), [=](cudaStream_t s) { return launch_build_mesh(ma, L, scratch, result, words, sms, s); });
-        BufInfo bi;
-        bi.kind        = kKindGeom;
-        bi.n           = L.n;
-        bi.format      = L.format;
-        bi.trailer_off = L.trailer_off;
-        bi.wide_off    = L.wide_off;
-        bi.tris_off    = L.tris_off;
-        ctx->registry[(uintptr_t)result] = bi;
+        PendingGeom pg;
+        RRError     e = prepare_geometry(build_input, bp, temporary_buffer, geometry_buffer, &pg);
+        if (e != RR_SUCCESS) return e;
+        record_build(S(command_stream), pg);
+        register_geometry(ctx, pg);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
+                                        uint32_t                    count,
+                                        const RRGeometryBuildInput* build_inputs,
+                                        const RRBuildOptions*       build_options,
+                                        const RRDevicePtr*          temporary_buffers,
+                                        const RRDevicePtr*          geometry_buffers,
+                                        RRCommandStream             command_stream)
+{
+    RR_LOG_INFO("rrCudaCmdBuildGeometries(%u)", count);
+    if (!context || !command_stream || (count > 0 && (!build_inputs || !temporary_buffers || !geometry_buffers)))
+        return RR_ERROR_INVALID_PARAMETER;
+    if (count == 0) return RR_SUCCESS;
+    RR_TRY({
+        BuildParams bp;
+        if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
+        Context*                 ctx = C(context);
+        DeviceGuard              g(ctx->device);
+        std::vector<PendingGeom> geoms(count);
+        RangeSet                 used;
+        for (uint32_t i = 0; i < count; ++i)
+        {
+            RRError e = prepare_geometry(build_inputs + i, bp, temporary_buffers[i], geometry_buffers[i], &geoms[i]);
+            if (e != RR_SUCCESS) return e;
+            if (!claim_build_ranges(used, geoms[i])) return RR_ERROR_INVALID_PARAMETER;
+        }
+        CommandStream* cs   = S(command_stream);
+        bool           many = false;
+        Op             op   = build_batch_op(ctx, geoms, &many);
+        record(cs, std::move(op), many);
+        cs->want_graph = cs->want_graph || many;
+        for (const PendingGeom& pg : geoms) register_geometry(ctx, pg);
         return RR_SUCCESS;
     })
 }
@@ -535,7 +785,9 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
         uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
         uint8_t*     result  = P(scene_buffer)->addr();
         DeviceWords* words   = ctx->words;
-        record(S(command_stream), [=](cudaStream_t s) -> cudaError_t {
+        record(
+            S(command_stream),
+            [=](cudaStream_t s) -> cudaError_t {
             cudaError_t e = cudaSuccess;
             if (n > 0)
             {
@@ -550,7 +802,8 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
             sa.forward = reinterpret_cast<const float*>(result + L.xforms_off);
             sa.n       = n;
             return launch_build_scene(sa, L, scratch, result, words, s);
-        });
+            },
+            true);
         BufInfo bi;
         bi.kind        = kKindScene;
         bi.n           = n;
@@ -597,6 +850,89 @@ RR_API RRError rrGetTraceMemoryRequirements(RRContext context, uint32_t ray_coun
     return RR_SUCCESS;
 }
 
+RR_API RRError rrCudaGetIntersectBatchMemoryRequirements(RRContext context, uint32_t request_count,
+                                                         uint32_t total_ray_count, size_t* scratch_size)
+{
+    if (!context || !scratch_size || !request_count) return RR_ERROR_INVALID_PARAMETER;
+    *scratch_size = batch_trace_layout(request_count, total_ray_count).total;
+    return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
+                                       uint32_t                      request_count,
+                                       const RRCudaIntersectRequest* requests,
+                                       RRDevicePtr                   scratch,
+                                       RRCommandStream               command_stream)
+{
+    RR_LOG_INFO("rrCudaCmdIntersectBatch(%u)", request_count);
+    if (!context || !requests || !request_count || !scratch || !command_stream) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        // Host staging of [request table | prefix], copied into the scratch by the op.
+        const BatchTraceLayout L0    = batch_trace_layout(request_count, 0);
+        const size_t           pre   = ((size_t)request_count + 1) * sizeof(uint32_t);
+        const size_t           gap   = L0.prefix_off - L0.req_off;
+        auto                   stage = std::make_shared<PinnedBlock>(gap + pre);
+        BatchTraceReq*         rq    = reinterpret_cast<BatchTraceReq*>(stage->p);
+        uint32_t*              pf    = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(stage->p) + gap);
+        std::memset(stage->p, 0, gap + pre);
+        uint64_t total = 0;
+        for (uint32_t k = 0; k < request_count; ++k)
+        {
+            const RRCudaIntersectRequest& q = requests[k];
+            if (!q.geometry || (q.ray_count && (!q.rays || !q.hits))) return RR_ERROR_INVALID_PARAMETER;
+            if (q.query != RR_INTERSECT_QUERY_CLOSEST && q.query != RR_INTERSECT_QUERY_ANY)
+                return RR_ERROR_INVALID_PARAMETER;
+            if (q.output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && q.output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+                return RR_ERROR_INVALID_PARAMETER;
+            uint8_t* bvh = P(q.geometry)->addr();
+            auto     it  = ctx->registry.find((uintptr_t)bvh);
+            BufInfo  bi;
+            if (it != ctx->registry.end()) bi = it->second;
+            if (bi.kind == kKindScene) return RR_ERROR_NOT_IMPLEMENTED;
+            BatchTraceReq r{};
+            r.bvh        = bvh;
+            r.rays       = q.ray_count ? P(q.rays)->addr() : nullptr;
+            r.hits       = q.ray_count ? P(q.hits)->addr() : nullptr;
+            r.ray_count  = q.ray_count;
+            r.node_limit = bi.kind == 0 ? kInvalid : (bi.n == 0 ? 0u : 2u * bi.n - 1u);
+            r.flags      = (q.query == RR_INTERSECT_QUERY_ANY ? kReqAny : 0u) |
+                      (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
+                      (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u);
+            rq[k] = r;
+            pf[k] = (uint32_t)total;
+            total += q.ray_count;
+            if (total >= 0xffffffffull) return RR_ERROR_INVALID_PARAMETER;
+        }
+        pf[request_count]        = (uint32_t)total;
+        const BatchTraceLayout L = batch_trace_layout(request_count, total);
+        uint8_t*               sc = P(scratch)->addr();
+        BatchTraceArgs         a{};
+        a.req           = reinterpret_cast<const BatchTraceReq*>(sc + L.req_off);
+        a.prefix        = reinterpret_cast<const uint32_t*>(sc + L.prefix_off);
+        a.count         = request_count;
+        a.total         = (uint32_t)total;
+        a.scratch       = sc;
+        a.scratch_bytes = L.total;
+        a.spill_off     = L.spill_off;
+        a.words         = ctx->words;
+        a.sm_count      = ctx->sm_count;
+        a.blocks_per_sm = (int)ctx->topts.blocks_per_sm;
+        a.collect_stats = ctx->topts.collect_stats ? 1 : 0;
+        const size_t bytes = gap + pre;
+        record(
+            S(command_stream),
+            [=](cudaStream_t s) -> cudaError_t {
+                cudaError_t e = cudaMemcpyAsync(sc + L.req_off, stage->p, bytes, cudaMemcpyHostToDevice, s);
+                if (e != cudaSuccess) return e;
+                return launch_trace_batch(a, s);
+            },
+            true);
+        return RR_SUCCESS;
+    })
+}
+
 RR_API RRError rrAllocateCommandStream(RRContext context, RRCommandStream* command_stream)
 {
     if (!context || !command_stream) return RR_ERROR_INVALID_PARAMETER;
@@ -633,8 +969,9 @@ RR_API RRError rrSumbitCommandStream(RRContext context, RRCommandStream command_
         if (wait_event) check(cudaStreamWaitEvent(st, E(wait_event)->ev, 0), "cudaStreamWaitEvent");
         if (!cs->external)
         {
+            flush_builds(cs);
             bool done = false;
-            if (ctx->graphs && !cs->graph_failed && cs->ops.size() > 1)
+            if (ctx->graphs && !cs->graph_failed && (cs->ops.size() > 1 || cs->want_graph))
             {
                 if (!cs->graph || cs->graph_ops != cs->ops.size())
                 {

@@ -1,13 +1,25 @@
-// build_lbvh.cu -- LBVH build of one triangle mesh on sm_103a.
+// build_lbvh.cu -- LBVH build of triangle meshes on sm_103a, one mesh or many
+// meshes fused into one set of launches.
 //
 // Pipeline (reference: vlk/hlbvh_builder.cpp:159-351):
-//   k_mesh_bounds   lbvh_calc_mesh_aabb.comp:121-179  exact min/max of all
+//   k_batch_init    trailers, bounds and histogram words of every geometry
+//   k_batch_bounds  lbvh_calc_mesh_aabb.comp:121-179  exact min/max of all
 //                   referenced vertices, order-preserving uint atomics
-//   k_morton        lbvh_calc_morton_codes_mesh.comp:78-130
-//   radix sort      vlk/radix_sort.cpp (sort.cu, onesweep)
-//   k_emit          lbvh_emit_hierarchy_mesh.comp:78-217 (Karras 2012)
-//   k_refit         lbvh_fit_aabb_mesh.comp:94-205 (atomic bottom-up climb)
+//   k_batch_morton  lbvh_calc_morton_codes_mesh.comp:78-130, plus the digit
+//                   histograms of the sort (one read of the keys fewer)
+//   radix sort      vlk/radix_sort.cpp (sort.cu, onesweep, per geometry)
+//   k_batch_emit    lbvh_emit_hierarchy_mesh.comp:78-217 (Karras 2012)
+//   k_batch_refit   lbvh_fit_aabb_mesh.comp:94-205 (atomic bottom-up climb)
 //   wide collapse   (wide.cu) when the WIDE8 node format is requested
+//
+// Fused builds.  Every geometry keeps its own scratch and result buffer (the
+// sizes rrGetGeometryBuildMemoryRequirements gives for it alone) and is
+// described by a BuildItem in device memory.  The element range of every
+// geometry is cut into sort tiles (radix_sort_tile_keys keys); a block of a
+// tile-mapped kernel finds its geometry by a binary search over the tiles'
+// exclusive prefix, so one launch covers all geometries however uneven they
+// are, and a single mesh is the batch of one.  Results are those of separate
+// builds: no value crosses from one geometry to another.
 //
 // Arithmetic follows the oracle's rules (IEEE fp32, no contraction: the file
 // is compiled with --fmad=false), so codes, permutation, topology and boxes
@@ -18,11 +30,13 @@
 
 namespace rr
 {
-cudaError_t launch_collapse_wide(const GeomLayout& L, uint8_t* scratch, uint8_t* result, DeviceWords* words,
-                                 int sm_count, cudaStream_t s);
+cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s);
 
 namespace
 {
+constexpr int kBlk   = 256;  // threads of the tile-mapped kernels
+constexpr int kChunk = 256;  // elements per block of the emit / refit kernels
+
 struct F3
 {
     float x, y, z;
@@ -42,63 +56,21 @@ __device__ __forceinline__ float ord2f(uint32_t u)
     return __uint_as_float(u);
 }
 
-__device__ __forceinline__ uint32_t tri_index(const MeshArgs& m, uint64_t k)
+__device__ __forceinline__ uint32_t tri_index(const BuildItem& m, uint64_t k)
 {
-    return m.index16 ? (uint32_t)((const uint16_t*)m.indices)[k] : ((const uint32_t*)m.indices)[k];
+    return m.index16 ? (uint32_t)__ldg((const uint16_t*)m.indices + k) : __ldg((const uint32_t*)m.indices + k);
 }
-__device__ __forceinline__ F3 vtx(const MeshArgs& m, uint32_t i)
+__device__ __forceinline__ F3 vtx(const BuildItem& m, uint32_t i)
 {
     const float* p = m.vertices + (uint64_t)i * m.stride_floats;
     return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
-__device__ __forceinline__ void tri_verts(const MeshArgs& m, uint32_t t, F3& a, F3& b, F3& c)
+__device__ __forceinline__ void tri_verts(const BuildItem& m, uint32_t t, F3& a, F3& b, F3& c)
 {
     uint32_t i0 = tri_index(m, 3ull * t), i1 = tri_index(m, 3ull * t + 1), i2 = tri_index(m, 3ull * t + 2);
     a = vtx(m, i0);
     b = vtx(m, i1);
     c = vtx(m, i2);
-}
-
-// Exact mesh box over all referenced vertices.
-__global__ void __launch_bounds__(256) k_mesh_bounds(MeshArgs m, uint32_t* bounds)
-{
-    uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < m.n; t += gridDim.x * blockDim.x)
-    {
-        F3 a, b, c;
-        tri_verts(m, t, a, b, c);
-        F3 l = vmin(vmin(a, b), c), h = vmax(vmax(a, b), c);
-        lo[0] = min(lo[0], f2ord(l.x));
-        lo[1] = min(lo[1], f2ord(l.y));
-        lo[2] = min(lo[2], f2ord(l.z));
-        hi[0] = max(hi[0], f2ord(h.x));
-        hi[1] = max(hi[1], f2ord(h.y));
-        hi[2] = max(hi[2], f2ord(h.z));
-    }
-    __shared__ uint32_t s[6][8];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-    {
-        uint32_t a = __reduce_min_sync(0xffffffffu, lo[k]);
-        uint32_t b = __reduce_max_sync(0xffffffffu, hi[k]);
-        if (lane == 0)
-        {
-            s[k][w]     = a;
-            s[k + 3][w] = b;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 6)
-    {
-        int      k = threadIdx.x;
-        uint32_t v = s[k][0];
-        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) v = k < 3 ? min(v, s[k][i]) : max(v, s[k][i]);
-        if (k < 3)
-            atomicMin(&bounds[k], v);
-        else
-            atomicMax(&bounds[k + 1], v);
-    }
 }
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t r)
@@ -120,36 +92,6 @@ __device__ __forceinline__ uint64_t expand_bits21(uint64_t v)
     return v;
 }
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
-
-template <int kBits>
-__global__ void __launch_bounds__(256) k_morton(MeshArgs m, const uint32_t* __restrict__ bounds, void* codes)
-{
-    const F3 mlo = f3(ord2f(bounds[0]), ord2f(bounds[1]), ord2f(bounds[2]));
-    const F3 mhi = f3(ord2f(bounds[4]), ord2f(bounds[5]), ord2f(bounds[6]));
-    const F3 ext = f3(mhi.x - mlo.x, mhi.y - mlo.y, mhi.z - mlo.z);
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < m.n; t += gridDim.x * blockDim.x)
-    {
-        F3 a, b, c;
-        tri_verts(m, t, a, b, c);
-        F3 l = vmin(vmin(a, b), c), h = vmax(vmax(a, b), c);
-        F3 p = f3((0.5f * (l.x + h.x) - mlo.x) / ext.x, (0.5f * (l.y + h.y) - mlo.y) / ext.y,
-                  (0.5f * (l.z + h.z) - mlo.z) / ext.z);
-        if (kBits == 63)
-        {
-            const float s = 2097152.0f;
-            uint64_t    x = (uint64_t)clampf(p.x * s, 0.f, s - 1.f), y = (uint64_t)clampf(p.y * s, 0.f, s - 1.f),
-                     z = (uint64_t)clampf(p.z * s, 0.f, s - 1.f);
-            ((uint64_t*)codes)[t] = (expand_bits21(x) << 2) | (expand_bits21(y) << 1) | expand_bits21(z);
-        }
-        else
-        {
-            const float s = 1024.0f;
-            uint32_t    x = (uint32_t)clampf(p.x * s, 0.f, s - 1.f), y = (uint32_t)clampf(p.y * s, 0.f, s - 1.f),
-                     z = (uint32_t)clampf(p.z * s, 0.f, s - 1.f);
-            ((uint32_t*)codes)[t] = (expand_bits(x) << 2) | (expand_bits(y) << 1) | expand_bits(z);
-        }
-    }
-}
 
 // clz as the reference shader defines it (32 - findMSB(v), findMSB(0) = -1).
 __device__ __forceinline__ int clz_p1(uint32_t v) { return __clz(v) + 1; }
@@ -174,11 +116,10 @@ struct Delta
     }
 };
 
+// Internal node i (< n - 1) of a Karras tree over n sorted codes.
 template <int kBits>
-__global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, uint32_t n, BvhNode* nodes)
+__device__ __forceinline__ void emit_node(const void* __restrict__ codes, uint32_t n, uint32_t i, BvhNode* nodes)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i + 1 >= n) return;
     Delta<kBits> delta{codes, (int64_t)n};
     const int64_t ii = i;
     // FindSpan
@@ -193,10 +134,10 @@ __global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, ui
         t /= 2;
         if (delta(ii, ii + (l + t) * d) > dmin) l += t;
     } while (t > 1);
-    const int64_t e  = ii + l * d;
+    const int64_t e    = ii + l * d;
     const int64_t lo_e = ii < e ? ii : e, hi_e = ii < e ? e : ii;
-    const int64_t sx = lo_e > 0 ? lo_e : 0;
-    const int64_t sy = hi_e < (int64_t)n - 1 ? hi_e : (int64_t)n - 1;
+    const int64_t sx   = lo_e > 0 ? lo_e : 0;
+    const int64_t sy   = hi_e < (int64_t)n - 1 ? hi_e : (int64_t)n - 1;
     // FindSplit
     int64_t   left = sx, right = sy;
     const int nid  = delta(left, right);
@@ -219,6 +160,15 @@ __global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, ui
     if (i == 0) nodes[0].parent = kInvalid;
 }
 
+// One sorted array (the instance tree of a scene build).
+template <int kBits>
+__global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, uint32_t n, BvhNode* nodes)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    emit_node<kBits>(codes, n, i, nodes);
+}
+
 __device__ __forceinline__ F3 ldcg3(const float* p) { return f3(__ldcg(p), __ldcg(p + 1), __ldcg(p + 2)); }
 
 // Box of a child node as the fit shader computes it (lbvh_fit_aabb_mesh.comp:94-118).
@@ -239,20 +189,211 @@ __device__ __forceinline__ void child_box(const BvhNode* nodes, uint32_t c, F3& 
     }
 }
 
-__global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __restrict__ sorted_idx, BvhNode* nodes,
-                                               DeviceWords* words)
+template <int kBits>
+struct KeyCfg
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m.n) return;
-    const uint32_t n    = m.n;
-    const uint32_t leaf = n - 1 + k;
-    const uint32_t prim = sorted_idx[k];
-    F3             a, b, c;
-    tri_verts(m, prim, a, b, c);
+    static constexpr uint32_t kTile   = kBits == 63 ? 2048u : 4096u;  // == radix_sort_tile_keys(kBits)
+    static constexpr uint32_t kPasses = kBits == 63 ? 8u : 4u;
+    static constexpr uint32_t kChunks = kTile / kChunk;              // emit / refit blocks per tile
+};
+
+__device__ __forceinline__ uint32_t* sort_words(const BuildItem& it)
+{
+    return reinterpret_cast<uint32_t*>(it.scratch + it.s_sort);
+}
+
+// Per geometry: trailer, bounds identities, digit histograms and run counters.
+__global__ void __launch_bounds__(kBlk) k_batch_init(BatchArgs b)
+{
+    const uint32_t   g  = blockIdx.x;
+    const BuildItem& it = b.items[g];
+    if (g == 0)
+        for (int k = threadIdx.x; k < kBatchCounters; k += blockDim.x) (&b.ctl->sort_tile[0])[k] = 0;
+    if (threadIdx.x == 0)
+    {
+        Trailer t{};
+        t.magic          = kMagic;
+        t.version        = kVersion;
+        t.kind           = kKindGeom;
+        t.node_format    = b.format;
+        t.leaf_count     = it.n;
+        t.node_count     = it.n == 0 ? 0 : 2 * it.n - 1;
+        t.wide_nodes_off = it.wide_off;
+        t.wide_tris_off  = it.tris_off;
+        t.wide_capacity  = it.wide_capacity;
+        t.tri_capacity   = it.tri_capacity;
+        t.morton_bits    = b.morton_bits;
+        *reinterpret_cast<Trailer*>(it.result + it.trailer_off) = t;
+    }
+    if (it.n == 0) return;
+    uint32_t* bounds = reinterpret_cast<uint32_t*>(it.scratch + it.s_bounds);
+    if (threadIdx.x < 8) bounds[threadIdx.x] = threadIdx.x < 4 ? 0xffffffffu : 0u;
+    const uint32_t passes = b.morton_bits > 32 ? 8u : 4u;
+    uint32_t*      ss     = sort_words(it);
+    for (uint32_t k = threadIdx.x; k < passes * 256u + 64u; k += blockDim.x) ss[k] = 0;
+}
+
+struct TileRef
+{
+    uint32_t g;
+    uint32_t tile;  // tile within the geometry
+};
+__device__ __forceinline__ TileRef tile_ref(const BatchArgs& b, uint32_t t)
+{
+    const uint32_t g = batch_find(b.tile_prefix, b.count, t);
+    return TileRef{g, t - __ldg(b.tile_prefix + g)};
+}
+
+// Exact box of the referenced vertices of one tile's triangles; also zeroes
+// the tile's look-back words of every sort pass.
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_bounds(BatchArgs b)
+{
+    using Cfg            = KeyCfg<kBits>;
+    const TileRef    r   = tile_ref(b, blockIdx.x);
+    const BuildItem& it  = b.items[r.g];
+    const uint32_t   n   = it.n;
+    const uint64_t   beg = (uint64_t)r.tile * Cfg::kTile;
+    const uint64_t   end = min((uint64_t)n, beg + Cfg::kTile);
+    uint32_t         lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+#pragma unroll 4
+    for (uint64_t t = beg + threadIdx.x; t < end; t += kBlk)
+    {
+        F3 a, bb, c;
+        tri_verts(it, (uint32_t)t, a, bb, c);
+        F3 l = vmin(vmin(a, bb), c), h = vmax(vmax(a, bb), c);
+        lo[0] = min(lo[0], f2ord(l.x));
+        lo[1] = min(lo[1], f2ord(l.y));
+        lo[2] = min(lo[2], f2ord(l.z));
+        hi[0] = max(hi[0], f2ord(h.x));
+        hi[1] = max(hi[1], f2ord(h.y));
+        hi[2] = max(hi[2], f2ord(h.z));
+    }
+    __shared__ uint32_t s[6][kBlk / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        uint32_t x = __reduce_min_sync(0xffffffffu, lo[k]);
+        uint32_t y = __reduce_max_sync(0xffffffffu, hi[k]);
+        if (lane == 0)
+        {
+            s[k][w]     = x;
+            s[k + 3][w] = y;
+        }
+    }
+    uint32_t* lb = sort_words(it) + Cfg::kPasses * 256u + 64u;
+#pragma unroll
+    for (uint32_t p = 0; p < Cfg::kPasses; ++p) lb[((size_t)p * it.tiles + r.tile) * 256u + threadIdx.x] = 0;
+    __syncthreads();
+    if (threadIdx.x < 6)
+    {
+        const int k = threadIdx.x;
+        uint32_t  v = s[k][0];
+        for (int i = 1; i < kBlk / 32; ++i) v = k < 3 ? min(v, s[k][i]) : max(v, s[k][i]);
+        uint32_t* bounds = reinterpret_cast<uint32_t*>(it.scratch + it.s_bounds);
+        if (k < 3)
+            atomicMin(&bounds[k], v);
+        else
+            atomicMax(&bounds[k + 1], v);
+    }
+}
+
+// Morton codes of one tile's triangle box centres and the tile's digit
+// histograms of every sort pass.
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_morton(BatchArgs b)
+{
+    using Cfg = KeyCfg<kBits>;
+    __shared__ uint32_t h[Cfg::kPasses][256];
+    for (uint32_t k = threadIdx.x; k < Cfg::kPasses * 256u; k += kBlk) (&h[0][0])[k] = 0;
+    __syncthreads();
+    const TileRef    r      = tile_ref(b, blockIdx.x);
+    const BuildItem& it     = b.items[r.g];
+    const uint32_t   n      = it.n;
+    const uint32_t*  bounds = reinterpret_cast<const uint32_t*>(it.scratch + it.s_bounds);
+    const F3         mlo    = f3(ord2f(bounds[0]), ord2f(bounds[1]), ord2f(bounds[2]));
+    const F3         mhi    = f3(ord2f(bounds[4]), ord2f(bounds[5]), ord2f(bounds[6]));
+    const F3         ext    = f3(mhi.x - mlo.x, mhi.y - mlo.y, mhi.z - mlo.z);
+    const uint64_t   beg    = (uint64_t)r.tile * Cfg::kTile;
+    const uint64_t   end    = min((uint64_t)n, beg + Cfg::kTile);
+    void*            codes  = it.scratch + it.s_codes;
+#pragma unroll 4
+    for (uint64_t t = beg + threadIdx.x; t < end; t += kBlk)
+    {
+        F3 a, bb, c;
+        tri_verts(it, (uint32_t)t, a, bb, c);
+        F3 l = vmin(vmin(a, bb), c), hh = vmax(vmax(a, bb), c);
+        F3 p = f3((0.5f * (l.x + hh.x) - mlo.x) / ext.x, (0.5f * (l.y + hh.y) - mlo.y) / ext.y,
+                  (0.5f * (l.z + hh.z) - mlo.z) / ext.z);
+        if (kBits == 63)
+        {
+            const float s = 2097152.0f;
+            uint64_t    x = (uint64_t)clampf(p.x * s, 0.f, s - 1.f), y = (uint64_t)clampf(p.y * s, 0.f, s - 1.f),
+                     z = (uint64_t)clampf(p.z * s, 0.f, s - 1.f);
+            const uint64_t code = (expand_bits21(x) << 2) | (expand_bits21(y) << 1) | expand_bits21(z);
+            ((uint64_t*)codes)[t] = code;
+#pragma unroll
+            for (uint32_t q = 0; q < Cfg::kPasses; ++q) atomicAdd(&h[q][(code >> (8 * q)) & 0xffu], 1u);
+        }
+        else
+        {
+            const float s = 1024.0f;
+            uint32_t    x = (uint32_t)clampf(p.x * s, 0.f, s - 1.f), y = (uint32_t)clampf(p.y * s, 0.f, s - 1.f),
+                     z = (uint32_t)clampf(p.z * s, 0.f, s - 1.f);
+            const uint32_t code = (expand_bits(x) << 2) | (expand_bits(y) << 1) | expand_bits(z);
+            ((uint32_t*)codes)[t] = code;
+#pragma unroll
+            for (uint32_t q = 0; q < Cfg::kPasses; ++q) atomicAdd(&h[q][(code >> (8 * q)) & 0xffu], 1u);
+        }
+    }
+    __syncthreads();
+    uint32_t* gh = sort_words(it);
+    for (uint32_t k = threadIdx.x; k < Cfg::kPasses * 256u; k += kBlk)
+    {
+        const uint32_t v = (&h[0][0])[k];
+        if (v) atomicAdd(gh + k, v);
+    }
+    if (r.tile == 0 && threadIdx.x < 8)
+    {
+        Trailer* tr                 = reinterpret_cast<Trailer*>(it.result + it.trailer_off);
+        tr->bounds[threadIdx.x] = (threadIdx.x & 3) == 3 ? 0u : bounds[threadIdx.x];
+    }
+}
+
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_emit(BatchArgs b)
+{
+    using Cfg            = KeyCfg<kBits>;
+    const uint32_t   t   = blockIdx.x / Cfg::kChunks;
+    const TileRef    r   = tile_ref(b, t);
+    const BuildItem& it  = b.items[r.g];
+    const uint64_t   i64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
+    if (i64 + 1 >= it.n) return;
+    emit_node<kBits>(it.scratch + it.s_codes, it.n, (uint32_t)i64, reinterpret_cast<BvhNode*>(it.result));
+}
+
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_refit(BatchArgs b, DeviceWords* words)
+{
+    using Cfg            = KeyCfg<kBits>;
+    const uint32_t   t   = blockIdx.x / Cfg::kChunks;
+    const TileRef    r   = tile_ref(b, t);
+    const BuildItem& it  = b.items[r.g];
+    const uint64_t   k64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
+    const uint32_t   n   = it.n;
+    if (k64 >= n) return;
+    const uint32_t  k          = (uint32_t)k64;
+    BvhNode*        nodes      = reinterpret_cast<BvhNode*>(it.result);
+    const uint32_t* sorted_idx = reinterpret_cast<const uint32_t*>(it.scratch + it.s_idx);
+    const uint32_t  leaf       = n - 1 + k;
+    const uint32_t  prim       = sorted_idx[k];
+    F3              a, bb, c;
+    tri_verts(it, prim, a, bb, c);
     uint32_t parent = (n == 1) ? kInvalid : __ldcg(&nodes[leaf].parent);
     float4*  dst    = reinterpret_cast<float4*>(nodes + leaf);
     __stcg(dst + 0, make_float4(a.x, a.y, a.z, __uint_as_float(kInvalid)));
-    __stcg(dst + 1, make_float4(b.x, b.y, b.z, __uint_as_float(prim)));
+    __stcg(dst + 1, make_float4(bb.x, bb.y, bb.z, __uint_as_float(prim)));
     __stcg(dst + 2, make_float4(c.x, c.y, c.z, __uint_as_float(parent)));
     __stcg(dst + 3, make_float4(0.f, 0.f, 0.f, __uint_as_float(0u)));
     uint32_t addr = parent;
@@ -295,15 +436,59 @@ __global__ void __launch_bounds__(256) k_refit(MeshArgs m, const uint32_t* __res
     }
 }
 
-__global__ void k_init_trailer(Trailer* t, Trailer v) { *t = v; }
-__global__ void k_copy_bounds(const uint32_t* b, Trailer* t)
+__global__ void k_put_single(BuildItem* items, BuildItem it, uint32_t* tile_prefix, uint32_t tiles)
 {
-    if (threadIdx.x < 8) t->bounds[threadIdx.x] = (threadIdx.x & 3) == 3 ? 0u : b[threadIdx.x];
+    if (threadIdx.x == 0)
+    {
+        items[0]       = it;
+        tile_prefix[0] = 0;
+        tile_prefix[1] = tiles;
+    }
 }
+
+__global__ void k_init_trailer(Trailer* t, Trailer v) { *t = v; }
 
 inline int grid_for(uint64_t n, int block) { return (int)std::max<uint64_t>(1, (n + block - 1) / block); }
 
+template <int kBits>
+cudaError_t run_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s)
+{
+    using Cfg = KeyCfg<kBits>;
+    if (radix_sort_tile_keys(kBits) != Cfg::kTile) return cudaErrorInvalidConfiguration;
+    k_batch_bounds<kBits><<<b.total_tiles, kBlk, 0, s>>>(b);
+    k_batch_morton<kBits><<<b.total_tiles, kBlk, 0, s>>>(b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if ((e = launch_radix_sort_batch(b, words, s)) != cudaSuccess) return e;
+    const uint64_t blocks = (uint64_t)b.total_tiles * Cfg::kChunks;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_batch_emit<kBits><<<(unsigned)blocks, kBlk, 0, s>>>(b);
+    k_batch_refit<kBits><<<(unsigned)blocks, kBlk, 0, s>>>(b, words);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (b.format == RR_CUDA_NODE_FORMAT_WIDE8) return launch_collapse_batch(b, words, sm_count, s);
+    return cudaSuccess;
+}
+
 }  // namespace
+
+size_t batch_desc_bytes(uint32_t count)
+{
+    return align_up((size_t)count * sizeof(BuildItem), kAlign) + 2 * align_up(((size_t)count + 1) * 4, kAlign) +
+           align_up(sizeof(BatchCtl), kAlign);
+}
+
+void batch_carve(uint8_t* block, uint32_t count, BuildItem** items, uint32_t** tile_prefix, uint32_t** level_prefix,
+                 BatchCtl** ctl)
+{
+    size_t off    = 0;
+    *items        = reinterpret_cast<BuildItem*>(block + off);
+    off           = align_up((size_t)count * sizeof(BuildItem), kAlign);
+    *tile_prefix  = reinterpret_cast<uint32_t*>(block + off);
+    off          += align_up(((size_t)count + 1) * 4, kAlign);
+    *level_prefix = reinterpret_cast<uint32_t*>(block + off);
+    off          += align_up(((size_t)count + 1) * 4, kAlign);
+    *ctl          = reinterpret_cast<BatchCtl*>(block + off);
+}
 
 GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
 {
@@ -324,10 +509,12 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
         off             = L.tris_off + L.tri_capacity * sizeof(WideTri);
     }
     L.total = align_up(off, kAlign);
-    // Scratch: bounds | codes | codes_alt | idx | idx_alt | sort | collapse queues.
+    // Scratch: batch descriptor of one | bounds | codes | codes_alt | idx |
+    // idx_alt | sort | collapse queues.
     const size_t kb = L.morton_bits == 63 ? 8 : 4;
-    L.s_bounds      = 0;
-    L.s_codes       = kAlign;
+    L.s_desc        = 0;
+    L.s_bounds      = align_up(batch_desc_bytes(1), kAlign);
+    L.s_codes       = L.s_bounds + kAlign;
     L.s_codes_alt   = align_up(L.s_codes + kb * n, kAlign);
     L.s_idx         = align_up(L.s_codes_alt + kb * n, kAlign);
     L.s_idx_alt     = align_up(L.s_idx + 4ull * n, kAlign);
@@ -337,6 +524,33 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
     L.s_queue_bytes = (format == RR_CUDA_NODE_FORMAT_WIDE8 && n > 0) ? 2 * kAlign + 2ull * 8ull * n : 0;
     L.s_total       = align_up(L.s_queue + L.s_queue_bytes, kAlign);
     return L;
+}
+
+BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t stride_floats, const void* indices,
+                          int index16, uint8_t* scratch, uint8_t* result)
+{
+    BuildItem it{};
+    it.vertices      = vertices;
+    it.indices       = indices;
+    it.scratch       = scratch;
+    it.result        = result;
+    it.stride_floats = stride_floats;
+    it.s_bounds      = L.s_bounds;
+    it.s_codes       = L.s_codes;
+    it.s_codes_alt   = L.s_codes_alt;
+    it.s_idx         = L.s_idx;
+    it.s_idx_alt     = L.s_idx_alt;
+    it.s_sort        = L.s_sort;
+    it.s_queue       = L.s_queue;
+    it.trailer_off   = L.trailer_off;
+    it.wide_off      = L.wide_off;
+    it.tris_off      = L.tris_off;
+    it.wide_capacity = (uint32_t)L.wide_capacity;
+    it.tri_capacity  = (uint32_t)L.tri_capacity;
+    it.n             = L.n;
+    it.index16       = index16 ? 1u : 0u;
+    it.tiles         = L.sort_tiles;
+    return it;
 }
 
 cudaError_t launch_emit(const void* sorted_codes, int bits, uint32_t n, BvhNode* nodes, cudaStream_t s)
@@ -349,53 +563,49 @@ cudaError_t launch_emit(const void* sorted_codes, int bits, uint32_t n, BvhNode*
     return cudaGetLastError();
 }
 
+cudaError_t launch_build_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s)
+{
+    if (b.count == 0) return cudaSuccess;
+    k_batch_init<<<b.count, kBlk, 0, s>>>(b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || b.total_tiles == 0) return e;
+    return b.morton_bits == 63 ? run_batch<63>(b, words, sm_count, s) : run_batch<30>(b, words, sm_count, s);
+}
+
 cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
                               DeviceWords* words, int sm_count, cudaStream_t s)
 {
-    Trailer tr{};
-    tr.magic          = kMagic;
-    tr.version        = kVersion;
-    tr.kind           = kKindGeom;
-    tr.node_format    = L.format;
-    tr.leaf_count     = L.n;
-    tr.node_count     = L.n == 0 ? 0 : 2 * L.n - 1;
-    tr.wide_nodes_off = L.wide_off;
-    tr.wide_tris_off  = L.tris_off;
-    tr.wide_capacity  = L.wide_capacity;
-    tr.tri_capacity   = L.tri_capacity;
-    tr.morton_bits    = L.morton_bits;
-    Trailer* dtr      = reinterpret_cast<Trailer*>(result + L.trailer_off);
-    k_init_trailer<<<1, 1, 0, s>>>(dtr, tr);
-    if (L.n == 0) return cudaGetLastError();
-
-    uint32_t*   bounds = reinterpret_cast<uint32_t*>(scratch + L.s_bounds);
-    cudaError_t e      = cudaMemsetAsync(bounds, 0xff, 16, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bounds + 4, 0, 16, s);
-    if (e != cudaSuccess) return e;
-    const int blocks = std::min(grid_for(L.n, 256), sm_count * 8);
-    k_mesh_bounds<<<blocks, 256, 0, s>>>(m, bounds);
-    k_copy_bounds<<<1, 32, 0, s>>>(bounds, dtr);
-    void*     codes     = scratch + L.s_codes;
-    void*     codes_alt = scratch + L.s_codes_alt;
-    uint32_t* idx       = reinterpret_cast<uint32_t*>(scratch + L.s_idx);
-    uint32_t* idx_alt   = reinterpret_cast<uint32_t*>(scratch + L.s_idx_alt);
-    if (L.morton_bits == 63)
-        k_morton<63><<<blocks, 256, 0, s>>>(m, bounds, codes);
-    else
-        k_morton<30><<<blocks, 256, 0, s>>>(m, bounds, codes);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    bool alt = false;
-    e = launch_radix_sort(codes, codes_alt, idx, idx_alt, L.n, (int)L.morton_bits, scratch + L.s_sort, L.sort_tiles,
-                          words, s, &alt);
-    if (e != cudaSuccess) return e;
-    const void*     sc   = alt ? codes_alt : codes;
-    const uint32_t* sidx = alt ? idx_alt : idx;
-    BvhNode*        nodes = reinterpret_cast<BvhNode*>(result);
-    if ((e = launch_emit(sc, (int)L.morton_bits, L.n, nodes, s)) != cudaSuccess) return e;
-    k_refit<<<grid_for(L.n, 256), 256, 0, s>>>(m, sidx, nodes, words);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (L.format == RR_CUDA_NODE_FORMAT_WIDE8) return launch_collapse_wide(L, scratch, result, words, sm_count, s);
-    return cudaSuccess;
+    if (L.n == 0)
+    {
+        // No scratch is required for an empty mesh: write the trailer only.
+        Trailer tr{};
+        tr.magic       = kMagic;
+        tr.version     = kVersion;
+        tr.kind        = kKindGeom;
+        tr.node_format = L.format;
+        tr.morton_bits = L.morton_bits;
+        k_init_trailer<<<1, 1, 0, s>>>(reinterpret_cast<Trailer*>(result + L.trailer_off), tr);
+        return cudaGetLastError();
+    }
+    BuildItem* items = nullptr;
+    uint32_t * tp = nullptr, *lp = nullptr;
+    BatchCtl*  ctl = nullptr;
+    batch_carve(scratch + L.s_desc, 1, &items, &tp, &lp, &ctl);
+    k_put_single<<<1, 32, 0, s>>>(items, make_build_item(L, m.vertices, m.stride_floats, m.indices, m.index16, scratch,
+                                                         result),
+                                  tp, L.sort_tiles);
+    BatchArgs b{};
+    b.items        = items;
+    b.tile_prefix  = tp;
+    b.level_prefix = lp;
+    b.ctl          = ctl;
+    b.count        = 1;
+    b.total_tiles  = L.sort_tiles;
+    b.total_prims  = L.n;
+    b.max_n        = L.n;
+    b.format       = L.format;
+    b.morton_bits  = L.morton_bits;
+    return launch_build_batch(b, words, sm_count, s);
 }
 
 }  // namespace rr

@@ -116,11 +116,81 @@ struct GeomLayout
     size_t   tri_capacity;
     size_t   total;
     // scratch
-    size_t   s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_queue, s_queue_bytes,
+    size_t   s_desc, s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_queue, s_queue_bytes,
         s_total;
     uint32_t sort_tiles, sort_passes;
 };
 GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits);
+
+struct DeviceWords;
+
+// One geometry of a (possibly fused) build, resident on the device.  Offsets
+// are the geometry's GeomLayout offsets into its own scratch / result buffer.
+struct __align__(16) BuildItem
+{
+    const float* vertices;
+    const void*  indices;
+    uint8_t*     scratch;
+    uint8_t*     result;
+    uint64_t     stride_floats;
+    uint64_t     s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_queue;
+    uint64_t     trailer_off, wide_off, tris_off;
+    uint32_t     wide_capacity, tri_capacity;
+    uint32_t     n;
+    uint32_t     index16;
+    uint32_t     tiles;     // sort tiles of this geometry
+    uint32_t     pad;
+};
+
+// Batch-wide control words (device).
+constexpr int kBatchCounters = 64;
+struct BatchCtl
+{
+    uint32_t sort_tile[16];  // tile claim counter of every onesweep pass
+    uint32_t pad[kBatchCounters - 16];
+};
+
+// A fused build of `count` geometries with the same node format and key
+// width.  `items`, `tile_prefix` (count + 1 exclusive prefix of the sort
+// tiles), `level_prefix` (count + 1, collapse work per level) and `ctl` are
+// device memory.
+struct BatchArgs
+{
+    const BuildItem* items;
+    const uint32_t*  tile_prefix;
+    uint32_t*        level_prefix;
+    BatchCtl*        ctl;
+    uint32_t         count;
+    uint32_t         total_tiles;   // sum of items[i].tiles
+    uint64_t         total_prims;   // sum of items[i].n
+    uint32_t         max_n;         // largest items[i].n
+    uint32_t         format;
+    uint32_t         morton_bits;
+};
+size_t batch_desc_bytes(uint32_t count);
+// Geometry owning tile t: the largest g < count with prefix[g] <= t (prefix
+// has count + 1 entries, prefix[count] > t).  Empty geometries are skipped.
+__device__ __forceinline__ uint32_t batch_find(const uint32_t* __restrict__ prefix, uint32_t count, uint32_t t)
+{
+    uint32_t lo = 0, hi = count;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(prefix + mid) <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+// Carve `count` items + prefixes + control words from a device block of
+// batch_desc_bytes(count) bytes.
+void batch_carve(uint8_t* block, uint32_t count, BuildItem** items, uint32_t** tile_prefix, uint32_t** level_prefix,
+                 BatchCtl** ctl);
+BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t stride_floats, const void* indices,
+                          int index16, uint8_t* scratch, uint8_t* result);
+// Enqueue the whole fused build (the descriptors must already be on the device).
+cudaError_t launch_build_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s);
 
 struct SceneLayout
 {
@@ -164,6 +234,13 @@ cudaError_t launch_radix_sort(void* codes, void* codes_alt, uint32_t* idx, uint3
                               int key_bits, uint8_t* sort_scratch, uint32_t tiles, DeviceWords* words,
                               cudaStream_t s, bool* sorted_in_alt);
 size_t   radix_sort_scratch_bytes(uint32_t n, int key_bits, uint32_t* tiles, uint32_t* passes);
+// Keys per sort tile (and per tile of the fused build's tile-mapped kernels).
+uint32_t radix_sort_tile_keys(int key_bits);
+// Per-geometry sort of a fused build: every geometry's Morton codes (at
+// s_codes) are sorted into s_codes / s_idx in place (an even pass count), its
+// digit histograms (s_sort, built by the Morton kernel) already summed and its
+// look-back words already zeroed.  One launch per digit pass for all geometries.
+cudaError_t launch_radix_sort_batch(const BatchArgs& b, DeviceWords* words, cudaStream_t s);
 
 struct TraceArgs
 {
@@ -190,6 +267,49 @@ struct TraceArgs
     int             blocks_per_sm;
     int             sm_count;
 };
+// One request of a multi-request traversal launch (rrCudaCmdIntersectBatch).
+constexpr uint32_t kReqAny   = 1;  // any-hit query (else closest)
+constexpr uint32_t kReqFull  = 2;  // full RRHit output (else instance id)
+constexpr uint32_t kReqEmpty = 4;  // geometry without triangles: every ray misses
+struct __align__(16) BatchTraceReq
+{
+    const uint8_t* bvh;   // geometry result buffer (binary nodes at offset 0)
+    const uint8_t* rays;  // RRRay[ray_count]
+    void*          hits;
+    uint32_t       ray_count;
+    uint32_t       node_limit;  // binary nodes in the buffer (kInvalid: unknown)
+    uint32_t       flags;
+    uint32_t       pad;
+};
+static_assert(sizeof(BatchTraceReq) == 48, "request layout");
+
+// Scratch of a multi-request launch: control words | request table | ray
+// prefix (count + 1) | per-thread stack spill.
+struct BatchTraceLayout
+{
+    size_t req_off, prefix_off, spill_off, total;
+};
+BatchTraceLayout batch_trace_layout(uint32_t count, uint64_t total_rays);
+
+struct BatchTraceArgs
+{
+    const BatchTraceReq* req;
+    const uint32_t*      prefix;
+    uint32_t             count;
+    uint32_t             total;  // prefix[count]
+    uint8_t*             scratch;
+    size_t               scratch_bytes;
+    size_t               spill_off;
+    DeviceWords*         words;
+    int                  sm_count;
+    int                  blocks_per_sm;
+    int                  collect_stats;
+};
+// Every request's rays in one persistent launch (reference visit order per
+// ray, so each hit equals the single-request result).  The request table and
+// prefix must already be in the scratch.
+cudaError_t launch_trace_batch(const BatchTraceArgs& a, cudaStream_t s);
+
 cudaError_t launch_trace_binary(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_wide(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_persistent(const TraceArgs& a, cudaStream_t s);

@@ -103,17 +103,70 @@ __global__ void __launch_bounds__(kRadix) k_scan_hist(uint32_t* hist)
     h[threadIdx.x] = x - v + add;
 }
 
-template <class K, bool kFirst>
-__global__ void __launch_bounds__(kBlock) k_onesweep(const K* __restrict__ kin,
-                                                     const uint32_t* __restrict__ vin,
-                                                     K* __restrict__ kout,
-                                                     uint32_t* __restrict__ vout,
-                                                     uint32_t n,
-                                                     int      shift,
-                                                     const uint32_t* __restrict__ digit_offsets,
-                                                     uint32_t* tile_counter,
-                                                     uint32_t* lookback,
-                                                     DeviceWords* words)
+// What one onesweep block works on: the key run of one sort (a whole array, or
+// one geometry of a fused build) and its tile within that run.
+template <class K>
+struct SegView
+{
+    const K*        kin;
+    const uint32_t* vin;
+    K*              kout;
+    uint32_t*       vout;
+    uint32_t        n;
+    const uint32_t* digit_offsets;  // this pass's exclusive digit offsets
+    uint32_t*       lookback;       // this pass's status words, 256 per tile
+    uint32_t        tile;           // tile index within the run
+};
+
+// One array (the TLAS build).
+template <class K>
+struct SegSingle
+{
+    const K*        kin;
+    const uint32_t* vin;
+    K*              kout;
+    uint32_t*       vout;
+    uint32_t        n;
+    const uint32_t* digit_offsets;
+    uint32_t*       lookback;
+    __device__ __forceinline__ SegView<K> view(uint32_t t) const
+    {
+        return SegView<K>{kin, vin, kout, vout, n, digit_offsets, lookback, t};
+    }
+};
+
+// Every geometry of a fused build; pass p reads the (codes, idx) pair that
+// pass p - 1 wrote (even passes read s_codes / s_idx).
+template <class K>
+struct SegBatch
+{
+    const BuildItem* items;
+    const uint32_t*  tile_prefix;
+    uint32_t         count;
+    uint32_t         pass;
+    uint32_t         passes;
+    __device__ __forceinline__ SegView<K> view(uint32_t t) const
+    {
+        const uint32_t   g  = batch_find(tile_prefix, count, t);
+        const BuildItem& it = items[g];
+        uint8_t*         sc = it.scratch;
+        const bool       odd = (pass & 1u) != 0;
+        uint32_t*        ss  = reinterpret_cast<uint32_t*>(sc + it.s_sort);
+        SegView<K>       v;
+        v.kin           = reinterpret_cast<const K*>(sc + (odd ? it.s_codes_alt : it.s_codes));
+        v.kout          = reinterpret_cast<K*>(sc + (odd ? it.s_codes : it.s_codes_alt));
+        v.vin           = reinterpret_cast<const uint32_t*>(sc + (odd ? it.s_idx_alt : it.s_idx));
+        v.vout          = reinterpret_cast<uint32_t*>(sc + (odd ? it.s_idx : it.s_idx_alt));
+        v.n             = it.n;
+        v.digit_offsets = ss + pass * kRadix;
+        v.lookback      = ss + passes * kRadix + 64 + (size_t)pass * it.tiles * kRadix;
+        v.tile          = t - __ldg(tile_prefix + g);
+        return v;
+    }
+};
+
+template <class K, bool kFirst, class Seg>
+__global__ void __launch_bounds__(kBlock) k_onesweep(Seg seg, int shift, uint32_t* tile_counter, DeviceWords* words)
 {
     constexpr int kKpt  = Cfg<K>::kKpt;
     constexpr int kTile = kBlock * kKpt;
@@ -129,7 +182,17 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(const K* __restrict__ kin,
     if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
     for (int i = lane; i < kRadix; i += 32) warp_hist[w][i] = 0;
     __syncthreads();
-    const uint32_t tile = s_tile;
+    // Tiles are claimed in order, so every earlier tile of the same run is
+    // already resident or done: the look-back below always makes progress.
+    const SegView<K>      sv            = seg.view(s_tile);
+    const K* __restrict__ kin           = sv.kin;
+    const uint32_t*       vin           = sv.vin;
+    K* __restrict__       kout          = sv.kout;
+    uint32_t* __restrict__ vout         = sv.vout;
+    const uint32_t        n             = sv.n;
+    const uint32_t*       digit_offsets = sv.digit_offsets;
+    uint32_t*             lookback      = sv.lookback;
+    const uint32_t        tile          = sv.tile;
     const uint64_t base = (uint64_t)tile * kTile + (uint64_t)w * 32 * kKpt;
 
     K        key[kKpt];
@@ -257,12 +320,82 @@ __global__ void k_iota(uint32_t* v, uint32_t n)
     if (i < n) v[i] = i;
 }
 
+// Exclusive digit offsets of every (geometry, pass) of a fused build: block
+// g * passes + p scans geometry g's pass-p histogram in place.
+__global__ void __launch_bounds__(kRadix) k_scan_hist_batch(const BuildItem* __restrict__ items, uint32_t passes)
+{
+    __shared__ uint32_t warp_sum[kRadix / 32];
+    const uint32_t      g = blockIdx.x / passes, p = blockIdx.x % passes;
+    const BuildItem&    it = items[g];
+    if (it.n == 0) return;
+    uint32_t* h    = reinterpret_cast<uint32_t*>(it.scratch + it.s_sort) + p * kRadix;
+    uint32_t  v    = h[threadIdx.x];
+    uint32_t  lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t  x    = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    uint32_t add = 0;
+    for (uint32_t k = 0; k < w; ++k) add += warp_sum[k];
+    h[threadIdx.x] = x - v + add;
+}
+
+template <class K>
+cudaError_t batch_passes(const BatchArgs& b, uint32_t passes, DeviceWords* words, cudaStream_t s)
+{
+    for (uint32_t p = 0; p < passes; ++p)
+    {
+        SegBatch<K> seg{b.items, b.tile_prefix, b.count, p, passes};
+        if (p == 0)
+            k_onesweep<K, true><<<b.total_tiles, kBlock, 0, s>>>(seg, (int)(p * kRadixBits), &b.ctl->sort_tile[p],
+                                                                  words);
+        else
+            k_onesweep<K, false><<<b.total_tiles, kBlock, 0, s>>>(seg, (int)(p * kRadixBits), &b.ctl->sort_tile[p],
+                                                                   words);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <class K>
+cudaError_t single_passes(void* codes, void* codes_alt, uint32_t* idx, uint32_t* idx_alt, uint32_t n,
+                          uint32_t passes, uint32_t tiles, const SortScratch& sc, DeviceWords* words, cudaStream_t s)
+{
+    void*     kin  = codes;
+    void*     kout = codes_alt;
+    uint32_t* vin  = idx;
+    uint32_t* vout = idx_alt;
+    for (uint32_t p = 0; p < passes; ++p)
+    {
+        SegSingle<K> seg{(const K*)kin, vin, (K*)kout, vout, n, sc.hist + p * kRadix,
+                         sc.lookback + (size_t)p * tiles * kRadix};
+        if (p == 0)
+            k_onesweep<K, true><<<tiles, kBlock, 0, s>>>(seg, (int)(p * kRadixBits), sc.counters + p, words);
+        else
+            k_onesweep<K, false><<<tiles, kBlock, 0, s>>>(seg, (int)(p * kRadixBits), sc.counters + p, words);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    return cudaSuccess;
+}
+
 }  // namespace
+
+uint32_t radix_sort_tile_keys(int key_bits)
+{
+    return (uint32_t)kBlock * (uint32_t)(key_bits > 32 ? Cfg<uint64_t>::kKpt : Cfg<uint32_t>::kKpt);
+}
 
 size_t radix_sort_scratch_bytes(uint32_t n, int key_bits, uint32_t* tiles_out, uint32_t* passes_out)
 {
-    const int      kpt    = key_bits > 32 ? Cfg<uint64_t>::kKpt : Cfg<uint32_t>::kKpt;
-    const uint32_t tile   = kBlock * kpt;
+    const uint32_t tile   = radix_sort_tile_keys(key_bits);
     const uint32_t tiles  = n == 0 ? 0 : (n + tile - 1) / tile;
     const uint32_t passes = (uint32_t)((key_bits + kRadixBits - 1) / kRadixBits);
     if (tiles_out) *tiles_out = tiles;
@@ -293,42 +426,21 @@ cudaError_t launch_radix_sort(void* codes, void* codes_alt, uint32_t* idx, uint3
     else
         k_global_hist<uint32_t><<<hist_blocks, kBlock, 0, s>>>((const uint32_t*)codes, n, (int)passes, sc.hist);
     k_scan_hist<<<passes, kRadix, 0, s>>>(sc.hist);
-    void*     kin = codes;
-    void*     kout = codes_alt;
-    uint32_t* vin = idx;
-    uint32_t* vout = idx_alt;
-    for (uint32_t p = 0; p < passes; ++p)
-    {
-        uint32_t* lb = sc.lookback + (size_t)p * tiles * kRadix;
-        if (wide)
-        {
-            if (p == 0)
-                k_onesweep<uint64_t, true><<<tiles, kBlock, 0, s>>>((const uint64_t*)kin, vin, (uint64_t*)kout, vout,
-                                                                     n, p * kRadixBits, sc.hist + p * kRadix,
-                                                                     sc.counters + p, lb, words);
-            else
-                k_onesweep<uint64_t, false><<<tiles, kBlock, 0, s>>>((const uint64_t*)kin, vin, (uint64_t*)kout,
-                                                                      vout, n, p * kRadixBits, sc.hist + p * kRadix,
-                                                                      sc.counters + p, lb, words);
-        }
-        else
-        {
-            if (p == 0)
-                k_onesweep<uint32_t, true><<<tiles, kBlock, 0, s>>>((const uint32_t*)kin, vin, (uint32_t*)kout, vout,
-                                                                     n, p * kRadixBits, sc.hist + p * kRadix,
-                                                                     sc.counters + p, lb, words);
-            else
-                k_onesweep<uint32_t, false><<<tiles, kBlock, 0, s>>>((const uint32_t*)kin, vin, (uint32_t*)kout,
-                                                                      vout, n, p * kRadixBits, sc.hist + p * kRadix,
-                                                                      sc.counters + p, lb, words);
-        }
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
+    e = wide ? single_passes<uint64_t>(codes, codes_alt, idx, idx_alt, n, passes, tiles, sc, words, s)
+             : single_passes<uint32_t>(codes, codes_alt, idx, idx_alt, n, passes, tiles, sc, words, s);
+    if (e != cudaSuccess) return e;
     *sorted_in_alt = (passes & 1) != 0;
     return cudaSuccess;
+}
+
+cudaError_t launch_radix_sort_batch(const BatchArgs& b, DeviceWords* words, cudaStream_t s)
+{
+    if (b.total_tiles == 0) return cudaSuccess;
+    const uint32_t passes = b.morton_bits > 32 ? 8u : 4u;
+    k_scan_hist_batch<<<b.count * passes, kRadix, 0, s>>>(b.items, passes);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return b.morton_bits > 32 ? batch_passes<uint64_t>(b, passes, words, s) : batch_passes<uint32_t>(b, passes, words, s);
 }
 
 }  // namespace rr

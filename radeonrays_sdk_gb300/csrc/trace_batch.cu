@@ -1,0 +1,151 @@
+// trace_batch.cu -- many intersection requests (different geometries, ray
+// counts, query kinds and outputs) traced by one persistent launch.
+//
+// No reference counterpart: the reference dispatches isect.comp once per
+// rrCmdIntersect.  This is the launch a serving loop packs its admitted
+// requests into.  The ray space of the launch is the concatenation of the
+// requests' rays; a lane that takes global ray g finds its request by a binary
+// search over the requests' exclusive ray prefix and then runs the same
+// per-ray state machine as the single-request persistent kernel
+// (trace_persistent.cuh): the reference's visit order and arithmetic, so every
+// hit is bit-identical to tracing that request alone with rrCmdIntersect.
+#include "trace_persistent.cuh"
+
+namespace rr
+{
+namespace
+{
+constexpr size_t kBatchHeader = 256;  // ray counter
+
+template <bool kStats>
+__global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, uint32_t gcap)
+{
+    __shared__ uint32_t s_stack[kPBlock * kPShort];
+    const uint32_t      tglob = blockIdx.x * blockDim.x + threadIdx.x;
+    PStack              st;
+    st.s    = s_stack + threadIdx.x;
+    st.g    = reinterpret_cast<uint32_t*>(a.scratch + a.spill_off) + (uint64_t)tglob * gcap;
+    st.gcap = gcap;
+    uint32_t*      ray_ctr = reinterpret_cast<uint32_t*>(a.scratch);
+    const uint32_t lane    = threadIdx.x & 31;
+    const uint32_t lt      = (1u << lane) - 1u;
+    const uint32_t count   = a.total;
+
+    PRay           s;
+    const BvhNode* nodes = nullptr;
+    uint32_t       gid = kInvalid, r = 0, nlim = 0, nf = 0;
+    bool           any = false, active = false, pending = false, exhausted = false;
+    for (;;)
+    {
+        __syncwarp();
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
+        {
+            const uint32_t n    = exhausted ? 0u : __popc(idle);
+            uint32_t       base = 0;
+            if (n)
+            {
+                const int leader = __ffs(idle) - 1;
+                if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+                base      = __shfl_sync(0xffffffffu, base, leader);
+                exhausted = base + n >= count;
+            }
+            if (!active)
+            {
+                if (pending)
+                {
+                    void*      hits = a.req[r].hits;
+                    const bool full = (a.req[r].flags & kReqFull) != 0;
+                    if (s.caddr != kInvalid)
+                    {
+                        const NodeView nd = load_binary_node(nodes, s.caddr);
+                        if (full)
+                            write_hit<true>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                        else
+                            write_hit<false>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                    }
+                    else if (full)
+                        write_miss<true>(hits, gid);
+                    else
+                        write_miss<false>(hits, gid);
+                    if (kStats)
+                    {
+                        atomicAdd(&a.words->rays, 1ull);
+                        atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
+                    }
+                    pending = false;
+                }
+                const uint32_t my = base + __popc(idle & lt);
+                if (n && my < count)
+                {
+                    r                     = batch_find(a.prefix, a.count, my);
+                    gid                   = my - __ldg(a.prefix + r);
+                    const BatchTraceReq& q = a.req[r];
+                    const uint32_t       fl = q.flags;
+                    if (fl & kReqEmpty)
+                    {
+                        if (fl & kReqFull)
+                            write_miss<true>(q.hits, gid);
+                        else
+                            write_miss<false>(q.hits, gid);
+                    }
+                    else
+                    {
+                        active = true;
+                        nf     = 0;
+                        nodes  = reinterpret_cast<const BvhNode*>(q.bvh);
+                        nlim   = q.node_limit;
+                        any    = (fl & kReqAny) != 0;
+                        p_start(s, q.rays, gid);
+                    }
+                }
+            }
+        }
+        const uint32_t amask = __ballot_sync(0xffffffffu, active);
+        if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
+        if (active && p_step<false, true>(s, nodes, nlim, st, a.words, nf, any))
+        {
+            active  = false;
+            pending = true;
+        }
+    }
+}
+
+template <bool kStats>
+cudaError_t go(const BatchTraceArgs& a, cudaStream_t s)
+{
+    auto kern   = k_trace_batch<kStats>;
+    int  per_sm = a.blocks_per_sm;
+    if (per_sm <= 0)
+    {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0) != cudaSuccess) per_sm = 1;
+        per_sm = per_sm > 0 ? per_sm : 1;
+    }
+    const PGrid g = persistent_grid(a.sm_count, per_sm, a.total, a.scratch_bytes, a.spill_off);
+    cudaError_t e = cudaMemsetAsync(a.scratch, 0, kBatchHeader, s);
+    if (e != cudaSuccess) return e;
+    kern<<<g.blocks, kPBlock, 0, s>>>(a, g.gcap);
+    return cudaGetLastError();
+}
+}  // namespace
+
+BatchTraceLayout batch_trace_layout(uint32_t count, uint64_t total_rays)
+{
+    BatchTraceLayout L;
+    L.req_off    = kBatchHeader;
+    L.prefix_off = align_up(L.req_off + (size_t)count * sizeof(BatchTraceReq), kAlign);
+    L.spill_off  = align_up(L.prefix_off + ((size_t)count + 1) * sizeof(uint32_t), kAlign);
+    // The single-request scratch per ray (trace_scratch_bytes) minus its
+    // header: the persistent grid takes its spill stacks from it.
+    L.total = L.spill_off + (trace_scratch_bytes(total_rays > 0xffffffffull ? 0xffffffffu : (uint32_t)total_rays) -
+                             kTraceScratchHeader);
+    return L;
+}
+
+cudaError_t launch_trace_batch(const BatchTraceArgs& a, cudaStream_t s)
+{
+    if (a.total == 0) return cudaSuccess;
+    return a.collect_stats ? go<true>(a, s) : go<false>(a, s);
+}
+
+}  // namespace rr

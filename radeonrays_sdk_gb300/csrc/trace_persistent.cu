@@ -1,11 +1,8 @@
 // trace_persistent.cu -- persistent lane-refill traversal over the reference's
 // 64-byte binary nodes.
 //
-// The per-ray algorithm is the reference's (vlk/kernels/isect.comp:105-245):
-// the same slab and triangle arithmetic (trace_common.cuh), near child first
-// (child 1 iff it is hit and child 0's entry distance is larger), a LIFO stack
-// of deferred children, strict `t < closest_t` accept.  The visit order is
-// therefore exactly the reference's and the hits are bit-identical to the
+// The per-ray algorithm (trace_persistent.cuh, p_step) is the reference's
+// (vlk/kernels/isect.comp:105-245), so the hits are bit-identical to the
 // plain kernel and to the oracle, ties and any-hit choices included.
 //
 // What differs is the scheduling: a persistent grid whose lanes each advance
@@ -15,116 +12,12 @@
 // idle while its longest ray finishes; refilling keeps them working.  The
 // stack is a short stack in shared memory (interleaved across the block) that
 // spills to a per-thread region of the caller's scratch buffer.
-#include "rr_internal.h"
-#include "trace_common.cuh"
+#include "trace_persistent.cuh"
 
 namespace rr
 {
 namespace
 {
-constexpr int      kPBlock    = 128;
-constexpr int      kPShort    = 32;   // shared short-stack entries per thread
-constexpr uint32_t kPSpillCap = 256;  // global spill entries per thread (binary LBVH depth <= 64)
-constexpr uint32_t kPRefillMin = 8;   // idle lanes that trigger a refill
-
-struct PRay
-{
-    Ray      ray;
-    F3       inv, oxi;
-    float    ct;
-    uint32_t caddr;  // leaf of the closest hit
-    uint32_t addr;   // node to fetch next
-    uint32_t gsp;    // entries spilled to global
-    uint32_t steps;
-    int      sp;     // entries in the short stack
-};
-
-struct PStack
-{
-    uint32_t* s;  // this thread's first short-stack entry (shared), entries kPBlock apart
-    uint32_t* g;  // global spill region
-    uint32_t  gcap;
-    __device__ __forceinline__ uint32_t& at(int k) const { return s[k * kPBlock]; }
-};
-
-// One iteration of the reference's traversal loop.  Returns true when the ray
-// is finished (stack empty, or a hit accepted by an any-hit query).
-template <bool kAny>
-__device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ nodes, uint32_t node_limit,
-                                       const PStack& st, DeviceWords* words, uint32_t& nf)
-{
-    if (++s.steps > kFetchCap || s.addr >= node_limit)
-    {
-        raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
-        s.caddr = kInvalid;
-        return true;
-    }
-    const NodeView nd = load_binary_node(nodes, s.addr);
-    ++nf;
-    // Single exit: the internal-node and leaf paths rejoin before the pop.
-    bool pop = true, done = false;
-    if (nd.child0 != kInvalid)
-    {
-        float a0, a1, b0, b1;
-        isect_box(nd.l0, nd.h0, s.inv, s.oxi, s.ct, s.ray.tmin, a0, a1);
-        isect_box(nd.l1, nd.h1, s.inv, s.oxi, s.ct, s.ray.tmin, b0, b1);
-        const bool tc0 = a0 <= a1, tc1 = b0 <= b1;
-        const bool c1f = tc1 && (a0 > b0);
-        if (tc0 || tc1)
-        {
-            const bool     first1   = c1f || !tc0;
-            const uint32_t next     = first1 ? nd.child1 : nd.child0;
-            const uint32_t deferred = first1 ? nd.child0 : nd.child1;
-            if (tc0 && tc1)
-            {
-                if (s.sp == kPShort)
-                {
-                    if (s.gsp + kPShort > st.gcap)
-                    {
-                        raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
-                        s.sp = kPShort - 1;  // overwrite the top entry: result flagged invalid
-                    }
-                    else
-                    {
-                        for (int k = 0; k < kPShort; ++k) st.g[s.gsp + k] = st.at(k);
-                        s.gsp += kPShort;
-                        s.sp = 0;
-                    }
-                }
-                st.at(s.sp++) = deferred;
-            }
-            s.addr = next;
-            pop    = false;
-        }
-    }
-    else
-    {
-        const float t = isect_tri(s.ray, nd.l0, nd.h0, nd.l1, s.ct);
-        if (t < s.ct)
-        {
-            s.ct    = t;
-            s.caddr = s.addr;
-            if (kAny) done = true;
-        }
-    }
-    if (pop && !done)
-    {
-        if (s.sp == 0 && s.gsp == 0)
-            done = true;
-        else
-        {
-            if (s.sp == 0)
-            {
-                s.gsp -= kPShort;
-                for (int k = 0; k < kPShort; ++k) st.at(k) = st.g[s.gsp + k];
-                s.sp = kPShort;
-            }
-            s.addr = st.at(--s.sp);
-        }
-    }
-    return done;
-}
-
 template <bool kAny, bool kFull, bool kStats>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, uint32_t gcap)
 {
@@ -187,16 +80,9 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         write_miss<kFull>(a.hits, gid);
                     else
                     {
-                        active  = true;
-                        nf      = 0;
-                        s.ray   = load_ray(a.rays, gid);
-                        s.inv   = safe_invdir(s.ray.d);
-                        s.oxi   = f3(-s.ray.o.x * s.inv.x, -s.ray.o.y * s.inv.y, -s.ray.o.z * s.inv.z);
-                        s.ct    = s.ray.tmax;
-                        s.caddr = kInvalid;
-                        s.addr  = 0;
-                        s.gsp = s.steps = 0;
-                        s.sp            = 0;
+                        active = true;
+                        nf     = 0;
+                        p_start(s, a.rays, gid);
                     }
                 }
             }
@@ -221,17 +107,10 @@ cudaError_t go(const TraceArgs& a, cudaStream_t s)
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0) != cudaSuccess) per_sm = 1;
         per_sm = per_sm > 0 ? per_sm : 1;
     }
-    uint64_t       threads = (uint64_t)a.sm_count * per_sm * kPBlock;
-    const uint64_t need    = ((uint64_t)a.ray_count + 31) / 32 * 32;
-    if (threads > need) threads = (need + kPBlock - 1) / kPBlock * kPBlock;
-    const int      blocks = (int)(threads / kPBlock);
-    threads               = (uint64_t)blocks * kPBlock;
-    uint64_t gcap = (a.scratch_bytes - kTraceScratchHeader) / (threads * sizeof(uint32_t));
-    gcap          = gcap / kPShort * kPShort;
-    if (gcap > kPSpillCap) gcap = kPSpillCap;
+    const PGrid g = persistent_grid(a.sm_count, per_sm, a.ray_count, a.scratch_bytes, kTraceScratchHeader);
     cudaError_t e = cudaMemsetAsync(a.scratch, 0, kTraceScratchHeader, s);
     if (e != cudaSuccess) return e;
-    kern<<<blocks, kPBlock, 0, s>>>(a, (uint32_t)gcap);
+    kern<<<g.blocks, kPBlock, 0, s>>>(a, g.gcap);
     return cudaGetLastError();
 }
 }  // namespace

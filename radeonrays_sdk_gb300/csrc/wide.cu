@@ -126,23 +126,6 @@ __device__ __forceinline__ uint32_t collect_leaves(const BvhNode* nodes, uint32_
     return cnt;
 }
 
-// Warp-aggregated atomicAdd over a full warp (all 32 lanes must call it):
-// every lane adds v and gets its own offset.
-__device__ __forceinline__ uint32_t warp_add(uint32_t* ctr, uint32_t v)
-{
-    const int lane = threadIdx.x & 31;
-    uint32_t  x    = v;
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
-    uint32_t       base  = 0;
-    if (lane == 31 && total) base = atomicAdd(ctr, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    return base + x - v;
-}
 
 // Exponent e (biased) of the smallest power of two s with ceil(ext / s) <= 255.
 __device__ __forceinline__ int pick_exp(float lo, float hi)
@@ -162,25 +145,66 @@ __device__ __forceinline__ int pick_exp(float lo, float hi)
     return ex;
 }
 
-__global__ void k_collapse_init(const BvhNode* nodes, uint32_t n, CollapseCtl* ctl, Item* q0, WideNode* wn,
-                                WideTri* wt)
+// Per-geometry views of a fused build's collapse state.
+__device__ __forceinline__ CollapseCtl* ctl_of(const BuildItem& it)
 {
-    if (threadIdx.x != 0) return;
+    return reinterpret_cast<CollapseCtl*>(it.scratch + it.s_queue);
+}
+__device__ __forceinline__ Item* queue_of(const BuildItem& it, int level)
+{
+    Item* q0 = reinterpret_cast<Item*>(it.scratch + it.s_queue + 2 * kAlign);
+    return (level & 1) ? q0 + it.n : q0;
+}
+
+// Warp-aggregated atomicAdd where the lanes form runs of equal counters:
+// `peers` is the lane's run (lanes with the same counter, contiguous), v its
+// addend.  All 32 lanes must call it; a run with valid == false adds nothing.
+__device__ __forceinline__ uint32_t run_add(uint32_t* ctr, uint32_t v, uint32_t peers, bool valid)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t  x    = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const int      first  = __ffs(peers) - 1;
+    const int      last   = 31 - __clz(peers);
+    const uint32_t before = __shfl_sync(0xffffffffu, x - v, first);
+    const uint32_t total  = __shfl_sync(0xffffffffu, x, last) - before;
+    uint32_t       base   = 0;
+    if (lane == last && valid && total) base = atomicAdd(ctr, total);
+    base = __shfl_sync(0xffffffffu, base, last);
+    return base + (x - v) - before;
+}
+
+__global__ void k_collapse_init(BatchArgs b)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.count) return;
+    const BuildItem& it = b.items[g];
+    const uint32_t   n  = it.n;
+    if (n == 0) return;
+    const BvhNode* nodes = reinterpret_cast<const BvhNode*>(it.result);
+    CollapseCtl*   ctl   = ctl_of(it);
+    Item*          q0    = queue_of(it, 0);
+    WideNode*      wn    = reinterpret_cast<WideNode*>(it.result + it.wide_off);
+    WideTri*       wt    = reinterpret_cast<WideTri*>(it.result + it.tris_off);
     for (int i = 0; i < kMaxLevels + 2; ++i) ctl->level_count[i] = 0;
     if (n == 1)
     {
         // A one-triangle mesh: one wide node with a single triangle slot.
         BvhNode  lf = nodes[0];
         WideNode w{};
-        Bx       b = node_union(lf);
+        Bx       bx = node_union(lf);
         for (int k = 0; k < 3; ++k)
         {
-            w.p[k] = b.lo[k];
-            int e  = pick_exp(b.lo[k], b.hi[k]);
+            w.p[k] = bx.lo[k];
+            int e  = pick_exp(bx.lo[k], bx.hi[k]);
             w.e[k] = (uint8_t)e;
             float inv = __uint_as_float((uint32_t)(254 - e) << 23);
             w.qlo[k][0] = 0;
-            w.qhi[k][0] = (uint8_t)min(255.f, ceilf(__fmul_ru(__fsub_ru(b.hi[k], b.lo[k]), inv)));
+            w.qhi[k][0] = (uint8_t)min(255.f, ceilf(__fmul_ru(__fsub_ru(bx.hi[k], bx.lo[k]), inv)));
         }
         w.imask      = 0;
         w.child_base = 0;
@@ -211,17 +235,58 @@ __global__ void k_collapse_init(const BvhNode* nodes, uint32_t n, CollapseCtl* c
     ctl->tri_count     = 0;
 }
 
-__global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restrict__ nodes, int level,
-                                                        CollapseCtl* ctl, const Item* __restrict__ qin,
-                                                        Item* __restrict__ qout, WideNode* wn, WideTri* wt,
-                                                        uint32_t wide_capacity, uint32_t tri_capacity,
-                                                        DeviceWords* words)
+// Exclusive prefix over geometries of this level's work items (one block).
+constexpr int kScanBlock = 1024;
+__global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int level)
 {
-    const uint32_t count = *((volatile uint32_t*)&ctl->level_count[level]);
-    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < ((count + 31u) & ~31u);
+    __shared__ uint32_t warp_sum[kScanBlock / 32];
+    const uint32_t per = (b.count + kScanBlock - 1) / kScanBlock;
+    const uint32_t g0  = threadIdx.x * per;
+    uint32_t       sum = 0;
+    for (uint32_t g = g0; g < g0 + per && g < b.count; ++g)
+        if (b.items[g].n > 0) sum += ctl_of(b.items[g])->level_count[level];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t  x    = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    uint32_t add = 0;
+    for (int k = 0; k < w; ++k) add += warp_sum[k];
+    uint32_t run = x - sum + add;
+    for (uint32_t g = g0; g < g0 + per && g < b.count; ++g)
+    {
+        b.level_prefix[g] = run;
+        if (b.items[g].n > 0) run += ctl_of(b.items[g])->level_count[level];
+    }
+    if (threadIdx.x == kScanBlock - 1) b.level_prefix[b.count] = x + add;
+}
+
+// One level of the collapse for every geometry: work item `it` of the level
+// belongs to the geometry found in the level prefix (a batch of one reads
+// its count directly).
+__global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, DeviceWords* words)
+{
+    const uint32_t total = b.count == 1 ? *((volatile uint32_t*)&ctl_of(b.items[0])->level_count[level])
+                                        : *((volatile uint32_t*)&b.level_prefix[b.count]);
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < ((total + 31u) & ~31u);
          it += gridDim.x * blockDim.x)
     {
-        const bool active = it < count;
+        const bool     active = it < total;
+        const uint32_t g      = !active ? 0xffffffffu : (b.count == 1 ? 0u : batch_find(b.level_prefix, b.count, it));
+        const uint32_t peers  = __match_any_sync(0xffffffffu, g);
+        const BuildItem* bi   = active ? b.items + g : b.items;
+        const uint32_t local  = active ? it - (b.count == 1 ? 0u : __ldg(b.level_prefix + g)) : 0u;
+        const BvhNode* __restrict__ nodes = reinterpret_cast<const BvhNode*>(bi->result);
+        CollapseCtl*   ctl           = ctl_of(*bi);
+        const Item* __restrict__ qin = queue_of(*bi, level);
+        Item* __restrict__ qout      = queue_of(*bi, level + 1);
+        WideNode*      wn            = reinterpret_cast<WideNode*>(bi->result + bi->wide_off);
+        WideTri*       wt            = reinterpret_cast<WideTri*>(bi->result + bi->tris_off);
+        const uint32_t wide_capacity = bi->wide_capacity, tri_capacity = bi->tri_capacity;
         uint32_t   ch[8];
         Bx         cb[8];
         bool       cint[8];
@@ -229,7 +294,7 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
         Item       item{0, 0};
         if (active)
         {
-            item          = qin[it];
+            item          = qin[local];
             BvhNode root  = load_node(nodes, item.b);
             ch[0]         = root.child0;
             ch[1]         = root.child1;
@@ -293,9 +358,9 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
         }
         // Allocate (warp-aggregated over the full warp; inactive lanes add 0).
         __syncwarp();
-        const uint32_t child_base = warp_add(&ctl->wide_count, n_int);
-        const uint32_t tri_base   = warp_add(&ctl->tri_count, n_leaf);
-        const uint32_t qpos       = warp_add(&ctl->level_count[level + 1], n_int);
+        const uint32_t child_base = run_add(&ctl->wide_count, n_int, peers, active);
+        const uint32_t tri_base   = run_add(&ctl->tri_count, n_leaf, peers, active);
+        const uint32_t qpos       = run_add(&ctl->level_count[level + 1], n_int, peers, active);
         if (!active) continue;
         if (child_base + n_int > wide_capacity || tri_base + n_leaf > tri_capacity)
         {
@@ -417,9 +482,14 @@ __global__ void __launch_bounds__(128) k_collapse_level(const BvhNode* __restric
     }
 }
 
-__global__ void k_collapse_finish(CollapseCtl* ctl, Trailer* tr, DeviceWords* words)
+__global__ void k_collapse_finish(BatchArgs b, DeviceWords* words)
 {
-    if (threadIdx.x != 0) return;
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.count) return;
+    const BuildItem& it = b.items[g];
+    if (it.n == 0) return;
+    const CollapseCtl* ctl = ctl_of(it);
+    Trailer*           tr  = reinterpret_cast<Trailer*>(it.result + it.trailer_off);
     if (ctl->level_count[kMaxLevels] != 0) atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH);
     tr->wide_count     = ctl->wide_count;
     tr->wide_tri_count = ctl->tri_count;
@@ -427,33 +497,28 @@ __global__ void k_collapse_finish(CollapseCtl* ctl, Trailer* tr, DeviceWords* wo
 
 }  // namespace
 
-cudaError_t launch_collapse_wide(const GeomLayout& L, uint8_t* scratch, uint8_t* result, DeviceWords* words,
-                                 int sm_count, cudaStream_t s)
+cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s)
 {
-    if (L.n == 0) return cudaSuccess;
-    CollapseCtl*    ctl   = reinterpret_cast<CollapseCtl*>(scratch + L.s_queue);
-    Item*           q0    = reinterpret_cast<Item*>(scratch + L.s_queue + 2 * kAlign);
-    Item*           q1    = q0 + L.n;
-    const BvhNode*  nodes = reinterpret_cast<const BvhNode*>(result);
-    WideNode*       wn    = reinterpret_cast<WideNode*>(result + L.wide_off);
-    WideTri*        wt    = reinterpret_cast<WideTri*>(result + L.tris_off);
-    Trailer*        tr    = reinterpret_cast<Trailer*>(result + L.trailer_off);
+    if (b.count == 0 || b.total_prims == 0) return cudaSuccess;
     static_assert(sizeof(CollapseCtl) <= 2 * kAlign, "collapse control block");
-    k_collapse_init<<<1, 32, 0, s>>>(nodes, L.n, ctl, q0, wn, wt);
-    if (L.n > 1)
+    const int per_geom = (int)((b.count + 127) / 128);
+    k_collapse_init<<<per_geom, 128, 0, s>>>(b);
+    if (b.max_n > 1)
     {
-        uint64_t bound = 1;
+        // Work items of a level are bounded by count * 8^level and by the
+        // number of triangles (every item is a distinct internal subtree).
+        uint64_t bound = b.count;
         for (int level = 0; level < kMaxLevels; ++level)
         {
-            const uint64_t cap    = std::min<uint64_t>(bound, (uint64_t)L.n);
-            const int      blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((cap + 127) / 128, (uint64_t)sm_count * 16));
-            k_collapse_level<<<blocks, 128, 0, s>>>(nodes, level, ctl, (level & 1) ? q1 : q0, (level & 1) ? q0 : q1,
-                                                    wn, wt, (uint32_t)L.wide_capacity, (uint32_t)L.tri_capacity,
-                                                    words);
-            bound = std::min<uint64_t>(bound * 8, (uint64_t)L.n);
+            if (b.count > 1) k_level_scan<<<1, kScanBlock, 0, s>>>(b, level);
+            const uint64_t cap    = std::min<uint64_t>(bound, b.total_prims);
+            const int      blocks = (int)std::max<uint64_t>(
+                1, std::min<uint64_t>((cap + 127) / 128, (uint64_t)sm_count * 16));
+            k_collapse_level<<<blocks, 128, 0, s>>>(b, level, words);
+            bound = std::min<uint64_t>(bound * 8, b.total_prims);
         }
     }
-    k_collapse_finish<<<1, 32, 0, s>>>(ctl, tr, words);
+    k_collapse_finish<<<per_geom, 128, 0, s>>>(b, words);
     return cudaGetLastError();
 }
 

@@ -116,7 +116,13 @@ class RRCudaTraversalStats(C.Structure):
                 ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64)]
 
 
+class RRCudaIntersectRequest(C.Structure):
+    _fields_ = [("geometry", C.c_void_p), ("query", C.c_int), ("output", C.c_int), ("rays", C.c_void_p),
+                ("ray_count", C.c_uint32), ("hits", C.c_void_p)]
+
+
 assert C.sizeof(RRGeometryBuildInput) == 16 and C.sizeof(RRInstance) == 56 and C.sizeof(RRMemoryRequirements) == 24
+assert C.sizeof(RRCudaIntersectRequest) == 40
 
 # Every symbol the headers declare, with its ctypes prototype.
 _P = C.c_void_p
@@ -155,6 +161,10 @@ PROTOTYPES = {
     "rrCudaIntersectNoAlloc": [_P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
     "rrCudaAutotuneTraversal": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P,
                                 C.POINTER(RRCudaTraversalOptions)],
+    "rrCudaCmdBuildGeometries": [_P, C.c_uint32, C.POINTER(RRGeometryBuildInput), C.POINTER(RRBuildOptions), _PP,
+                                 _PP, _P],
+    "rrCudaGetIntersectBatchMemoryRequirements": [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_size_t)],
+    "rrCudaCmdIntersectBatch": [_P, C.c_uint32, C.POINTER(RRCudaIntersectRequest), _P, _P],
 }
 
 _LIB = None
@@ -280,6 +290,63 @@ class Context:
             self.release_stream(cs)
         return result
 
+    def build_geometries(self, meshes, node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30, stream=None,
+                         api="batch"):
+        """Build many meshes [(vertices (V, 3) float32, indices (T, 3) int32), ...] (cuda tensors).
+
+        api "batch": one rrCudaCmdBuildGeometries call (one fused build);
+        "record": one rrCmdBuildGeometry per mesh on an internal command
+        stream (fused when the stream is submitted); "separate": one
+        rrCmdBuildGeometry per mesh on an external stream (each runs alone).
+        Scratch and results are slices of two device buffers at 256-byte
+        offsets.  Returns the list of result tensors (views)."""
+        torch = _torch()
+        n = len(meshes)
+        opts, keep = self._options(node_format, morton_bits)
+        reqs, inputs = [], []
+        for v, i in meshes:
+            ntri = i.numel() // 3
+            bi, mesh = self._build_input(self.ptr(v) if ntri else None, v.numel() // 3, 12,
+                                         self.ptr(i) if ntri else None, ntri, False)
+            inputs.append((bi, mesh))
+            req = RRMemoryRequirements()
+            check(self.L.rrGetGeometryBuildMemoryRequirements(self.ctx, C.byref(bi), C.byref(opts), C.byref(req)),
+                  "rrGetGeometryBuildMemoryRequirements")
+            reqs.append((req.temporary_build_buffer_size, req.result_buffer_size))
+        al = lambda x: (x + 255) // 256 * 256  # noqa: E731
+        s_off = np.cumsum([0] + [al(s) for s, _ in reqs])
+        r_off = np.cumsum([0] + [al(r) for _, r in reqs])
+        dev = meshes[0][0].device if n else torch.device("cuda")
+        scratch = torch.empty(max(int(s_off[-1]), 256), dtype=torch.uint8, device=dev)
+        result = torch.empty(max(int(r_off[-1]), 256), dtype=torch.uint8, device=dev)
+        s_ptrs = [self.ptr(scratch, int(s_off[k])) for k in range(n)]
+        r_ptrs = [self.ptr(result, int(r_off[k])) for k in range(n)]
+        if api == "separate":
+            cs = self.external_stream(torch.cuda.current_stream(dev))
+            for k in range(n):
+                check(self.L.rrCmdBuildGeometry(self.ctx, RR_BUILD_OPERATION_BUILD, C.byref(inputs[k][0]),
+                                                C.byref(opts), s_ptrs[k], r_ptrs[k], cs), "rrCmdBuildGeometry")
+            torch.cuda.current_stream(dev).synchronize()
+            check(self.L.rrReleaseExternalCommandStream(self.ctx, cs), "rrReleaseExternalCommandStream")
+        else:
+            own = stream is None
+            cs = self.command_stream() if own else stream
+            if api == "batch":
+                arr = (RRGeometryBuildInput * max(n, 1))(*[b for b, _ in inputs])
+                sp = (C.c_void_p * max(n, 1))(*[p.value for p in s_ptrs])
+                rp = (C.c_void_p * max(n, 1))(*[p.value for p in r_ptrs])
+                check(self.L.rrCudaCmdBuildGeometries(self.ctx, n, arr, C.byref(opts), sp, rp, cs),
+                      "rrCudaCmdBuildGeometries")
+            else:
+                for k in range(n):
+                    check(self.L.rrCmdBuildGeometry(self.ctx, RR_BUILD_OPERATION_BUILD, C.byref(inputs[k][0]),
+                                                    C.byref(opts), s_ptrs[k], r_ptrs[k], cs), "rrCmdBuildGeometry")
+            if own:
+                self.submit(cs)
+                self.release_stream(cs)
+        self._keep = (scratch, inputs)
+        return [result[int(r_off[k]): int(r_off[k]) + reqs[k][1]] for k in range(n)]
+
     def build_scene(self, geometries, transforms, stream=None):
         """geometries: list of result tensors; transforms: (I, 3, 4) float array (object->world)."""
         torch = _torch()
@@ -329,6 +396,46 @@ class Context:
         scratch = torch.empty(self.trace_scratch_bytes(max(R, 1)), dtype=torch.uint8, device=rays.device)
         cs = self.command_stream()
         self.cmd_intersect(bvh, rays, R, hits, scratch, cs, query, output, indirect)
+        self.submit(cs)
+        self.release_stream(cs)
+        return hits
+
+    # -- many requests in one launch
+    def batch_scratch_bytes(self, request_count: int, total_rays: int) -> int:
+        n = C.c_size_t()
+        check(self.L.rrCudaGetIntersectBatchMemoryRequirements(self.ctx, request_count, total_rays, C.byref(n)),
+              "rrCudaGetIntersectBatchMemoryRequirements")
+        return n.value
+
+    def cmd_intersect_batch(self, reqs, scratch, stream):
+        """reqs: [(bvh tensor, rays tensor (R, 8) or (ptr, R), hits tensor or ptr, query, output), ...] with
+        device tensors or raw device addresses; records one rrCudaCmdIntersectBatch."""
+        n = len(reqs)
+        arr = (RRCudaIntersectRequest * n)()
+        for k, (bvh, rays, hits, q, o) in enumerate(reqs):
+            if isinstance(rays, tuple):
+                rays_ptr, count = rays
+            else:
+                rays_ptr, count = rays, rays.shape[0]
+            arr[k] = RRCudaIntersectRequest(self.ptr(bvh), q, o, self.ptr(rays_ptr) if count else None, count,
+                                            self.ptr(hits) if count else None)
+        check(self.L.rrCudaCmdIntersectBatch(self.ctx, n, arr, self.ptr(scratch), stream), "rrCudaCmdIntersectBatch")
+
+    def intersect_batch(self, reqs):
+        """reqs: [(bvh, rays (R, 8) cuda tensor, query, output), ...] -> list of hit tensors (one launch)."""
+        torch = _torch()
+        hits = []
+        full = []
+        for bvh, rays, q, o in reqs:
+            R = rays.shape[0]
+            h = torch.full((R, 4) if o == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT else (R,), -1, dtype=torch.int32,
+                           device=rays.device)
+            hits.append(h)
+            full.append((bvh, rays, h, q, o))
+        total = sum(r.shape[0] for _, r, _, _ in reqs)
+        scratch = torch.empty(self.batch_scratch_bytes(len(reqs), total), dtype=torch.uint8, device="cuda")
+        cs = self.command_stream()
+        self.cmd_intersect_batch(full, scratch, cs)
         self.submit(cs)
         self.release_stream(cs)
         return hits
