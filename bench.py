@@ -65,10 +65,16 @@ def parse():
     ap.add_argument("--block", type=int, default=0, help="chosen kernel threads per block (0: library default)")
     ap.add_argument("--per-sm", type=int, default=0, help="chosen kernel resident blocks per SM (0: occupancy)")
     ap.add_argument("--ray-order", type=int, default=0, help="chosen kernel: 0 default, 1 given order, 2 sorted")
-    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "blas2048"],
-                    help="heightfield: the headline line; blas2048: fused multi-BLAS build + two-level traversal")
+    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "blas2048", "serving"],
+                    help="heightfield: the headline line; blas2048: fused multi-BLAS build + two-level traversal; "
+                         "serving: resident scenes + continuous batching")
     ap.add_argument("--blas", type=int, default=2048)
     ap.add_argument("--batch-rays", type=int, default=8_388_608)
+    ap.add_argument("--scenes", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=300)
+    ap.add_argument("--slots", type=int, default=3)
+    ap.add_argument("--slot-rays", type=int, default=1 << 22)
+    ap.add_argument("--hbm-budget-gb", type=float, default=120.0)
     ap.add_argument("--chosen", type=int, default=0,
                     help="chosen traversal: 0 autotuned (rrCudaAutotuneTraversal), 2 wide (8-wide nodes), "
                          "3 binary persistent")
@@ -512,12 +518,64 @@ def run_batch(args):
     ctx.close()
 
 
+def run_serving(args):
+    """--workload serving: 64 resident scenes (log-uniform 10^4..2x10^6
+    triangles, soup or heightfield), Poisson arrivals of log-uniform 1,024..
+    1,048,576-ray requests (70% closest, 30% any-hit), continuous batching
+    into rrCudaCmdIntersectBatch launches.  Saturation throughput first (all
+    requests at t = 0), then offered loads of 50/80/95% of it: throughput and
+    p50/p99 request latency (arrival to hits in host memory)."""
+    import torch
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    from radeonrays_sdk_gb300 import rr, serving
+    meshes = serving.config4(args.scenes)
+    ntri = sum(i.shape[0] for _, i in meshes)
+    ctx = rr.Context()
+    pool = serving.ScenePool(ctx, int(args.hbm_budget_gb * (1 << 30)))
+    for k, (v, i) in enumerate(meshes):
+        pool.register(k, v, i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(len(meshes)):
+        pool.acquire(k)
+        pool.release(k)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    server = serving.Server(ctx, pool, slot_rays=args.slot_rays, slots=args.slots, max_requests=256)
+    warm = serving.make_requests(meshes, 16, rate_per_s=1e9, seed=40)
+    server.run(warm)
+    sat_reqs = serving.make_requests(meshes, args.requests, rate_per_s=1e9, seed=41)
+    sat = server.run(sat_reqs)
+    mean_rays = sat["rays"] / sat["requests"]
+    cap = sat["throughput_mrays_s"] * 1e6 / mean_rays  # requests per second at saturation
+    sweep = []
+    for k, frac in enumerate((0.5, 0.8, 0.95)):
+        reqs = serving.make_requests(meshes, args.requests, rate_per_s=frac * cap, seed=42 + k)
+        res = server.run(reqs)
+        res["offered_load"] = frac
+        res["rate_req_s"] = frac * cap
+        sweep.append(res)
+    line = {"metric": "serving: throughput Mrays/s and p50/p99 request latency (continuous batching)",
+            "workload": f"{len(meshes)} resident scenes ({ntri:,} triangles), requests of 1,024..1,048,576 rays "
+                        "(log-uniform), 70% closest / 30% any-hit (tmax U[0.01,0.5]), incoherent rays in each "
+                        "scene's box, Poisson arrivals",
+            "slots": args.slots, "slot_rays": args.slot_rays, "hbm_budget_gb": args.hbm_budget_gb,
+            "scene_build_s": build_s, "resident_bytes": pool.bytes, "saturation": sat, "load_sweep": sweep,
+            "latency_definition": "arrival to hits copied to the request's pinned host buffer",
+            "device_errors": ctx.device_errors()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "blas2048":
         run_batch(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

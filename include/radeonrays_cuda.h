@@ -44,7 +44,8 @@ typedef struct
 /* ---- traversal kernel selection ---------------------------------------- */
 typedef enum
 {
-    /* Wide kernel when the buffer holds wide nodes, else the binary kernel. */
+    /* Geometry: the wide kernel when the buffer holds wide nodes, else the
+     * binary kernel.  Scene: the persistent binary two-level kernel. */
     RR_CUDA_TRAVERSAL_AUTO = 0,
     /* One thread per ray, 64-byte binary nodes, reference visit order. */
     RR_CUDA_TRAVERSAL_BINARY = 1,

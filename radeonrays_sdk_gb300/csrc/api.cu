@@ -546,7 +546,10 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         sa.xforms     = reinterpret_cast<const float*>(bvh + bi.xforms_off);
         sa.inst       = reinterpret_cast<const InstanceDesc*>(bvh + bi.inst_off);
         sa.inst_count = bi.n;
-        sa.use_wide   = bi.scene_wide && trav != RR_CUDA_TRAVERSAL_BINARY;
+        // AUTO: the persistent binary two-level kernel (fastest on incoherent
+        // rays; the 8-wide BLAS kernel stays selectable as WIDE).
+        sa.use_wide       = bi.scene_wide && trav == RR_CUDA_TRAVERSAL_WIDE;
+        sa.use_persistent = trav == RR_CUDA_TRAVERSAL_AUTO || trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT;
         return [=](cudaStream_t s) { return launch_trace_scene(sa, s); };
     }
     // Geometry (registered) or an unknown buffer, traversed as binary nodes
@@ -1268,7 +1271,7 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
                 cand.push_back(o);
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);
-            if (bi.kind != kKindScene) add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
+            add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
             if (has_wide)
             {
                 add(RR_CUDA_TRAVERSAL_WIDE, 1);

@@ -320,9 +320,11 @@ struct SceneTraceArgs
     const float*        xforms;     // [inverse, forward] 12 floats each
     const InstanceDesc* inst;
     uint32_t            inst_count;
-    int                 use_wide;
+    int                 use_wide;        // 8-wide BLAS kernel
+    int                 use_persistent;  // persistent binary two-level kernel
 };
 cudaError_t launch_trace_scene(const SceneTraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_scene_persistent(const SceneTraceArgs& a, cudaStream_t s);
 
 struct SceneBuildArgs
 {

@@ -39,7 +39,7 @@ def test_scene_trace(ctx, orc, fmt):
             ctx.set_traversal(1)
             plain = hits_np(ctx.intersect(scene, rays, query=q, output=o))
             assert np.array_equal(plain, g[f"hits_q{q}_o{o}"]), (q, o)
-            ctx.set_traversal(0)
+            ctx.set_traversal(2)  # the 8-wide BLAS kernel (plain binary when the BLASes have no wide nodes)
             chosen = hits_np(ctx.intersect(scene, rays, query=q, output=o))
             want = g[f"hits_q{q}_o{o}"]
             if o == 0:
@@ -51,6 +51,42 @@ def test_scene_trace(ctx, orc, fmt):
             else:
                 assert np.array_equal(chosen != INVALID, want != INVALID)
     ctx.set_traversal(0)
+    assert ctx.device_errors() == 0
+
+
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_scene_trace_persistent_bit_identical(ctx, orc, fmt):
+    """The persistent two-level kernel (AUTO and BINARY_PERSISTENT) keeps the
+    reference visit order: hits equal the oracle's bit for bit."""
+    g = golden("scene6")
+    _, scene = scene_from_fixture(ctx, g, fmt)
+    rays = to_dev(g["rays"])
+    for trav in (0, 3):
+        for q in (0, 1):
+            for o in (0, 1):
+                ctx.set_traversal(trav)
+                got = hits_np(ctx.intersect(scene, rays, query=q, output=o))
+                assert np.array_equal(got, g[f"hits_q{q}_o{o}"]), (trav, q, o)
+    ctx.set_traversal(0)
+    assert ctx.device_errors() == 0
+
+
+def test_scene_persistent_larger(ctx, orc):
+    from radeonrays_sdk_gb300 import scenes
+    blas_np, M, rays = scenes.config2(n_blas=40, lo_tris=16, hi_tris=5000, nrays=60000)
+    fused = ctx.build_geometries([(to_dev(v), to_dev(i)) for v, i in blas_np], node_format=0)
+    scene = ctx.build_scene(fused, M)
+    onodes = [orc.build_mesh(v, i)[0] for v, i in blas_np]
+    tlas, xf = orc.build_scene(onodes, [i.shape[0] for _, i in blas_np], M)
+    for q in (0, 1):
+        r = rays.copy()
+        if q == 1:
+            r[:, 7] = np.float32(5.0)
+        want = orc.trace_scene(tlas, xf, onodes, r, query=q)
+        ctx.set_traversal(3)
+        got = hits_np(ctx.intersect(scene, to_dev(r), query=q))
+        ctx.set_traversal(0)
+        assert np.array_equal(got, want), q
     assert ctx.device_errors() == 0
 
 
