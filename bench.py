@@ -6,21 +6,29 @@ uniform in its bounding box, directions uniform on the sphere), closest hit,
 full RRHit output.  A step is one rrCmdIntersect over all rays.
 
 Reported (one JSON line on rank 0):
-  value        chosen path (8-wide quantised nodes, persistent kernel) Mrays/s,
-               rays and BVH resident in HBM, CUDA events on the launch stream
+  value        chosen path Mrays/s (the kernel rrCudaAutotuneTraversal picks
+               for this workload: plain, persistent binary or 8-wide), rays
+               and BVH resident in HBM, CUDA events on the launch stream
   plain        the plain binary-node kernel on the same rays (reference order)
   latency_ms   p50 / p99 of the per-step (per-batch) latency of the chosen path
   e2e          the same metric through the C-ABI with pinned host buffers:
                H2D of the rays, trace, D2H of the hits inside the timed region
   roofline     algorithmic bytes of the chosen kernel per launch (ray + hit +
-               80 B per wide node fetch + 48 B per triangle fetch, counted by
+               node bytes x node fetches + 48 B x triangle fetches, counted by
                the kernel's own counters) / mean launch time, against the
                measured HBM copy bandwidth
   build        LBVH + wide collapse of the mesh through rrCmdBuildGeometry
+  hit_id_identity  chosen vs plain on every ray
+  fp64_t_error t / uv error of the chosen hits against an fp64 evaluation of
+               the same ray-triangle pairs on the first 1,048,576 rays
   cpu_baseline the oracle's C++ restatement of the reference traversal on the
                host cores, on a bounded sample of the same rays
 With --gpus N under torchrun every rank traces its own 16,777,216 rays against
 its own replica of the BVH (replicas only: the path has no exchange step).
+
+Other workloads (not the headline line): --workload blas2048 (fused build of
+2,048 BLASes + two-level traversal) and --workload serving (resident scenes,
+continuous batching, p50/p99 request latency).
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port of isect.comp; the reference's own bvh_analyzer cannot be built
@@ -29,6 +37,7 @@ on the GPU host) on the host cores, on a bounded sample of each step.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -61,6 +70,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-chunk", type=int, default=0, help="rays per pipelined chunk of the e2e run (0: 2^21)")
     ap.add_argument("--only", default="", help="profiling aid: 'chosen' or 'plain' runs only that kernel")
     ap.add_argument("--block", type=int, default=0, help="chosen kernel threads per block (0: library default)")
     ap.add_argument("--per-sm", type=int, default=0, help="chosen kernel resident blocks per SM (0: occupancy)")
@@ -354,19 +364,28 @@ def run_ours(args):
     # ---- end to end through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and not args.only:
-        ctx.set_traversal(rr.RR_CUDA_TRAVERSAL_AUTO)
+        # The chosen kernel, through the host-buffer entry point: H2D of the
+        # rays, the traversal and D2H of the hits, in chunks pipelined over
+        # three streams, all inside the timed region.
+        ctx.set_traversal(chosen_trav, args.block, args.per_sm, ray_order=chosen_order)
         rays_h = torch.from_numpy(rays).pin_memory()
         hits_h = torch.empty((R, 4), dtype=torch.int32).pin_memory()
+        rh, hh = C.c_void_p(rays_h.data_ptr()), C.c_void_p(hits_h.data_ptr())
 
         def e2e_step():
-            rays_d.copy_(rays_h, non_blocking=True)
-            trace_step()
-            hits_h.copy_(hits_d, non_blocking=True)
+            rr.check(L.rrCudaCmdIntersectHostBuffers(ctx.ctx, hb, rr.RR_INTERSECT_QUERY_CLOSEST, rh, R,
+                                                     rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hh, rb, hitb, sb,
+                                                     args.e2e_chunk, ext), "rrCudaCmdIntersectHostBuffers")
         per_e, total_e = time_steps(e2e_step, args.steps, args.warmup, ws, stream)
         total_e = max_over_ranks(total_e, ws)
         e2e = {"value": R * ws * args.steps / (total_e / 1e3) / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": int(rays_h.numel() * 4), "d2h_bytes_per_step": int(hits_h.numel() * 4),
-               "ms_per_step": total_e / args.steps}
+               "ms_per_step": total_e / args.steps,
+               "api": "rrCudaCmdIntersectHostBuffers (pinned host rays/hits, chunks of "
+                      f"{args.e2e_chunk or 2 ** 21:,} rays over 3 streams)"}
+        e2e_hits = hits_h.numpy().view(np.uint32)
+        e2e["hits_identical_to_device_run"] = bool(np.array_equal(e2e_hits, out["chosen"]["hits"])) \
+            if "chosen" in out else None
 
     if rank != 0:
         ctx.close()

@@ -44,8 +44,9 @@ typedef struct
 /* ---- traversal kernel selection ---------------------------------------- */
 typedef enum
 {
-    /* Geometry: the wide kernel when the buffer holds wide nodes, else the
-     * binary kernel.  Scene: the persistent binary two-level kernel. */
+    /* The persistent binary kernel (single- or two-level); its hits are
+     * bit-identical to RR_CUDA_TRAVERSAL_BINARY.  rrCudaAutotuneTraversal
+     * replaces it with the fastest kernel for a workload. */
     RR_CUDA_TRAVERSAL_AUTO = 0,
     /* One thread per ray, 64-byte binary nodes, reference visit order. */
     RR_CUDA_TRAVERSAL_BINARY = 1,
@@ -170,6 +171,32 @@ RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
                                         const RRDevicePtr*          temporary_buffers,
                                         const RRDevicePtr*          geometry_buffers,
                                         RRCommandStream             command_stream);
+
+/* Intersect rays that live in host memory (no counterpart in the reference
+ * API, whose rrCmdIntersect takes device buffers, radeonrays.h:391-400).
+ * The rays are cut into chunks of `chunk_rays` (0 = 2^21), and each chunk is
+ * copied in, traced and its hits copied out on one of three CUDA streams
+ * owned by the context.  The copies of one chunk overlap the traversal of the
+ * others, so the host transfers hide behind the kernels.
+ *   host_rays   RRRay[ray_count] in host memory (page-locked for overlap)
+ *   host_hits   RRHit[ray_count] (or uint32_t for INSTANCE_ID) in host memory
+ *   rays, hits  device buffers of ray_count records (staging)
+ *   scratch     rrGetTraceMemoryRequirements(ray_count) bytes
+ * The traversal kernel is the context's (rrCudaSetTraversalOptions); the hits
+ * are those of rrCmdIntersect on the same rays.  The work joins back into the
+ * command stream's CUDA stream, so an event after it covers the copies. */
+RR_API RRError rrCudaCmdIntersectHostBuffers(RRContext              context,
+                                             RRDevicePtr            scene_buffer,
+                                             RRIntersectQuery       query,
+                                             const void*            host_rays,
+                                             uint32_t               ray_count,
+                                             RRIntersectQueryOutput query_output,
+                                             void*                  host_hits,
+                                             RRDevicePtr            rays,
+                                             RRDevicePtr            hits,
+                                             RRDevicePtr            scratch,
+                                             uint32_t               chunk_rays,
+                                             RRCommandStream        command_stream);
 
 /* ---- many intersection requests in one launch ---------------------------
  * No counterpart in the reference API (one rrCmdIntersect dispatches one

@@ -183,6 +183,22 @@ struct Context
     // capture are kept until the context goes.
     std::deque<std::pair<cudaEvent_t, Op>> retired;
     std::vector<Op>                        kept;
+    // Side streams and fork/join events of host-buffer tracing (copy/compute
+    // pipelining), created on first use.
+    static constexpr int kPipe = 3;
+    cudaStream_t         pipe[kPipe]      = {};
+    cudaEvent_t          pipe_fork        = nullptr;
+    cudaEvent_t          pipe_join[kPipe] = {};
+    void ensure_pipe()
+    {
+        if (pipe_fork) return;
+        for (int p = 0; p < kPipe; ++p)
+        {
+            check(cudaStreamCreateWithFlags(&pipe[p], cudaStreamNonBlocking), "pipeline stream");
+            check(cudaEventCreateWithFlags(&pipe_join[p], cudaEventDisableTiming), "pipeline event");
+        }
+        check(cudaEventCreateWithFlags(&pipe_fork, cudaEventDisableTiming), "pipeline event");
+    }
     void retire(Op&& op, cudaStream_t s)
     {
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -219,6 +235,13 @@ struct Context
         }
         retired.clear();
         kept.clear();
+        for (int p = 0; p < kPipe; ++p)
+        {
+            if (pipe[p]) cudaStreamSynchronize(pipe[p]);
+            if (pipe[p]) cudaStreamDestroy(pipe[p]);
+            if (pipe_join[p]) cudaEventDestroy(pipe_join[p]);
+        }
+        if (pipe_fork) cudaEventDestroy(pipe_fork);
         if (words) cudaFree(words);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -556,8 +579,12 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     // from the root like the reference (vlk/intersector.cpp:290).
     a.empty             = (bi.kind == kKindGeom && bi.n == 0);
     const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
-    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT) return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
-    if (has_wide && trav != RR_CUDA_TRAVERSAL_BINARY)
+    // AUTO: the persistent binary kernel (the fastest on incoherent rays,
+    // bit-identical to BINARY); rrCudaAutotuneTraversal refines the choice
+    // per workload.
+    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || trav == RR_CUDA_TRAVERSAL_AUTO)
+        return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
+    if (has_wide && trav == RR_CUDA_TRAVERSAL_WIDE)
     {
         a.wide_nodes = reinterpret_cast<const WideNode*>(bvh + bi.wide_off);
         a.wide_tris  = reinterpret_cast<const WideTri*>(bvh + bi.tris_off);
@@ -842,6 +869,94 @@ RR_API RRError rrCmdIntersect(RRContext              context,
             indirect_ray_count ? reinterpret_cast<const uint32_t*>(P(indirect_ray_count)->addr()) : nullptr;
         record(S(command_stream), trace_op(ctx, P(scene_buffer)->addr(), P(rays)->addr(), ray_count, ind,
                                            P(hits)->addr(), P(scratch)->addr(), query, query_output, ctx->topts));
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCudaCmdIntersectHostBuffers(RRContext              context,
+                                             RRDevicePtr            scene_buffer,
+                                             RRIntersectQuery       query,
+                                             const void*            host_rays,
+                                             uint32_t               ray_count,
+                                             RRIntersectQueryOutput query_output,
+                                             void*                  host_hits,
+                                             RRDevicePtr            rays,
+                                             RRDevicePtr            hits,
+                                             RRDevicePtr            scratch,
+                                             uint32_t               chunk_rays,
+                                             RRCommandStream        command_stream)
+{
+    RR_LOG_INFO("rrCudaCmdIntersectHostBuffers");
+    if (!context || !scene_buffer || !host_rays || !host_hits || !rays || !hits || !scratch || !command_stream ||
+        !ray_count)
+        return RR_ERROR_INVALID_PARAMETER;
+    if (query != RR_INTERSECT_QUERY_CLOSEST && query != RR_INTERSECT_QUERY_ANY) return RR_ERROR_INVALID_PARAMETER;
+    if (query_output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && query_output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+        return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        ctx->ensure_pipe();
+        // Chunks go round-robin to the side streams; each stream owns an equal
+        // share of the scratch (rrGetTraceMemoryRequirements(ray_count) bytes).
+        const size_t   total = trace_scratch_bytes(ray_count);
+        const int      np    = ray_count >= 3u * 8192u ? Context::kPipe : 1;
+        const size_t   region = np == 1 ? total : total / np / kAlign * kAlign;
+        const uint64_t fit    = np == 1 ? ray_count : (region - 256) / 256;
+        uint64_t       chunk  = chunk_rays ? chunk_rays : (1u << 21);
+        if (chunk > fit) chunk = fit;
+        if (chunk > ray_count) chunk = ray_count;
+        const size_t hs = query_output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? 16 : 4;
+        std::vector<Op> chunks;
+        std::vector<int> lane;
+        uint8_t*        bvh = P(scene_buffer)->addr();
+        uint8_t*        dr  = P(rays)->addr();
+        uint8_t*        dh  = P(hits)->addr();
+        uint8_t*        sc  = P(scratch)->addr();
+        int             k   = 0;
+        for (uint64_t off = 0; off < ray_count; off += chunk, ++k)
+        {
+            const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, ray_count - off);
+            const int      p = k % np;
+            Op             tr = trace_op(ctx, bvh, dr + 32 * off, n, nullptr, dh + hs * off, sc + (size_t)p * region, query,
+                                         query_output, ctx->topts);
+            const uint8_t* hr = reinterpret_cast<const uint8_t*>(host_rays) + 32 * off;
+            uint8_t*       hh = reinterpret_cast<uint8_t*>(host_hits) + hs * off;
+            uint8_t*       r  = dr + 32 * off;
+            uint8_t*       h  = dh + hs * off;
+            chunks.push_back([=](cudaStream_t st) -> cudaError_t {
+                cudaError_t e = cudaMemcpyAsync(r, hr, 32ull * n, cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) e = tr(st);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(hh, h, hs * n, cudaMemcpyDeviceToHost, st);
+                return e;
+            });
+            lane.push_back(p);
+        }
+        cudaStream_t side[Context::kPipe];
+        cudaEvent_t  join[Context::kPipe];
+        for (int p = 0; p < Context::kPipe; ++p)
+        {
+            side[p] = ctx->pipe[p];
+            join[p] = ctx->pipe_join[p];
+        }
+        cudaEvent_t fork = ctx->pipe_fork;
+        record(S(command_stream), [=](cudaStream_t s) -> cudaError_t {
+            cudaError_t e = cudaSuccess;
+            if (np == 1)
+            {
+                for (size_t i = 0; i < chunks.size() && e == cudaSuccess; ++i) e = chunks[i](s);
+                return e;
+            }
+            e = cudaEventRecord(fork, s);
+            for (int p = 0; p < np && e == cudaSuccess; ++p) e = cudaStreamWaitEvent(side[p], fork, 0);
+            for (size_t i = 0; i < chunks.size() && e == cudaSuccess; ++i) e = chunks[i](side[lane[i]]);
+            for (int p = 0; p < np && e == cudaSuccess; ++p)
+            {
+                e = cudaEventRecord(join[p], side[p]);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join[p], 0);
+            }
+            return e;
+        });
         return RR_SUCCESS;
     })
 }

@@ -164,6 +164,7 @@ PROTOTYPES = {
     "rrCudaCmdBuildGeometries": [_P, C.c_uint32, C.POINTER(RRGeometryBuildInput), C.POINTER(RRBuildOptions), _PP,
                                  _PP, _P],
     "rrCudaGetIntersectBatchMemoryRequirements": [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_size_t)],
+    "rrCudaCmdIntersectHostBuffers": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P, _P, _P, C.c_uint32, _P],
     "rrCudaCmdIntersectBatch": [_P, C.c_uint32, C.POINTER(RRCudaIntersectRequest), _P, _P],
 }
 
@@ -399,6 +400,29 @@ class Context:
         self.submit(cs)
         self.release_stream(cs)
         return hits
+
+    def intersect_host(self, bvh, rays_host, query=RR_INTERSECT_QUERY_CLOSEST, output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT,
+                       chunk_rays=0, staging=None):
+        """rays_host: CPU float32 tensor (R, 8), pinned for copy/compute overlap.  Returns the hits as a CPU
+        int32 tensor ((R, 4) or (R,)) through one rrCudaCmdIntersectHostBuffers call.  `staging` may pass
+        (rays_dev, hits_dev, scratch) to reuse device buffers."""
+        torch = _torch()
+        R = rays_host.shape[0]
+        full = output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT
+        hits_host = torch.full((R, 4) if full else (R,), -1, dtype=torch.int32).pin_memory()
+        if staging is None:
+            staging = (torch.empty((R, 8), dtype=torch.float32, device="cuda"),
+                       torch.full((R, 4) if full else (R,), -1, dtype=torch.int32, device="cuda"),
+                       torch.empty(self.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda"))
+        rd, hd, sc = staging
+        cs = self.command_stream()
+        check(self.L.rrCudaCmdIntersectHostBuffers(self.ctx, self.ptr(bvh), query, C.c_void_p(rays_host.data_ptr()), R,
+                                                   output, C.c_void_p(hits_host.data_ptr()), self.ptr(rd),
+                                                   self.ptr(hd), self.ptr(sc), chunk_rays, cs),
+              "rrCudaCmdIntersectHostBuffers")
+        self.submit(cs)
+        self.release_stream(cs)
+        return hits_host
 
     # -- many requests in one launch
     def batch_scratch_bytes(self, request_count: int, total_rays: int) -> int:
