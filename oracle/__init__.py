@@ -93,6 +93,18 @@ def sort(codes):
     return sc, si
 
 
+def fit(nodes, vertices, indices):
+    """Refit of an existing tree with new vertex positions (the update path,
+    lbvh_fit_aabb_mesh.comp with UPDATE_KERNEL): every leaf takes the vertices
+    of its primitive (child1), then boxes are rebuilt bottom-up.  Returns a copy."""
+    v, i, stride, i16 = _mesh(vertices, indices)
+    n = i.size // 3
+    out = np.array(nodes, dtype=NODE_DTYPE, copy=True)
+    if n:
+        lib().rro_fit(_p(v), C.c_uint32(stride), _p(i), C.c_int(i16), C.c_uint32(n), _p(out))
+    return out
+
+
 def build_mesh(vertices, indices, bits=30, threads=8):
     """Full LBVH build.  Returns (nodes, sorted_idx, sorted_codes)."""
     v, i, stride, i16 = _mesh(vertices, indices)

@@ -676,10 +676,46 @@ RR_API RRError rrGetGeometryBuildMemoryRequirements(RRContext                   
         GeomLayout L                                      = geom_layout(m->triangle_count, bp.format, bp.bits);
         memory_requirements->result_buffer_size           = L.total;
         memory_requirements->temporary_build_buffer_size  = L.s_total;
-        memory_requirements->temporary_update_buffer_size = 0;
+        memory_requirements->temporary_update_buffer_size = L.u_total;
         return RR_SUCCESS;
     })
 }
+
+namespace
+{
+// RR_BUILD_OPERATION_UPDATE (reference vlk/intersector.cpp:178-201,
+// vlk/update_hlbvh.cpp:140-180): the buffer must hold a build of a mesh with
+// the same triangle count on this context; its node format and key width are
+// kept.  The binary format needs no scratch; WIDE8 needs u_total bytes.
+RRError record_update(Context* ctx, const RRGeometryBuildInput* in, RRDevicePtr temporary_buffer,
+                      RRDevicePtr geometry_buffer, CommandStream* cs)
+{
+    const RRTriangleMeshPrimitive* m = nullptr;
+    RRError                        e = check_mesh_input(in, &m, true);
+    if (e != RR_SUCCESS) return e;
+    if (!geometry_buffer) return RR_ERROR_INVALID_PARAMETER;
+    uint8_t* result = P(geometry_buffer)->addr();
+    auto     it     = ctx->registry.find((uintptr_t)result);
+    if (it == ctx->registry.end() || it->second.kind != kKindGeom || it->second.n != m->triangle_count)
+        return RR_ERROR_INVALID_PARAMETER;
+    uint32_t bits = 30;
+    // The key width is not needed by an update (no Morton codes); the layout
+    // only depends on it for scratch offsets that an update does not use.
+    const GeomLayout L = geom_layout(m->triangle_count, it->second.format, bits);
+    if (L.u_total > 0 && !temporary_buffer) return RR_ERROR_INVALID_PARAMETER;
+    MeshArgs ma;
+    ma.vertices          = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
+    ma.stride_floats     = m->vertex_stride >> 2;
+    ma.indices           = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
+    ma.index16           = m->index_type == RR_INDEX_TYPE_UINT16;
+    ma.n                 = m->triangle_count;
+    uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
+    DeviceWords* words   = ctx->words;
+    const int    sms     = ctx->sm_count;
+    record(cs, [=](cudaStream_t s) { return launch_update_mesh(ma, L, scratch, result, words, sms, s); });
+    return RR_SUCCESS;
+}
+}  // namespace
 
 RR_API RRError rrCmdBuildGeometry(RRContext                   context,
                                   RRBuildOperation            build_operation,
@@ -692,7 +728,12 @@ RR_API RRError rrCmdBuildGeometry(RRContext                   context,
     RR_LOG_INFO("rrCmdBuildGeometry");
     if (!context || !command_stream || !build_input) return RR_ERROR_INVALID_PARAMETER;
     RR_TRY({
-        if (build_operation == RR_BUILD_OPERATION_UPDATE) return RR_ERROR_NOT_IMPLEMENTED;
+        if (build_operation == RR_BUILD_OPERATION_UPDATE)
+        {
+            Context*    ctx = C(context);
+            DeviceGuard g(ctx->device);
+            return record_update(ctx, build_input, temporary_buffer, geometry_buffer, S(command_stream));
+        }
         if (build_operation != RR_BUILD_OPERATION_BUILD) return RR_ERROR_INVALID_PARAMETER;
         BuildParams bp;
         if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;

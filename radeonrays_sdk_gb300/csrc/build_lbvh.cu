@@ -373,22 +373,14 @@ __global__ void __launch_bounds__(kBlk) k_batch_emit(BatchArgs b)
     emit_node<kBits>(it.scratch + it.s_codes, it.n, (uint32_t)i64, reinterpret_cast<BvhNode*>(it.result));
 }
 
-template <int kBits>
-__global__ void __launch_bounds__(kBlk) k_batch_refit(BatchArgs b, DeviceWords* words)
+// Leaf k of a geometry takes triangle `prim`'s vertices, then climbs: the
+// second child to arrive at a node (atomic flag) writes the node's two child
+// boxes and goes on to its parent (lbvh_fit_aabb_mesh.comp:94-205).
+__device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, uint32_t n, uint32_t k, uint32_t prim,
+                                         DeviceWords* words)
 {
-    using Cfg            = KeyCfg<kBits>;
-    const uint32_t   t   = blockIdx.x / Cfg::kChunks;
-    const TileRef    r   = tile_ref(b, t);
-    const BuildItem& it  = b.items[r.g];
-    const uint64_t   k64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
-    const uint32_t   n   = it.n;
-    if (k64 >= n) return;
-    const uint32_t  k          = (uint32_t)k64;
-    BvhNode*        nodes      = reinterpret_cast<BvhNode*>(it.result);
-    const uint32_t* sorted_idx = reinterpret_cast<const uint32_t*>(it.scratch + it.s_idx);
-    const uint32_t  leaf       = n - 1 + k;
-    const uint32_t  prim       = sorted_idx[k];
-    F3              a, bb, c;
+    const uint32_t leaf = n - 1 + k;
+    F3             a, bb, c;
     tri_verts(it, prim, a, bb, c);
     uint32_t parent = (n == 1) ? kInvalid : __ldcg(&nodes[leaf].parent);
     float4*  dst    = reinterpret_cast<float4*>(nodes + leaf);
@@ -436,6 +428,42 @@ __global__ void __launch_bounds__(kBlk) k_batch_refit(BatchArgs b, DeviceWords* 
     }
 }
 
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_refit(BatchArgs b, DeviceWords* words)
+{
+    using Cfg            = KeyCfg<kBits>;
+    const uint32_t   t   = blockIdx.x / Cfg::kChunks;
+    const TileRef    r   = tile_ref(b, t);
+    const BuildItem& it  = b.items[r.g];
+    const uint64_t   k64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
+    const uint32_t   n   = it.n;
+    if (k64 >= n) return;
+    const uint32_t  k          = (uint32_t)k64;
+    BvhNode*        nodes      = reinterpret_cast<BvhNode*>(it.result);
+    const uint32_t* sorted_idx = reinterpret_cast<const uint32_t*>(it.scratch + it.s_idx);
+    fit_leaf(it, nodes, n, k, sorted_idx[k], words);
+}
+
+// RR_BUILD_OPERATION_UPDATE (lbvh_reset_update_flags.comp:58-80): every
+// node's flag back to 0.  The reference dispatches this with one group only
+// (vlk/update_hlbvh.cpp:150) and so leaves most flags at 1; here every node
+// is reset.
+__global__ void __launch_bounds__(kBlk) k_update_reset(BvhNode* nodes, uint32_t count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) nodes[i].update = 0;
+}
+
+// lbvh_fit_aabb_mesh.comp:129-205 with UPDATE_KERNEL: the leaf keeps its
+// primitive (child1) and takes the new vertices, then the usual climb.
+__global__ void __launch_bounds__(kBlk) k_update_fit(BuildItem it, DeviceWords* words)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= it.n) return;
+    BvhNode* nodes = reinterpret_cast<BvhNode*>(it.result);
+    fit_leaf(it, nodes, it.n, k, __ldcg(&nodes[it.n - 1 + k].child1), words);
+}
+
 __global__ void k_put_single(BuildItem* items, BuildItem it, uint32_t* tile_prefix, uint32_t tiles)
 {
     if (threadIdx.x == 0)
@@ -449,7 +477,6 @@ __global__ void k_put_single(BuildItem* items, BuildItem it, uint32_t* tile_pref
 __global__ void k_init_trailer(Trailer* t, Trailer v) { *t = v; }
 
 inline int grid_for(uint64_t n, int block) { return (int)std::max<uint64_t>(1, (n + block - 1) / block); }
-
 template <int kBits>
 cudaError_t run_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s)
 {
@@ -523,6 +550,9 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
     L.s_queue       = align_up(L.s_sort + L.s_sort_bytes, kAlign);
     L.s_queue_bytes = (format == RR_CUDA_NODE_FORMAT_WIDE8 && n > 0) ? 2 * kAlign + 2ull * 8ull * n : 0;
     L.s_total       = align_up(L.s_queue + L.s_queue_bytes, kAlign);
+    // An update re-collapses the wide nodes: descriptor of one + queues.
+    L.u_queue = align_up(batch_desc_bytes(1), kAlign);
+    L.u_total = L.s_queue_bytes ? align_up(L.u_queue + L.s_queue_bytes, kAlign) : 0;
     return L;
 }
 
@@ -570,6 +600,35 @@ cudaError_t launch_build_batch(const BatchArgs& b, DeviceWords* words, int sm_co
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || b.total_tiles == 0) return e;
     return b.morton_bits == 63 ? run_batch<63>(b, words, sm_count, s) : run_batch<30>(b, words, sm_count, s);
+}
+
+cudaError_t launch_update_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
+                               DeviceWords* words, int sm_count, cudaStream_t s)
+{
+    if (L.n == 0) return cudaSuccess;
+    BuildItem it = make_build_item(L, m.vertices, m.stride_floats, m.indices, m.index16, scratch, result);
+    it.s_queue   = L.u_queue;
+    k_update_reset<<<grid_for(2ull * L.n - 1, kBlk), kBlk, 0, s>>>(reinterpret_cast<BvhNode*>(result), 2 * L.n - 1);
+    k_update_fit<<<grid_for(L.n, kBlk), kBlk, 0, s>>>(it, words);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || L.format != RR_CUDA_NODE_FORMAT_WIDE8) return e;
+    BuildItem* items = nullptr;
+    uint32_t * tp = nullptr, *lp = nullptr;
+    BatchCtl*  ctl = nullptr;
+    batch_carve(scratch, 1, &items, &tp, &lp, &ctl);
+    k_put_single<<<1, 32, 0, s>>>(items, it, tp, L.sort_tiles);
+    BatchArgs b{};
+    b.items        = items;
+    b.tile_prefix  = tp;
+    b.level_prefix = lp;
+    b.ctl          = ctl;
+    b.count        = 1;
+    b.total_tiles  = L.sort_tiles;
+    b.total_prims  = L.n;
+    b.max_n        = L.n;
+    b.format       = L.format;
+    b.morton_bits  = L.morton_bits;
+    return launch_collapse_batch(b, words, sm_count, s);
 }
 
 cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,

@@ -118,6 +118,8 @@ struct GeomLayout
     // scratch
     size_t   s_desc, s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_queue, s_queue_bytes,
         s_total;
+    // update scratch (RR_BUILD_OPERATION_UPDATE): descriptor | collapse queues
+    size_t   u_queue, u_total;
     uint32_t sort_tiles, sort_passes;
 };
 GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits);
@@ -227,6 +229,11 @@ struct MeshArgs
 
 cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
                               DeviceWords* words, int sm_count, cudaStream_t s);
+// RR_BUILD_OPERATION_UPDATE: new vertex positions, same topology.  Leaves take
+// their triangle's new vertices, boxes are refitted bottom-up and the 8-wide
+// nodes (if any) are collapsed again.  `scratch` holds L.u_total bytes.
+cudaError_t launch_update_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
+                               DeviceWords* words, int sm_count, cudaStream_t s);
 
 // Sort (codes, identity values) stably; bits = 30 (uint32 keys) or 63 (uint64).
 // Returns in *sorted_in_alt whether the result is in the alt buffers.

@@ -291,6 +291,31 @@ class Context:
             self.release_stream(cs)
         return result
 
+    def update_geometry(self, vertices, indices, result, stream=None, scratch=None):
+        """RR_BUILD_OPERATION_UPDATE of `result` (built on this context from a mesh with the same triangle
+        count) with new vertex positions: leaves take the new vertices, boxes are refitted, wide nodes are
+        collapsed again."""
+        torch = _torch()
+        ntri = indices.numel() // 3
+        nvert = vertices.numel() // 3
+        bi, mesh = self._build_input(self.ptr(vertices) if ntri else None, nvert, 12,
+                                     self.ptr(indices) if ntri else None, ntri, indices.dtype == torch.int16)
+        req = RRMemoryRequirements()
+        opts, keep = self._options()
+        check(self.L.rrGetGeometryBuildMemoryRequirements(self.ctx, C.byref(bi), C.byref(opts), C.byref(req)),
+              "rrGetGeometryBuildMemoryRequirements")
+        if scratch is None and req.temporary_update_buffer_size:
+            scratch = torch.empty(req.temporary_update_buffer_size, dtype=torch.uint8, device=vertices.device)
+        own = stream is None
+        cs = self.command_stream() if own else stream
+        check(self.L.rrCmdBuildGeometry(self.ctx, RR_BUILD_OPERATION_UPDATE, C.byref(bi), C.byref(opts),
+                                        self.ptr(scratch) if scratch is not None else None, self.ptr(result), cs),
+              "rrCmdBuildGeometry(update)")
+        if own:
+            self.submit(cs)
+            self.release_stream(cs)
+        return result
+
     def build_geometries(self, meshes, node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30, stream=None,
                          api="batch"):
         """Build many meshes [(vertices (V, 3) float32, indices (T, 3) int32), ...] (cuda tensors).

@@ -77,7 +77,9 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     nodes = (2 * 1000 - 1) * 64
     assert req_b.result_buffer_size == (nodes + 255) // 256 * 256 + 256
     assert req.result_buffer_size > req_b.result_buffer_size  # wide nodes + triangles appended
-    assert req.temporary_update_buffer_size == 0
+    # An update needs scratch only to collapse the wide nodes again.
+    assert req_b.temporary_update_buffer_size == 0
+    assert 0 < req.temporary_update_buffer_size < req.temporary_build_buffer_size
     # Unsupported primitive type / bad input.
     bi2 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1, C.pointer(mesh))
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi2), None, C.byref(req)) == \

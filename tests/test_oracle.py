@@ -185,3 +185,26 @@ def test_oracle_fp64_t_error_small(orc):
     e = orc.fp64_hit(g["rays"], tri9, hit.astype(np.uint32))
     rel = np.abs(t32[hit].astype(np.float64) - e[hit, 0]) / np.spacing(np.abs(t32[hit]))
     assert rel.max() < 64  # ulps; typical 0-2
+
+
+def test_oracle_fit_is_the_build_refit(orc):
+    """The update restatement (leaves take their primitive's vertices, then a
+    bottom-up refit) reproduces the built tree from the same vertices, and
+    every box still contains its subtree after moving the vertices."""
+    from radeonrays_sdk_gb300 import scenes
+    v, i = scenes.soup(3000, scenes.rng(80))
+    nodes, _, _ = orc.build_mesh(v, i)
+    again = orc.fit(nodes, v, i)
+    assert np.array_equal(again.view(np.uint32).reshape(-1, 16)[:, :12],
+                          nodes.view(np.uint32).reshape(-1, 16)[:, :12])
+    v2 = (v * np.float32(2.0) + np.float32(0.25)).astype(np.float32)
+    moved = orc.fit(nodes, v2, i)
+    assert np.array_equal(moved["child0"], nodes["child0"]) and np.array_equal(moved["child1"], nodes["child1"])
+    n = i.shape[0]
+    lo = np.minimum(np.minimum(moved["a0"], moved["a1"]), moved["b0"])[n - 1:]
+    hi = np.maximum(np.maximum(moved["a0"], moved["a1"]), moved["b0"])[n - 1:]
+    # The root's two child boxes together contain every moved leaf.
+    root = moved[0]
+    rlo = np.minimum(root["a0"], root["b0"])
+    rhi = np.maximum(root["a1"], root["b1"])
+    assert np.all(lo >= rlo) and np.all(hi <= rhi)
