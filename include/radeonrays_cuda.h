@@ -149,6 +149,17 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext               context,
                                        RRDevicePtr             scratch,
                                        RRCudaTraversalOptions* chosen);
 
+/* Make a geometry result buffer that was not built on this context -- read
+ * back from a file, copied from another process or context -- known to it, so
+ * that rrCmdIntersect, rrCmdBuildScene and updates treat it like one built
+ * here (no counterpart in the reference, whose buffers never leave their
+ * context).  Reads the buffer's 256-byte trailer with a blocking copy and
+ * checks magic, kind and counts against `triangle_count`; a mismatch returns
+ * RR_ERROR_INVALID_PARAMETER.  Geometry buffers are position-independent
+ * (indices, not pointers), so their bytes can be stored and loaded as they
+ * are; scene buffers hold BLAS addresses and are rebuilt instead. */
+RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_buffer, uint32_t triangle_count);
+
 /* Build `count` geometries in one fused set of launches (no counterpart in
  * the reference API, which records one rrCmdBuildGeometry per geometry,
  * radeonrays.h:322-328).  Geometry i reads build_inputs[i] and uses

@@ -748,6 +748,33 @@ RR_API RRError rrCmdBuildGeometry(RRContext                   context,
     })
 }
 
+RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_buffer, uint32_t triangle_count)
+{
+    RR_LOG_INFO("rrCudaRegisterGeometry(%u)", triangle_count);
+    if (!context || !geometry_buffer || triangle_count >= (1u << 30)) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*       ctx    = C(context);
+        DeviceGuard    g(ctx->device);
+        uint8_t*       result = P(geometry_buffer)->addr();
+        const uint32_t n      = triangle_count;
+        const size_t   toff   = align_up(n == 0 ? 0 : (2ull * n - 1) * sizeof(BvhNode), kAlign);
+        Trailer        t{};
+        check(cudaMemcpy(&t, result + toff, sizeof(Trailer), cudaMemcpyDeviceToHost), "read trailer");
+        if (t.magic != kMagic || t.version != kVersion || t.kind != kKindGeom || t.leaf_count != n ||
+            t.node_count != (n == 0 ? 0u : 2u * n - 1u))
+            return RR_ERROR_INVALID_PARAMETER;
+        if (t.node_format != RR_CUDA_NODE_FORMAT_BINARY && t.node_format != RR_CUDA_NODE_FORMAT_WIDE8)
+            return RR_ERROR_INVALID_PARAMETER;
+        const GeomLayout L = geom_layout(n, t.node_format, t.morton_bits);
+        if (t.wide_nodes_off != L.wide_off || t.wide_tris_off != L.tris_off) return RR_ERROR_INVALID_PARAMETER;
+        PendingGeom pg{};
+        pg.L      = L;
+        pg.result = result;
+        register_geometry(ctx, pg);
+        return RR_SUCCESS;
+    })
+}
+
 RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
                                         uint32_t                    count,
                                         const RRGeometryBuildInput* build_inputs,

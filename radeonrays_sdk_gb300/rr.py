@@ -165,6 +165,7 @@ PROTOTYPES = {
                                  _PP, _P],
     "rrCudaGetIntersectBatchMemoryRequirements": [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_size_t)],
     "rrCudaCmdIntersectHostBuffers": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P, _P, _P, C.c_uint32, _P],
+    "rrCudaRegisterGeometry": [_P, _P, C.c_uint32],
     "rrCudaCmdIntersectBatch": [_P, C.c_uint32, C.POINTER(RRCudaIntersectRequest), _P, _P],
 }
 
