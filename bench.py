@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=0, help="rays per pipelined chunk of the e2e run (0: 2^21)")
+    ap.add_argument("--quality", type=int, default=1,
+                    help="1: the chosen path traces a quality build (treelet restructure); 0: the fast build")
     ap.add_argument("--only", default="", help="profiling aid: 'chosen' or 'plain' runs only that kernel")
     ap.add_argument("--block", type=int, default=0, help="chosen kernel threads per block (0: library default)")
     ap.add_argument("--per-sm", type=int, default=0, help="chosen kernel resident blocks per SM (0: occupancy)")
@@ -318,17 +320,31 @@ def run_ours(args):
         ctx.release_ptrs()
     b_per, b_total = time_steps(build_step, 5, 2, 1, stream)
     build = {"ms": statistics.median(b_per), "mtris_s": ntri / statistics.median(b_per) / 1e3,
-             "format": "binary + wide8", "triangles": ntri}
+             "format": "binary + wide8", "triangles": ntri, "flags": "PREFER_FAST_BUILD (reference LBVH)"}
+    # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
+    # LBVH + treelet restructure); the plain path the reference's fast LBVH.
+    bvh_c = bvh
+    if args.quality:
+        bvh_c = torch.empty(r_bytes, dtype=torch.uint8, device="cuda")
+
+        def qbuild_step():
+            ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_WIDE8, stream=ext, scratch=scratch_b,
+                               result=bvh_c, quality=True)
+            ctx.release_ptrs()
+        q_per, _ = time_steps(qbuild_step, 3, 1, 1, stream)
+        build["quality"] = {"ms": statistics.median(q_per), "mtris_s": ntri / statistics.median(q_per) / 1e3,
+                            "flags": "no PREFER_FAST_BUILD: LBVH + 3 treelet-restructure passes (nodes >= 64 tris)"}
 
     rays_d = torch.from_numpy(rays).cuda()
     hits_d = torch.empty((R, 4), dtype=torch.int32, device="cuda")
     scratch_t = torch.empty(ctx.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda")
-    hb, rb, hitb = ctx.ptr(bvh), ctx.ptr(rays_d), ctx.ptr(hits_d)
+    hb, hcb, rb, hitb = ctx.ptr(bvh), ctx.ptr(bvh_c), ctx.ptr(rays_d), ctx.ptr(hits_d)
     sb = ctx.ptr(scratch_t)
     L = ctx.L
+    cur = {"bvh": hcb}
 
     def trace_step():
-        rr.check(L.rrCmdIntersect(ctx.ctx, hb, rr.RR_INTERSECT_QUERY_CLOSEST, rb, R, None,
+        rr.check(L.rrCmdIntersect(ctx.ctx, cur["bvh"], rr.RR_INTERSECT_QUERY_CLOSEST, rb, R, None,
                                   rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hitb, sb, ext), "rrCmdIntersect")
 
     out = {}
@@ -336,7 +352,7 @@ def run_ours(args):
     # unless a kernel is forced on the command line.
     chosen_trav, chosen_order, tuned = args.chosen, args.ray_order, None
     if args.chosen == 0 and args.only != "plain":
-        tuned = ctx.autotune(bvh, rays_d, hits=hits_d, scratch=scratch_t)
+        tuned = ctx.autotune(bvh_c, rays_d, hits=hits_d, scratch=scratch_t)
         chosen_trav, chosen_order = tuned["traversal"], tuned["ray_order"]
     # Fetch counters of each kernel (untimed run) -> algorithmic bytes.
     for name, trav in (("chosen", chosen_trav), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
@@ -346,6 +362,7 @@ def run_ours(args):
             continue
         shape = (args.block, args.per_sm) if name == "chosen" else (0, 0)
         order = chosen_order if name == "chosen" else 0
+        cur["bvh"] = hcb if name == "chosen" else hb
         ctx.set_traversal(trav, *shape, collect_stats=1, ray_order=order)
         trace_step()
         torch.cuda.synchronize()
@@ -373,7 +390,7 @@ def run_ours(args):
         rh, hh = C.c_void_p(rays_h.data_ptr()), C.c_void_p(hits_h.data_ptr())
 
         def e2e_step():
-            rr.check(L.rrCudaCmdIntersectHostBuffers(ctx.ctx, hb, rr.RR_INTERSECT_QUERY_CLOSEST, rh, R,
+            rr.check(L.rrCudaCmdIntersectHostBuffers(ctx.ctx, hcb, rr.RR_INTERSECT_QUERY_CLOSEST, rh, R,
                                                      rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hh, rb, hitb, sb,
                                                      args.e2e_chunk, ext), "rrCudaCmdIntersectHostBuffers")
         per_e, total_e = time_steps(e2e_step, args.steps, args.warmup, ws, stream)
@@ -433,16 +450,21 @@ def run_ours(args):
         flags_equal = bool(np.array_equal(ch[:, 2] != 0xFFFFFFFF, ph[:, 2] != 0xFFFFFFFF))
         hit = ph[:, 2] != 0xFFFFFFFF
         diff = np.where(hit & (ch[:, 3] != ph[:, 3]))[0]
-        ties = None
+        ties, gap = None, None
         if diff.size and diff.size < 100000:
             import oracle
             idx = i.astype(np.int64)
             ta = oracle.tri_test(rays[diff], v[idx[ch[diff, 3]]].reshape(-1, 9))[:, 0]
             tb = oracle.tri_test(rays[diff], v[idx[ph[diff, 3]]].reshape(-1, 9))[:, 0]
             ties = bool(np.array_equal(ta, tb))
+            gap = float((np.abs(ta.astype(np.float64) - tb) / np.spacing(np.maximum(np.abs(ta), np.abs(tb)))).max())
         line["hit_id_identity"] = {"rays": int(R), "hit_flags_identical": flags_equal,
                                    "prim_id_identical_fraction": float(1.0 - diff.size / max(1, int(hit.sum()))),
-                                   "mismatches": int(diff.size), "mismatches_are_equal_t_ties": ties}
+                                   "mismatches": int(diff.size), "mismatches_are_equal_t_ties": ties,
+                                   "mismatch_t_gap_ulp_max": gap,
+                                   "note": "chosen traces the quality (restructured) tree, plain the fast LBVH; "
+                                           "a mismatch is two triangles hit at (nearly) the same t, decided by "
+                                           "visit order and the reference's fp32 slab test"}
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu:

@@ -105,6 +105,16 @@ def fit(nodes, vertices, indices):
     return out
 
 
+def restructure(nodes, n, min_prims=64, passes=3):
+    """Treelet restructure of a built tree (rro_restructure).  Returns
+    (new nodes, number of treelets changed)."""
+    out = np.array(nodes, dtype=NODE_DTYPE, copy=True)
+    f = lib().rro_restructure
+    f.restype = C.c_uint32
+    changed = f(_p(out), C.c_uint32(n), C.c_uint32(min_prims), C.c_int(passes)) if n >= 3 else 0
+    return out, int(changed)
+
+
 def build_mesh(vertices, indices, bits=30, threads=8):
     """Full LBVH build.  Returns (nodes, sorted_idx, sorted_codes)."""
     v, i, stride, i16 = _mesh(vertices, indices)

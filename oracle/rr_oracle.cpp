@@ -797,6 +797,176 @@ void rro_emit(const void* sorted_codes, int bits, const uint32_t* sorted_idx, ui
               sorted_idx, n, nodes, threads);
 }
 
+// Treelet restructure (the reference's optional quality pass,
+// restructure_hlbvh.cpp:133-278 + restructure_bvh.comp, after Karras & Aila
+// 2013), restated deterministically: in post-order, every internal node X
+// whose subtree holds at least `min_prims` triangles roots a treelet of up to
+// 7 subtrees (grown by splitting the treelet leaf with the largest surface
+// area, first on ties), the topology of its internal nodes is replaced by the
+// one minimising the sum of node half-areas (dynamic programming over the 127
+// subsets, first minimum in enumeration order), if strictly cheaper, and the
+// treelet's boxes are refitted.  Node slots are reused, so the layout (root 0,
+// internal [0, n-2], leaves [n-1, 2n-2]) is kept.
+} // extern "C"
+
+static inline float half_area(const Box& b)
+{
+    const F3 e = sub(b.hi, b.lo);
+    return (e.x * e.y + e.y * e.z) + e.z * e.x;
+}
+
+static inline Box box_union(const Box& a, const Box& b) { return Box{vmin(a.lo, b.lo), vmax(a.hi, b.hi)}; }
+
+static void set_child_boxes(rro_node* nodes, uint32_t x)
+{
+    rro_node& nd = nodes[x];
+    const Box l  = node_box(nodes[nd.child0]);
+    const Box r  = node_box(nodes[nd.child1]);
+    st3(nd.aabb0_min_or_v0, l.lo);
+    st3(nd.aabb0_max_or_v1, l.hi);
+    st3(nd.aabb1_min_or_v2, r.lo);
+    st3(nd.aabb1_max_or_v3, r.hi);
+}
+
+// Restructure the treelet rooted at internal node x; returns true if changed.
+static bool restructure_treelet(rro_node* nodes, uint32_t n, uint32_t x)
+{
+    uint32_t leaf[7], inner[6];
+    float    la[7];
+    int      nl = 2, ni = 1;
+    inner[0]    = x;
+    leaf[0]     = nodes[x].child0;
+    leaf[1]     = nodes[x].child1;
+    la[0]       = half_area(node_box(nodes[leaf[0]]));
+    la[1]       = half_area(node_box(nodes[leaf[1]]));
+    while (nl < 7)
+    {
+        int   best = -1;
+        float ba   = -1.f;
+        for (int k = 0; k < nl; ++k)
+            if (leaf[k] < n - 1 && la[k] > ba)
+            {
+                ba   = la[k];
+                best = k;
+            }
+        if (best < 0) break;
+        const uint32_t c = leaf[best];
+        inner[ni++]      = c;
+        leaf[best]       = nodes[c].child0;
+        la[best]         = half_area(node_box(nodes[leaf[best]]));
+        leaf[nl]         = nodes[c].child1;
+        la[nl]           = half_area(node_box(nodes[leaf[nl]]));
+        ++nl;
+    }
+    if (nl < 3) return false;
+    const uint32_t full = (1u << nl) - 1;
+    Box            bx[7];
+    for (int k = 0; k < nl; ++k) bx[k] = node_box(nodes[leaf[k]]);
+    float   area[128], cost[128];
+    uint8_t part[128];
+    for (uint32_t s = 1; s <= full; ++s)
+    {
+        const int lo = __builtin_ctz(s);
+        Box       u  = bx[lo];
+        for (int k = lo + 1; k < nl; ++k)
+            if (s >> k & 1u) u = box_union(u, bx[k]);
+        area[s] = half_area(u);
+        if ((s & (s - 1)) == 0)
+        {
+            cost[s] = area[s];
+            part[s] = 0;
+            continue;
+        }
+        // Proper subsets p of s holding s's lowest bit, in decreasing order.
+        const uint32_t low  = s & (0u - s);
+        float          best = 0.f;
+        uint32_t       bp   = 0;
+        for (uint32_t p = (s - 1) & s; p; p = (p - 1) & s)
+        {
+            if (!(p & low)) continue;
+            const float c = cost[p] + cost[s ^ p];
+            if (bp == 0 || c < best)
+            {
+                best = c;
+                bp   = p;
+            }
+        }
+        cost[s] = area[s] + best;
+        part[s] = (uint8_t)bp;
+    }
+    // Cost of the current topology: every treelet node's half-area.
+    float cur = area[full];
+    for (int k = 1; k < ni; ++k) cur += half_area(node_box(nodes[inner[k]]));
+    for (int k = 0; k < nl; ++k) cur += la[k];
+    if (!(cost[full] < cur)) return false;
+    // Rebuild top-down in preorder; internal slots are reused in inner[] order.
+    uint32_t sset[6], sslot[6];
+    int      sp = 0, next = 1;
+    sset[sp]    = full;
+    sslot[sp++] = x;
+    uint32_t order[6];
+    int      no = 0;
+    while (sp > 0)
+    {
+        --sp;
+        const uint32_t s = sset[sp], slot = sslot[sp];
+        order[no++]      = slot;
+        const uint32_t p = part[s], q = s ^ p;
+        uint32_t       ch[2];
+        const uint32_t sides[2] = {p, q};
+        for (int k = 0; k < 2; ++k)
+        {
+            const uint32_t t = sides[k];
+            if ((t & (t - 1)) == 0)
+                ch[k] = leaf[__builtin_ctz(t)];
+            else
+            {
+                ch[k]       = inner[next++];
+                sset[sp]    = t;
+                sslot[sp++] = ch[k];
+            }
+        }
+        nodes[slot].child0   = ch[0];
+        nodes[slot].child1   = ch[1];
+        nodes[ch[0]].parent = slot;
+        nodes[ch[1]].parent = slot;
+    }
+    for (int k = no - 1; k >= 0; --k) set_child_boxes(nodes, order[k]);
+    return true;
+}
+
+extern "C" {
+
+uint32_t rro_restructure(rro_node* nodes, uint32_t n, uint32_t min_prims, int passes)
+{
+    if (n < 3) return 0;
+    uint32_t              changed = 0;
+    std::vector<uint32_t> cnt(2 * (size_t)n - 1, 1u);
+    for (int pass = 0; pass < passes; ++pass)
+    {
+        // Post-order over internal nodes (children before parents).
+        std::vector<std::pair<uint32_t, int>> st;
+        st.push_back({0u, 0});
+        while (!st.empty())
+        {
+            auto& top = st.back();
+            const uint32_t x = top.first;
+            if (top.second == 0)
+            {
+                top.second = 1;
+                const uint32_t c0 = nodes[x].child0, c1 = nodes[x].child1;
+                if (c1 < n - 1) st.push_back({c1, 0});
+                if (c0 < n - 1) st.push_back({c0, 0});
+                continue;
+            }
+            st.pop_back();
+            cnt[x] = cnt[nodes[x].child0] + cnt[nodes[x].child1];
+            if (cnt[x] >= min_prims && restructure_treelet(nodes, n, x)) ++changed;
+        }
+    }
+    return changed;
+}
+
 // Leaf vertices + bottom-up boxes (lbvh_fit_aabb_mesh.comp:94-205).
 void rro_fit(const float* vertices, uint32_t vertex_stride, const void* indices, int index16, uint32_t n,
              rro_node* nodes)

@@ -45,6 +45,7 @@ void rro_sort32(const uint32_t* codes, uint32_t n, uint32_t* sorted_codes, uint3
 void rro_sort64(const uint64_t* codes, uint32_t n, uint64_t* sorted_codes, uint32_t* sorted_idx);
 void rro_emit(const void* sorted_codes, int bits, const uint32_t* sorted_idx, uint32_t n, rro_node* nodes,
               int threads);
+uint32_t rro_restructure(rro_node* nodes, uint32_t n, uint32_t min_prims, int passes);
 void rro_fit(const float* vertices, uint32_t vertex_stride, const void* indices, int index16, uint32_t n,
              rro_node* nodes);
 void rro_build_mesh(const float* vertices, uint32_t vertex_stride, const void* indices, int index16, uint32_t n,

@@ -330,6 +330,8 @@ Op build_batch_op(Context* ctx, const std::vector<PendingGeom>& geoms, bool* man
     b.max_n        = max_n;
     b.format       = geoms[0].L.format;
     b.morton_bits  = geoms[0].L.morton_bits;
+    b.restructure_min    = geoms[0].L.restructure_min;
+    b.restructure_passes = geoms[0].L.restructure_passes;
     *many_launches = true;
     return [=](cudaStream_t s) {
         (void)dev;  // keeps the descriptors alive as long as the op
@@ -364,13 +366,18 @@ void record(CommandStream* cs, Op op, bool owns = false)
 
 struct BuildParams
 {
-    uint32_t format = RR_CUDA_NODE_FORMAT_WIDE8;
-    uint32_t bits   = 30;
+    uint32_t format      = RR_CUDA_NODE_FORMAT_WIDE8;
+    uint32_t bits        = 30;
+    bool     restructure = false;
 };
 
-// RRBuildOptions::backend_specific_info -> node format and key width.
+// RRBuildOptions -> node format, key width and quality.  As in the reference
+// (vlk/intersector.cpp:115-119, 170-181), options whose build_flags lack
+// RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD ask for the treelet restructure; no
+// options at all is a fast build.
 bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
 {
+    if (o) bp.restructure = (o->build_flags & RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD) == 0;
     if (!o || !o->backend_specific_info) return true;
     const RRCudaBuildOptions* c = reinterpret_cast<const RRCudaBuildOptions*>(o->backend_specific_info);
     if (c->struct_size < sizeof(RRCudaBuildOptions)) return false;
@@ -408,6 +415,8 @@ RRError prepare_geometry(const RRGeometryBuildInput* in, const BuildParams& bp, 
     if (e != RR_SUCCESS) return e;
     if (!geometry_buffer || (!temporary_buffer && m->triangle_count > 0)) return RR_ERROR_INVALID_PARAMETER;
     pg->L                = geom_layout(m->triangle_count, bp.format, bp.bits);
+    pg->L.restructure_min    = bp.restructure ? kRestructureMinPrims : 0u;
+    pg->L.restructure_passes = bp.restructure ? kRestructurePasses : 0u;
     pg->ma.vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
     pg->ma.stride_floats = m->vertex_stride >> 2;
     pg->ma.indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
@@ -446,7 +455,8 @@ void record_build(CommandStream* cs, const PendingGeom& pg)
     if (!cs->pending.empty())
     {
         const PendingGeom& f = cs->pending.front();
-        fits = f.L.format == pg.L.format && f.L.morton_bits == pg.L.morton_bits && claim_build_ranges(cs->pending_ranges, pg);
+        fits = f.L.format == pg.L.format && f.L.morton_bits == pg.L.morton_bits &&
+               f.L.restructure_min == pg.L.restructure_min && claim_build_ranges(cs->pending_ranges, pg);
     }
     if (!fits)
     {

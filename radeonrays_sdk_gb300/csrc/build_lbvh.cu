@@ -373,6 +373,214 @@ __global__ void __launch_bounds__(kBlk) k_batch_emit(BatchArgs b)
     emit_node<kBits>(it.scratch + it.s_codes, it.n, (uint32_t)i64, reinterpret_cast<BvhNode*>(it.result));
 }
 
+// ---- treelet restructure (quality build) -----------------------------------
+// The reference's optional pass (restructure_hlbvh.cpp:133-278,
+// restructure_bvh.comp; Karras & Aila 2013) restated deterministically: in
+// post-order -- a bottom-up climb where the second child to arrive continues --
+// every internal node X with at least `min_prims` triangles below it roots a
+// treelet of up to 7 subtrees, grown by splitting the treelet leaf with the
+// largest surface area (first on ties).  The topology of the treelet's
+// internal nodes is replaced by the one that minimises the sum of node
+// half-areas (dynamic programming over its 127 subsets, first minimum in
+// enumeration order) when that is strictly cheaper, and the treelet's boxes
+// are refitted.  Each node depends only on its own, finished subtree, so the
+// result is independent of scheduling and equals the oracle's rro_restructure.
+// Node slots are reused: the layout (root 0, internal [0, n-2], leaves
+// [n-1, 2n-2]) and all other fields stay as built.
+struct Bx3
+{
+    F3 lo, hi;
+};
+__device__ __forceinline__ float half_area3(const Bx3& b)
+{
+    const F3 e = f3(b.hi.x - b.lo.x, b.hi.y - b.lo.y, b.hi.z - b.lo.z);
+    return (e.x * e.y + e.y * e.z) + e.z * e.x;
+}
+__device__ __forceinline__ Bx3 box_of(const BvhNode* nodes, uint32_t c)
+{
+    Bx3 b;
+    child_box(nodes, c, b.lo, b.hi);
+    return b;
+}
+__device__ __forceinline__ void store_child_boxes(BvhNode* nodes, uint32_t x)
+{
+    BvhNode*       nd = nodes + x;
+    const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
+    F3             lo0, hi0, lo1, hi1;
+    child_box(nodes, c0, lo0, hi0);
+    child_box(nodes, c1, lo1, hi1);
+    __stcg(&nd->a0[0], lo0.x);
+    __stcg(&nd->a0[1], lo0.y);
+    __stcg(&nd->a0[2], lo0.z);
+    __stcg(&nd->a1[0], hi0.x);
+    __stcg(&nd->a1[1], hi0.y);
+    __stcg(&nd->a1[2], hi0.z);
+    __stcg(&nd->b0[0], lo1.x);
+    __stcg(&nd->b0[1], lo1.y);
+    __stcg(&nd->b0[2], lo1.z);
+    __stcg(&nd->b1[0], hi1.x);
+    __stcg(&nd->b1[1], hi1.y);
+    __stcg(&nd->b1[2], hi1.z);
+}
+
+__device__ void restructure_treelet(BvhNode* nodes, uint32_t n, uint32_t x)
+{
+    uint32_t leaf[7], inner[6];
+    float    la[7];
+    int      nl = 2, ni = 1;
+    inner[0]    = x;
+    leaf[0]     = __ldcg(&nodes[x].child0);
+    leaf[1]     = __ldcg(&nodes[x].child1);
+    la[0]       = half_area3(box_of(nodes, leaf[0]));
+    la[1]       = half_area3(box_of(nodes, leaf[1]));
+    while (nl < 7)
+    {
+        int   best = -1;
+        float ba   = -1.f;
+        for (int k = 0; k < nl; ++k)
+            if (leaf[k] < n - 1 && la[k] > ba)
+            {
+                ba   = la[k];
+                best = k;
+            }
+        if (best < 0) break;
+        const uint32_t c = leaf[best];
+        inner[ni++]      = c;
+        leaf[best]       = __ldcg(&nodes[c].child0);
+        la[best]         = half_area3(box_of(nodes, leaf[best]));
+        leaf[nl]         = __ldcg(&nodes[c].child1);
+        la[nl]           = half_area3(box_of(nodes, leaf[nl]));
+        ++nl;
+    }
+    if (nl < 3) return;
+    const uint32_t full = (1u << nl) - 1;
+    Bx3            bx[7];
+    for (int k = 0; k < nl; ++k) bx[k] = box_of(nodes, leaf[k]);
+    float   area[128], cost[128];
+    uint8_t part[128];
+    for (uint32_t s = 1; s <= full; ++s)
+    {
+        const int lo = __ffs(s) - 1;
+        Bx3       u  = bx[lo];
+        for (int k = lo + 1; k < nl; ++k)
+            if (s >> k & 1u)
+            {
+                u.lo = vmin(u.lo, bx[k].lo);
+                u.hi = vmax(u.hi, bx[k].hi);
+            }
+        area[s] = half_area3(u);
+        if ((s & (s - 1)) == 0)
+        {
+            cost[s] = area[s];
+            part[s] = 0;
+            continue;
+        }
+        const uint32_t low  = s & (0u - s);
+        float          best = 0.f;
+        uint32_t       bp   = 0;
+        for (uint32_t p = (s - 1) & s; p; p = (p - 1) & s)
+        {
+            if (!(p & low)) continue;
+            const float c = cost[p] + cost[s ^ p];
+            if (bp == 0 || c < best)
+            {
+                best = c;
+                bp   = p;
+            }
+        }
+        cost[s] = area[s] + best;
+        part[s] = (uint8_t)bp;
+    }
+    float cur = area[full];
+    for (int k = 1; k < ni; ++k) cur += half_area3(box_of(nodes, inner[k]));
+    for (int k = 0; k < nl; ++k) cur += la[k];
+    if (!(cost[full] < cur)) return;
+    uint32_t sset[6], sslot[6], order[6];
+    int      sp = 0, next = 1, no = 0;
+    sset[sp]    = full;
+    sslot[sp++] = x;
+    while (sp > 0)
+    {
+        --sp;
+        const uint32_t s = sset[sp], slot = sslot[sp];
+        order[no++]      = slot;
+        const uint32_t sides[2] = {part[s], s ^ part[s]};
+        uint32_t       ch[2];
+        for (int k = 0; k < 2; ++k)
+        {
+            const uint32_t t = sides[k];
+            if ((t & (t - 1)) == 0)
+                ch[k] = leaf[__ffs(t) - 1];
+            else
+            {
+                ch[k]       = inner[next++];
+                sset[sp]    = t;
+                sslot[sp++] = ch[k];
+            }
+        }
+        __stcg(&nodes[slot].child0, ch[0]);
+        __stcg(&nodes[slot].child1, ch[1]);
+        __stcg(&nodes[ch[0]].parent, slot);
+        __stcg(&nodes[ch[1]].parent, slot);
+    }
+    __threadfence();
+    for (int k = no - 1; k >= 0; --k) store_child_boxes(nodes, order[k]);
+}
+
+// One restructure pass of every geometry: leaf threads climb; the second to
+// arrive at a node counts its triangles and restructures it if it has enough.
+template <int kBits>
+__global__ void __launch_bounds__(kBlk) k_batch_restructure(BatchArgs b, DeviceWords* words)
+{
+    using Cfg            = KeyCfg<kBits>;
+    const uint32_t   t   = blockIdx.x / Cfg::kChunks;
+    const TileRef    r   = tile_ref(b, t);
+    const BuildItem& it  = b.items[r.g];
+    const uint64_t   k64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
+    const uint32_t   n   = it.n;
+    if (k64 >= n || n < 3) return;
+    BvhNode*  nodes = reinterpret_cast<BvhNode*>(it.result);
+    uint32_t* cnt   = reinterpret_cast<uint32_t*>(it.scratch + it.s_codes);  // free after emit: 2n-1 counts
+    const uint32_t leaf = n - 1 + (uint32_t)k64;
+    __stcg(&cnt[leaf], 1u);
+    uint32_t addr = __ldcg(&nodes[leaf].parent);
+    for (int level = 0; addr != kInvalid; ++level)
+    {
+        if (addr >= n - 1 || level > 96)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
+        __threadfence();
+        if (atomicExch(&nodes[addr].update, 1u) == 0u) return;
+        __threadfence();
+        const uint32_t c0 = __ldcg(&nodes[addr].child0), c1 = __ldcg(&nodes[addr].child1);
+        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            return;
+        }
+        const uint32_t c = __ldcg(&cnt[c0]) + __ldcg(&cnt[c1]);
+        __stcg(&cnt[addr], c);
+        if (c >= b.restructure_min) restructure_treelet(nodes, n, addr);
+        addr = __ldcg(&nodes[addr].parent);
+    }
+}
+
+// Every node's climb flag back to 0 before a restructure pass.
+__global__ void __launch_bounds__(kBlk) k_batch_reset_flags(BatchArgs b)
+{
+    for (uint32_t g = blockIdx.y; g < b.count; g += gridDim.y)
+    {
+        const BuildItem& it    = b.items[g];
+        const uint64_t   m     = it.n >= 3 ? 2ull * it.n - 1 : 0;  // smaller trees are not restructured
+        BvhNode*         nodes = reinterpret_cast<BvhNode*>(it.result);
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            nodes[i].update = 0;
+    }
+}
+
 // Leaf k of a geometry takes triangle `prim`'s vertices, then climbs: the
 // second child to arrive at a node (atomic flag) writes the node's two child
 // boxes and goes on to its parent (lbvh_fit_aabb_mesh.comp:94-205).
@@ -492,6 +700,18 @@ cudaError_t run_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cuda
     k_batch_emit<kBits><<<(unsigned)blocks, kBlk, 0, s>>>(b);
     k_batch_refit<kBits><<<(unsigned)blocks, kBlk, 0, s>>>(b, words);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (b.restructure_min)
+    {
+        const dim3 rgrid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((2ull * b.max_n + kBlk - 1) / kBlk,
+                                                                            (uint64_t)sm_count * 8)),
+                         std::min<uint32_t>(b.count, 65535u));
+        for (uint32_t pass = 0; pass < b.restructure_passes; ++pass)
+        {
+            k_batch_reset_flags<<<rgrid, kBlk, 0, s>>>(b);
+            k_batch_restructure<kBits><<<(unsigned)blocks, kBlk, 0, s>>>(b, words);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if (b.format == RR_CUDA_NODE_FORMAT_WIDE8) return launch_collapse_batch(b, words, sm_count, s);
     return cudaSuccess;
 }
@@ -662,8 +882,10 @@ cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* s
     b.total_tiles  = L.sort_tiles;
     b.total_prims  = L.n;
     b.max_n        = L.n;
-    b.format       = L.format;
-    b.morton_bits  = L.morton_bits;
+    b.format             = L.format;
+    b.morton_bits        = L.morton_bits;
+    b.restructure_min    = L.restructure_min;
+    b.restructure_passes = L.restructure_passes;
     return launch_build_batch(b, words, sm_count, s);
 }
 

@@ -121,7 +121,12 @@ struct GeomLayout
     // update scratch (RR_BUILD_OPERATION_UPDATE): descriptor | collapse queues
     size_t   u_queue, u_total;
     uint32_t sort_tiles, sort_passes;
+    // quality build: treelet restructure of nodes with >= restructure_min
+    // triangles (0: fast build), restructure_passes times
+    uint32_t restructure_min, restructure_passes;
 };
+constexpr uint32_t kRestructureMinPrims = 64;  // vlk/restructure_hlbvh.cpp:34
+constexpr uint32_t kRestructurePasses   = 3;   // vlk/restructure_hlbvh.cpp:35
 GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits);
 
 struct DeviceWords;
@@ -168,6 +173,8 @@ struct BatchArgs
     uint32_t         max_n;         // largest items[i].n
     uint32_t         format;
     uint32_t         morton_bits;
+    uint32_t         restructure_min;  // 0: fast build; else treelet restructure of nodes with >= this many triangles
+    uint32_t         restructure_passes;
 };
 size_t batch_desc_bytes(uint32_t count);
 // Geometry owning tile t: the largest g < count with prefix[g] <= t (prefix

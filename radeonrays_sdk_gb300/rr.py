@@ -252,9 +252,11 @@ class Context:
         return bi, mesh
 
     @staticmethod
-    def _options(node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30):
+    def _options(node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30, quality=False):
+        """quality=True clears RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD: the build adds the treelet restructure."""
         cuda_opts = RRCudaBuildOptions(C.sizeof(RRCudaBuildOptions), node_format, morton_bits, 0)
-        opts = RRBuildOptions(RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD, C.cast(C.pointer(cuda_opts), C.c_void_p))
+        flags = 0 if quality else RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD
+        opts = RRBuildOptions(flags, C.cast(C.pointer(cuda_opts), C.c_void_p))
         return opts, cuda_opts
 
     def geometry_requirements(self, ntri, node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30, nvert=0, stride=12,
@@ -267,8 +269,9 @@ class Context:
         return req.temporary_build_buffer_size, req.result_buffer_size
 
     def build_geometry(self, vertices, indices, node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30,
-                       stride=None, stream=None, scratch=None, result=None):
-        """vertices: cuda float32 tensor (V, k>=3) or flat; indices: cuda int32/int16 (T, 3)."""
+                       stride=None, stream=None, scratch=None, result=None, quality=False):
+        """vertices: cuda float32 tensor (V, k>=3) or flat; indices: cuda int32/int16 (T, 3).
+        quality=True: build flags without PREFER_FAST_BUILD (treelet restructure)."""
         torch = _torch()
         index16 = indices.dtype == torch.int16
         ntri = indices.numel() // 3
@@ -282,7 +285,7 @@ class Context:
             result = torch.empty(r_bytes, dtype=torch.uint8, device=dev)
         bi, mesh = self._build_input(self.ptr(vertices) if ntri else None, nvert, stride,
                                      self.ptr(indices) if ntri else None, ntri, index16)
-        opts, keep = self._options(node_format, morton_bits)
+        opts, keep = self._options(node_format, morton_bits, quality)
         own = stream is None
         cs = self.command_stream() if own else stream
         check(self.L.rrCmdBuildGeometry(self.ctx, RR_BUILD_OPERATION_BUILD, C.byref(bi), C.byref(opts),
@@ -318,7 +321,7 @@ class Context:
         return result
 
     def build_geometries(self, meshes, node_format=RR_CUDA_NODE_FORMAT_WIDE8, morton_bits=30, stream=None,
-                         api="batch"):
+                         api="batch", quality=False):
         """Build many meshes [(vertices (V, 3) float32, indices (T, 3) int32), ...] (cuda tensors).
 
         api "batch": one rrCudaCmdBuildGeometries call (one fused build);
@@ -329,7 +332,7 @@ class Context:
         offsets.  Returns the list of result tensors (views)."""
         torch = _torch()
         n = len(meshes)
-        opts, keep = self._options(node_format, morton_bits)
+        opts, keep = self._options(node_format, morton_bits, quality)
         reqs, inputs = [], []
         for v, i in meshes:
             ntri = i.numel() // 3

@@ -208,3 +208,57 @@ def test_oracle_fit_is_the_build_refit(orc):
     rlo = np.minimum(root["a0"], root["b0"])
     rhi = np.maximum(root["a1"], root["b1"])
     assert np.all(lo >= rlo) and np.all(hi <= rhi)
+
+
+def _check_tree(nodes, n):
+    """Every leaf reached exactly once from the root, parent links consistent,
+    every stored child box equal to the child's own box."""
+    seen = np.zeros(2 * n - 1, np.int32)
+    stack = [0]
+    while stack:
+        x = stack.pop()
+        seen[x] += 1
+        if x >= n - 1:
+            continue
+        for c, lo, hi in ((nodes["child0"][x], "a0", "a1"), (nodes["child1"][x], "b0", "b1")):
+            assert nodes["parent"][c] == x
+            if c < n - 1:
+                clo = np.minimum(nodes["a0"][c], nodes["b0"][c])
+                chi = np.maximum(nodes["a1"][c], nodes["b1"][c])
+            else:
+                tri = np.stack([nodes["a0"][c], nodes["a1"][c], nodes["b0"][c]])
+                clo, chi = tri.min(axis=0), tri.max(axis=0)
+            assert np.array_equal(nodes[lo][x], clo) and np.array_equal(nodes[hi][x], chi)
+            stack.append(int(c))
+    assert np.all(seen == 1)
+
+
+def _half_area_sum(nodes, n):
+    lo = np.minimum(nodes["a0"][: n - 1], nodes["b0"][: n - 1]).astype(np.float64)
+    hi = np.maximum(nodes["a1"][: n - 1], nodes["b1"][: n - 1]).astype(np.float64)
+    e = hi - lo
+    return float((e[:, 0] * e[:, 1] + e[:, 1] * e[:, 2] + e[:, 2] * e[:, 0]).sum())
+
+
+def test_oracle_restructure_is_a_valid_cheaper_tree(orc):
+    """The treelet restructure keeps a valid tree in the reference layout,
+    lowers the summed node area, is deterministic, and keeps every hit."""
+    from radeonrays_sdk_gb300 import scenes
+    v, i = scenes.heightfield(129, scenes.rng(81))
+    n = i.shape[0]
+    nodes, _, _ = orc.build_mesh(v, i)
+    r1, changed = orc.restructure(nodes, n, 64, 3)
+    r2, _ = orc.restructure(nodes, n, 64, 3)
+    assert changed > 0 and np.array_equal(r1.view(np.uint32), r2.view(np.uint32))
+    _check_tree(r1, n)
+    assert _half_area_sum(r1, n) < _half_area_sum(nodes, n)
+    assert np.array_equal(r1["child0"][n - 1:], nodes["child0"][n - 1:])  # leaves untouched
+    assert np.array_equal(r1["child1"][n - 1:], nodes["child1"][n - 1:])
+    rays = scenes.incoherent_rays(20000, v.min(axis=0), v.max(axis=0), scenes.rng(81, 1))
+    a, fa = orc.trace(nodes, rays, fetches=True)
+    b, fb = orc.trace(r1, rays, fetches=True)
+    assert np.array_equal(a[:, 2] != INVALID, b[:, 2] != INVALID)
+    assert fb.mean() < fa.mean()
+    if orc.ref_lib() is not None:
+        ok, _ = orc.ref_validate(r1)
+        assert ok
