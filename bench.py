@@ -82,6 +82,8 @@ def parse():
                          "serving: resident scenes + continuous batching")
     ap.add_argument("--blas", type=int, default=2048)
     ap.add_argument("--batch-rays", type=int, default=8_388_608)
+    ap.add_argument("--no-separate", action="store_true",
+                    help="blas2048: skip the one-by-one build baseline (about 160,000 launches)")
     ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--slots", type=int, default=3)
@@ -514,7 +516,8 @@ def run_batch(args):
     keep = ctx._keep
     f_t = timed(lambda: ctx.submit(cs), max(3, args.steps // 10), 2)
     # One rrCmdBuildGeometry per BLAS, each enqueued at once on a CUDA stream.
-    s_t = timed(lambda: ctx.build_geometries(meshes, node_format=fmt, api="separate"), 2, 1)
+    s_t = [float("nan")] if args.no_separate else \
+        timed(lambda: ctx.build_geometries(meshes, node_format=fmt, api="separate"), 2, 1)
     errors = ctx.device_errors()
     scene = ctx.build_scene(fused, M)
     tl_t = timed(lambda: ctx.build_scene(fused, M), 3, 1)

@@ -43,7 +43,7 @@ def lib() -> C.CDLL:
         _lib = C.CDLL(str(LIB))
         for name in ("rro_mesh_aabb", "rro_morton", "rro_sort32", "rro_sort64", "rro_emit", "rro_fit",
                      "rro_build_mesh", "rro_trace", "rro_build_scene", "rro_trace_scene", "rro_fp64_hit",
-                     "rro_trace_t", "rro_tri_test"):
+                     "rro_trace_t", "rro_tri_test", "rro_trace_leaves"):
             getattr(_lib, name).restype = None
     return _lib
 
@@ -128,17 +128,36 @@ def build_mesh(vertices, indices, bits=30, threads=8):
     return nodes, sidx, scodes
 
 
-def trace(nodes, rays, query=0, output=0, threads=8, hits=None, fetches=False):
+def trace(nodes, rays, query=0, output=0, threads=8, hits=None, fetches=False, box_leaves=False):
     """isect.comp semantics.  Full output: (R, 4) uint32 view of RRHit
-    (pre-filled with 0xFFFFFFFF unless `hits` is given); instance output: (R,) uint32."""
+    (pre-filled with 0xFFFFFFFF unless `hits` is given); instance output: (R,) uint32.
+    box_leaves: the tree of an AABB list (leaf = box, hit at the slab entry distance, uv = 0)."""
     R = rays.shape[0]
     r = np.ascontiguousarray(rays, dtype=np.float32)
     if hits is None:
         hits = np.full((R, 4) if output == 0 else (R,), INVALID, dtype=np.uint32)
     f = np.zeros(R, dtype=np.uint64) if fetches else None
-    lib().rro_trace(_p(nodes), C.c_uint32(nodes.size), _p(r), C.c_uint32(R), C.c_int(query), C.c_int(output),
-                    _p(hits), _p(f), C.c_int(threads))
+    lib().rro_trace_leaves(_p(nodes), C.c_uint32(nodes.size), _p(r), C.c_uint32(R), C.c_int(query),
+                           C.c_int(output), _p(hits), _p(f), C.c_int(threads), C.c_int(1 if box_leaves else 0))
     return (hits, f) if fetches else hits
+
+
+def aabb_vertices(boxes):
+    """An AABB list (n, 2, 4) or (n, 8) float32 [(min.xyz, _), (max.xyz, _)] as
+    the three leaf vertices the build stores for each box: (min, max, max)."""
+    b = np.asarray(boxes, dtype=np.float32).reshape(-1, 8)
+    lo, hi = b[:, 0:3], b[:, 4:7]
+    v = np.stack([lo, hi, hi], axis=1).reshape(-1, 3)
+    i = np.arange(v.shape[0], dtype=np.uint32).reshape(-1, 3)
+    return np.ascontiguousarray(v), i
+
+
+def build_aabbs(boxes, bits=30, threads=8):
+    """LBVH build of an AABB list: the mesh build over each box's (min, max,
+    max) leaf vertices -- same bounds (box min/max), same Morton input (box
+    centre) and the leaf layout the GPU writes.  Returns (nodes, sorted_idx, sorted_codes)."""
+    v, i = aabb_vertices(boxes)
+    return build_mesh(v, i, bits=bits, threads=threads)
 
 
 def trace_t(nodes, rays, threads=8):

@@ -414,8 +414,20 @@ static inline RayF xform_ray(const float* m, RayF r)
 // Single-level traversal of one ray (isect.comp:105-245).  The shader's split
 // 16-entry LDS stack + 64-entry global spill is a plain LIFO; the oracle uses a
 // vector with the same push/pop order.
+// Leaf of an AABB-list geometry (RR_PRIMITIVE_TYPE_AABB_LIST, which the
+// reference declares but does not implement, radeonrays.cpp:286-289): the leaf
+// holds its box as (min, max, max) in its three vertex slots.  The hit
+// distance is the slab entry distance (clamped to min_t); a miss returns
+// t_max.  Hit records of box leaves carry uv = (0, 0).
+static inline float isect_leaf_box(const RayF& r, F3 inv, F3 oxi, const float* lo, const float* hi, float t_max)
+{
+    float t0, t1;
+    isect_box(lo, hi, inv, oxi, t_max, r.tmin, t0, t1);
+    return t0 <= t1 ? t0 : t_max;
+}
+
 static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int full, void* hits, uint64_t gi,
-                      uint64_t* fetches)
+                      uint64_t* fetches, int box_leaves = 0)
 {
     RayF     r      = load_ray(rr);
     F3       inv    = safe_invdir(r.d);
@@ -457,7 +469,9 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
         }
         else
         {
-            float t = isect_tri(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1), ld3(nd.aabb1_min_or_v2), ct);
+            float t = box_leaves ? isect_leaf_box(r, inv, oxi, nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, ct)
+                                 : isect_tri(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                                             ld3(nd.aabb1_min_or_v2), ct);
             if (t < ct)
             {
                 if (!any)
@@ -470,8 +484,11 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
                     if (full)
                     {
                         rro_hit& h = ((rro_hit*)hits)[gi];
-                        barycentrics(hit_point(r, t), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
-                                     ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
+                        if (box_leaves)
+                            h.uv[0] = h.uv[1] = 0.f;
+                        else
+                            barycentrics(hit_point(r, t), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                                         ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
                         h.prim_id = nd.child1;
                         h.inst_id = 0;
                     }
@@ -490,8 +507,11 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
         if (full)
         {
             rro_hit& h = ((rro_hit*)hits)[gi];
-            barycentrics(hit_point(r, ct), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1), ld3(nd.aabb1_min_or_v2),
-                         h.uv[0], h.uv[1]);
+            if (box_leaves)
+                h.uv[0] = h.uv[1] = 0.f;
+            else
+                barycentrics(hit_point(r, ct), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                             ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
             h.prim_id = nd.child1;
             h.inst_id = 0;
         }
@@ -1019,6 +1039,24 @@ void rro_build_mesh(const float* vertices, uint32_t vertex_stride, const void* i
 // (16 B), 1 instance-id (uint32; the single-level kernel writes the primitive
 // id there, isect.comp:197,235).  An empty geometry (n_nodes == 0) misses.
 // fetches (optional): node fetches per ray.
+void rro_trace_leaves(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, int query,
+                      int output, void* hits, uint64_t* fetches, int threads, int box_leaves)
+{
+    const int any = query == 1, full = output == 0;
+    parallel_for(nrays, threads, [&](uint64_t i) {
+        if (n_nodes == 0)
+        {
+            if (full)
+                ((rro_hit*)hits)[i].inst_id = kInvalid;
+            else
+                ((uint32_t*)hits)[i] = kInvalid;
+            if (fetches) fetches[i] = 0;
+            return;
+        }
+        trace_one(nodes, rays[i], any, full, hits, i, fetches, box_leaves);
+    });
+}
+
 void rro_trace(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, int query, int output,
                void* hits, uint64_t* fetches, int threads)
 {

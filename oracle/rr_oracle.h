@@ -46,6 +46,9 @@ void rro_sort64(const uint64_t* codes, uint32_t n, uint64_t* sorted_codes, uint3
 void rro_emit(const void* sorted_codes, int bits, const uint32_t* sorted_idx, uint32_t n, rro_node* nodes,
               int threads);
 uint32_t rro_restructure(rro_node* nodes, uint32_t n, uint32_t min_prims, int passes);
+/* rro_trace with box leaves (AABB-list geometry) when box_leaves != 0. */
+void rro_trace_leaves(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, int query,
+                      int output, void* hits, uint64_t* fetches, int threads, int box_leaves);
 void rro_fit(const float* vertices, uint32_t vertex_stride, const void* indices, int index16, uint32_t n,
              rro_node* nodes);
 void rro_build_mesh(const float* vertices, uint32_t vertex_stride, const void* indices, int index16, uint32_t n,

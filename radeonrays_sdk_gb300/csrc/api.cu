@@ -84,6 +84,7 @@ struct BufInfo
     uint32_t format = RR_CUDA_NODE_FORMAT_BINARY;
     size_t   trailer_off = 0, wide_off = 0, tris_off = 0, xforms_off = 0, inst_off = 0;
     bool     scene_wide = false;
+    uint32_t prim_kind  = kPrimTriangles;  // geometry: triangles or AABB list
 };
 
 struct Context;
@@ -305,7 +306,7 @@ Op build_batch_op(Context* ctx, const std::vector<PendingGeom>& geoms, bool* man
     {
         const PendingGeom& g = geoms[i];
         hi[i]  = make_build_item(g.L, g.ma.vertices, g.ma.stride_floats, g.ma.indices, g.ma.index16, g.scratch,
-                                 g.result);
+                                 g.result, g.ma.prim_kind);
         htp[i] = (uint32_t)tiles;
         tiles += g.L.sort_tiles;
         prims += g.L.n;
@@ -390,8 +391,29 @@ bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
 
 // Validation of a triangle-mesh build input (reference radeonrays.cpp:242-299,
 // vlk/intersector.cpp:137-175).
-RRError check_mesh_input(const RRGeometryBuildInput* in, const RRTriangleMeshPrimitive** out, bool need_buffers)
+//
+// AABB lists (RR_PRIMITIVE_TYPE_AABB_LIST, radeonrays.h:194-206) are accepted
+// too, where the reference returns RR_ERROR_NOT_IMPLEMENTED
+// (radeonrays.cpp:286-289): one RRAABBListPrimitive of `aabb_count` boxes, each
+// a (min.xyz, _) (max.xyz, _) float4 pair `aabb_stride` bytes apart (at least
+// 32, a multiple of 4).  They are built into binary nodes only.
+RRError geometry_source(const RRGeometryBuildInput* in, bool need_buffers, MeshArgs* ma)
 {
+    if (in->primitive_type == RR_PRIMITIVE_TYPE_AABB_LIST)
+    {
+        if (in->primitive_count != 1 || !in->aabb_primitives) return RR_ERROR_INVALID_PARAMETER;
+        const RRAABBListPrimitive* b = in->aabb_primitives;
+        if (need_buffers && b->aabb_count > 0 && !b->aabbs) return RR_ERROR_INVALID_PARAMETER;
+        if (b->aabb_stride < 32 || (b->aabb_stride & 3u)) return RR_ERROR_INVALID_PARAMETER;
+        if (b->aabb_count >= (1u << 30)) return RR_ERROR_INVALID_PARAMETER;
+        ma->vertices      = b->aabbs ? reinterpret_cast<const float*>(P(b->aabbs)->addr()) : nullptr;
+        ma->stride_floats = b->aabb_stride >> 2;
+        ma->indices       = nullptr;
+        ma->index16       = 0;
+        ma->n             = b->aabb_count;
+        ma->prim_kind     = kPrimAabbs;
+        return RR_SUCCESS;
+    }
     if (in->primitive_type != RR_PRIMITIVE_TYPE_TRIANGLE_MESH) return RR_ERROR_NOT_IMPLEMENTED;
     if (in->primitive_count != 1 || !in->triangle_mesh_primitives) return RR_ERROR_INVALID_PARAMETER;
     const RRTriangleMeshPrimitive* m = in->triangle_mesh_primitives;
@@ -401,8 +423,19 @@ RRError check_mesh_input(const RRGeometryBuildInput* in, const RRTriangleMeshPri
     if (m->index_type != RR_INDEX_TYPE_UINT32 && m->index_type != RR_INDEX_TYPE_UINT16)
         return RR_ERROR_INVALID_PARAMETER;
     if (m->triangle_count >= (1u << 30)) return RR_ERROR_INVALID_PARAMETER;
-    *out = m;
+    ma->vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
+    ma->stride_floats = m->vertex_stride >> 2;
+    ma->indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
+    ma->index16       = m->index_type == RR_INDEX_TYPE_UINT16;
+    ma->n             = m->triangle_count;
+    ma->prim_kind     = kPrimTriangles;
     return RR_SUCCESS;
+}
+
+// Node format of a build: AABB lists have binary nodes only.
+inline uint32_t build_format(const MeshArgs& ma, uint32_t requested)
+{
+    return ma.prim_kind == kPrimAabbs ? (uint32_t)RR_CUDA_NODE_FORMAT_BINARY : requested;
 }
 
 // Validate one geometry build (reference radeonrays.cpp:242-299) and resolve
@@ -410,18 +443,12 @@ RRError check_mesh_input(const RRGeometryBuildInput* in, const RRTriangleMeshPri
 RRError prepare_geometry(const RRGeometryBuildInput* in, const BuildParams& bp, RRDevicePtr temporary_buffer,
                          RRDevicePtr geometry_buffer, PendingGeom* pg)
 {
-    const RRTriangleMeshPrimitive* m = nullptr;
-    RRError                        e = check_mesh_input(in, &m, true);
+    RRError e = geometry_source(in, true, &pg->ma);
     if (e != RR_SUCCESS) return e;
-    if (!geometry_buffer || (!temporary_buffer && m->triangle_count > 0)) return RR_ERROR_INVALID_PARAMETER;
-    pg->L                = geom_layout(m->triangle_count, bp.format, bp.bits);
+    if (!geometry_buffer || (!temporary_buffer && pg->ma.n > 0)) return RR_ERROR_INVALID_PARAMETER;
+    pg->L                    = geom_layout(pg->ma.n, build_format(pg->ma, bp.format), bp.bits);
     pg->L.restructure_min    = bp.restructure ? kRestructureMinPrims : 0u;
     pg->L.restructure_passes = bp.restructure ? kRestructurePasses : 0u;
-    pg->ma.vertices      = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
-    pg->ma.stride_floats = m->vertex_stride >> 2;
-    pg->ma.indices       = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
-    pg->ma.index16       = m->index_type == RR_INDEX_TYPE_UINT16;
-    pg->ma.n             = m->triangle_count;
     pg->scratch          = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
     pg->result           = P(geometry_buffer)->addr();
     return RR_SUCCESS;
@@ -437,6 +464,7 @@ void register_geometry(Context* ctx, const PendingGeom& pg)
     bi.trailer_off                      = pg.L.trailer_off;
     bi.wide_off                         = pg.L.wide_off;
     bi.tris_off                         = pg.L.tris_off;
+    bi.prim_kind                        = pg.ma.prim_kind;
     ctx->registry[(uintptr_t)pg.result] = bi;
 }
 
@@ -569,6 +597,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     const uint32_t trav  = o.traversal;
     const uint32_t nodes = bi.n == 0 ? 0u : 2u * bi.n - 1u;
     a.node_limit         = bi.kind == 0 ? kInvalid : nodes;
+    a.box_leaves         = bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs;
     a.wide_limit         = bi.n > 1 ? bi.n - 1 : 1u;
     a.tri_limit          = bi.n;
     if (bi.kind == kKindScene)
@@ -678,12 +707,12 @@ RR_API RRError rrGetGeometryBuildMemoryRequirements(RRContext                   
 {
     if (!context || !build_input || !memory_requirements) return RR_ERROR_INVALID_PARAMETER;
     RR_TRY({
-        const RRTriangleMeshPrimitive* m = nullptr;
-        RRError                        e = check_mesh_input(build_input, &m, false);
+        MeshArgs ma;
+        RRError  e = geometry_source(build_input, false, &ma);
         if (e != RR_SUCCESS) return e;
         BuildParams bp;
         if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
-        GeomLayout L                                      = geom_layout(m->triangle_count, bp.format, bp.bits);
+        GeomLayout L                                      = geom_layout(ma.n, build_format(ma, bp.format), bp.bits);
         memory_requirements->result_buffer_size           = L.total;
         memory_requirements->temporary_build_buffer_size  = L.s_total;
         memory_requirements->temporary_update_buffer_size = L.u_total;
@@ -700,25 +729,20 @@ namespace
 RRError record_update(Context* ctx, const RRGeometryBuildInput* in, RRDevicePtr temporary_buffer,
                       RRDevicePtr geometry_buffer, CommandStream* cs)
 {
-    const RRTriangleMeshPrimitive* m = nullptr;
-    RRError                        e = check_mesh_input(in, &m, true);
+    MeshArgs ma;
+    RRError  e = geometry_source(in, true, &ma);
     if (e != RR_SUCCESS) return e;
     if (!geometry_buffer) return RR_ERROR_INVALID_PARAMETER;
     uint8_t* result = P(geometry_buffer)->addr();
     auto     it     = ctx->registry.find((uintptr_t)result);
-    if (it == ctx->registry.end() || it->second.kind != kKindGeom || it->second.n != m->triangle_count)
+    if (it == ctx->registry.end() || it->second.kind != kKindGeom || it->second.n != ma.n ||
+        it->second.prim_kind != ma.prim_kind)
         return RR_ERROR_INVALID_PARAMETER;
     uint32_t bits = 30;
     // The key width is not needed by an update (no Morton codes); the layout
     // only depends on it for scratch offsets that an update does not use.
-    const GeomLayout L = geom_layout(m->triangle_count, it->second.format, bits);
+    const GeomLayout L = geom_layout(ma.n, it->second.format, bits);
     if (L.u_total > 0 && !temporary_buffer) return RR_ERROR_INVALID_PARAMETER;
-    MeshArgs ma;
-    ma.vertices          = m->vertices ? reinterpret_cast<const float*>(P(m->vertices)->addr()) : nullptr;
-    ma.stride_floats     = m->vertex_stride >> 2;
-    ma.indices           = m->triangle_indices ? P(m->triangle_indices)->addr() : nullptr;
-    ma.index16           = m->index_type == RR_INDEX_TYPE_UINT16;
-    ma.n                 = m->triangle_count;
     uint8_t*     scratch = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
     DeviceWords* words   = ctx->words;
     const int    sms     = ctx->sm_count;
@@ -777,9 +801,11 @@ RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_bu
             return RR_ERROR_INVALID_PARAMETER;
         const GeomLayout L = geom_layout(n, t.node_format, t.morton_bits);
         if (t.wide_nodes_off != L.wide_off || t.wide_tris_off != L.tris_off) return RR_ERROR_INVALID_PARAMETER;
+        if (t.prim_kind != kPrimTriangles && t.prim_kind != kPrimAabbs) return RR_ERROR_INVALID_PARAMETER;
         PendingGeom pg{};
-        pg.L      = L;
-        pg.result = result;
+        pg.L            = L;
+        pg.result       = result;
+        pg.ma.prim_kind = t.prim_kind;
         register_geometry(ctx, pg);
         return RR_SUCCESS;
     })
@@ -873,6 +899,9 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
             d.blas = (uint64_t)(uintptr_t)blas;
             if (it != ctx->registry.end() && it->second.kind == kKindGeom)
             {
+                // Instances of AABB-list geometry are not supported by the
+                // two-level kernels (their leaves are triangles).
+                if (it->second.prim_kind == kPrimAabbs) return RR_ERROR_NOT_IMPLEMENTED;
                 d.leaf_count = it->second.n;
                 if (it->second.format == RR_CUDA_NODE_FORMAT_WIDE8 && it->second.n > 0)
                 {
@@ -1095,7 +1124,8 @@ RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
             r.node_limit = bi.kind == 0 ? kInvalid : (bi.n == 0 ? 0u : 2u * bi.n - 1u);
             r.flags      = (q.query == RR_INTERSECT_QUERY_ANY ? kReqAny : 0u) |
                       (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
-                      (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u);
+                      (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u) |
+                      (bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs ? kReqBoxes : 0u);
             rq[k] = r;
             pf[k] = (uint32_t)total;
             total += q.ray_count;

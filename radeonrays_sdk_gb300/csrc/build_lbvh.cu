@@ -65,8 +65,18 @@ __device__ __forceinline__ F3 vtx(const BuildItem& m, uint32_t i)
     const float* p = m.vertices + (uint64_t)i * m.stride_floats;
     return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
+// The three leaf vertices of primitive t: a triangle's vertices, or for an
+// AABB list the box (min, max, max) read from its (min.xyzw, max.xyzw) pair.
 __device__ __forceinline__ void tri_verts(const BuildItem& m, uint32_t t, F3& a, F3& b, F3& c)
 {
+    if (m.prim_kind == kPrimAabbs)
+    {
+        const float* p = m.vertices + (uint64_t)t * m.stride_floats;
+        a              = f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+        b              = f3(__ldg(p + 4), __ldg(p + 5), __ldg(p + 6));
+        c              = b;
+        return;
+    }
     uint32_t i0 = tri_index(m, 3ull * t), i1 = tri_index(m, 3ull * t + 1), i2 = tri_index(m, 3ull * t + 2);
     a = vtx(m, i0);
     b = vtx(m, i1);
@@ -223,6 +233,7 @@ __global__ void __launch_bounds__(kBlk) k_batch_init(BatchArgs b)
         t.wide_capacity  = it.wide_capacity;
         t.tri_capacity   = it.tri_capacity;
         t.morton_bits    = b.morton_bits;
+        t.prim_kind      = it.prim_kind;
         *reinterpret_cast<Trailer*>(it.result + it.trailer_off) = t;
     }
     if (it.n == 0) return;
@@ -777,7 +788,7 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
 }
 
 BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t stride_floats, const void* indices,
-                          int index16, uint8_t* scratch, uint8_t* result)
+                          int index16, uint8_t* scratch, uint8_t* result, uint32_t prim_kind)
 {
     BuildItem it{};
     it.vertices      = vertices;
@@ -800,6 +811,7 @@ BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t s
     it.n             = L.n;
     it.index16       = index16 ? 1u : 0u;
     it.tiles         = L.sort_tiles;
+    it.prim_kind     = prim_kind;
     return it;
 }
 
@@ -826,7 +838,7 @@ cudaError_t launch_update_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* 
                                DeviceWords* words, int sm_count, cudaStream_t s)
 {
     if (L.n == 0) return cudaSuccess;
-    BuildItem it = make_build_item(L, m.vertices, m.stride_floats, m.indices, m.index16, scratch, result);
+    BuildItem it = make_build_item(L, m.vertices, m.stride_floats, m.indices, m.index16, scratch, result, m.prim_kind);
     it.s_queue   = L.u_queue;
     k_update_reset<<<grid_for(2ull * L.n - 1, kBlk), kBlk, 0, s>>>(reinterpret_cast<BvhNode*>(result), 2 * L.n - 1);
     k_update_fit<<<grid_for(L.n, kBlk), kBlk, 0, s>>>(it, words);
@@ -863,6 +875,7 @@ cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* s
         tr.kind        = kKindGeom;
         tr.node_format = L.format;
         tr.morton_bits = L.morton_bits;
+        tr.prim_kind   = m.prim_kind;
         k_init_trailer<<<1, 1, 0, s>>>(reinterpret_cast<Trailer*>(result + L.trailer_off), tr);
         return cudaGetLastError();
     }
@@ -871,7 +884,7 @@ cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* s
     BatchCtl*  ctl = nullptr;
     batch_carve(scratch + L.s_desc, 1, &items, &tp, &lp, &ctl);
     k_put_single<<<1, 32, 0, s>>>(items, make_build_item(L, m.vertices, m.stride_floats, m.indices, m.index16, scratch,
-                                                         result),
+                                                         result, m.prim_kind),
                                   tp, L.sort_tiles);
     BatchArgs b{};
     b.items        = items;

@@ -22,6 +22,12 @@ constexpr uint32_t kMaxInstancesRef = 2048;  // vlk/intersector.cpp:38 (accepted
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Primitive kinds of a geometry build.  An AABB-list leaf stores its box as
+// the three vertex slots (min, max, max): bounds, Morton centre and refit then
+// treat it exactly like a triangle with those vertices.
+constexpr uint32_t kPrimTriangles = 0;
+constexpr uint32_t kPrimAabbs     = 1;
+
 // 64-byte binary node in the reference layout (vlk/kernels/bvh2.h:25-35).
 // Internal nodes [0, N-2], leaves [N-1, 2N-2]; a leaf has child0 = invalid,
 // child1 = primitive id and its triangle's vertices in the first three vec3.
@@ -84,7 +90,8 @@ struct __align__(16) Trailer
     uint64_t tri_capacity;
     uint32_t bounds[8];     // mesh/scene box in the order-preserving uint encoding
     uint32_t morton_bits;
-    uint32_t pad[3];
+    uint32_t prim_kind;     // geometry: kPrimTriangles / kPrimAabbs
+    uint32_t pad[2];
     uint64_t xforms_off;    // scene: transforms [inverse, forward] per instance
     uint64_t inst_off;      // scene: InstanceDesc per instance
     uint64_t reserved[16];
@@ -146,7 +153,7 @@ struct __align__(16) BuildItem
     uint32_t     n;
     uint32_t     index16;
     uint32_t     tiles;     // sort tiles of this geometry
-    uint32_t     pad;
+    uint32_t     prim_kind; // kPrimTriangles / kPrimAabbs
 };
 
 // Batch-wide control words (device).
@@ -197,7 +204,7 @@ __device__ __forceinline__ uint32_t batch_find(const uint32_t* __restrict__ pref
 void batch_carve(uint8_t* block, uint32_t count, BuildItem** items, uint32_t** tile_prefix, uint32_t** level_prefix,
                  BatchCtl** ctl);
 BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t stride_floats, const void* indices,
-                          int index16, uint8_t* scratch, uint8_t* result);
+                          int index16, uint8_t* scratch, uint8_t* result, uint32_t prim_kind = kPrimTriangles);
 // Enqueue the whole fused build (the descriptors must already be on the device).
 cudaError_t launch_build_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s);
 
@@ -227,11 +234,12 @@ struct DeviceWords
 // ---- kernel launchers (all enqueue on `s`, return the launch error) ------
 struct MeshArgs
 {
-    const float* vertices;
-    uint64_t     stride_floats;
-    const void*  indices;
+    const float* vertices;       // triangles: vertex array; AABBs: the box array
+    uint64_t     stride_floats;  // vertex stride or box stride, in floats
+    const void*  indices;        // triangles only
     int          index16;
-    uint32_t     n;
+    uint32_t     n;              // triangles or boxes
+    uint32_t     prim_kind = kPrimTriangles;
 };
 
 cudaError_t launch_build_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* scratch, uint8_t* result,
@@ -280,11 +288,13 @@ struct TraceArgs
     int             block_size;
     int             blocks_per_sm;
     int             sm_count;
+    int             box_leaves;   // AABB-list geometry: leaves are boxes
 };
 // One request of a multi-request traversal launch (rrCudaCmdIntersectBatch).
 constexpr uint32_t kReqAny   = 1;  // any-hit query (else closest)
 constexpr uint32_t kReqFull  = 2;  // full RRHit output (else instance id)
 constexpr uint32_t kReqEmpty = 4;  // geometry without triangles: every ray misses
+constexpr uint32_t kReqBoxes = 8;  // AABB-list geometry: leaves are boxes
 struct __align__(16) BatchTraceReq
 {
     const uint8_t* bvh;   // geometry result buffer (binary nodes at offset 0)

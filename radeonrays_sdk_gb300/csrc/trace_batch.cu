@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
     PRay           s;
     const BvhNode* nodes = nullptr;
     uint32_t       gid = kInvalid, r = 0, nlim = 0, nf = 0;
-    bool           any = false, active = false, pending = false, exhausted = false;
+    bool           any = false, box = false, active = false, pending = false, exhausted = false;
     for (;;)
     {
         __syncwarp();
@@ -59,7 +59,14 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
                     if (s.caddr != kInvalid)
                     {
                         const NodeView nd = load_binary_node(nodes, s.caddr);
-                        if (full)
+                        if (box)
+                        {
+                            if (full)
+                                write_box_hit<true>(hits, gid, 0u, nd.child1, nd.child1);
+                            else
+                                write_box_hit<false>(hits, gid, 0u, nd.child1, nd.child1);
+                        }
+                        else if (full)
                             write_hit<true>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
                         else
                             write_hit<false>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
@@ -96,6 +103,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
                         nodes  = reinterpret_cast<const BvhNode*>(q.bvh);
                         nlim   = q.node_limit;
                         any    = (fl & kReqAny) != 0;
+                        box    = (fl & kReqBoxes) != 0;
                         p_start(s, q.rays, gid);
                     }
                 }
@@ -103,7 +111,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        if (active && p_step<false, true>(s, nodes, nlim, st, a.words, nf, any))
+        if (active && p_step<false, true>(s, nodes, nlim, st, a.words, nf, any, box))
         {
             active  = false;
             pending = true;

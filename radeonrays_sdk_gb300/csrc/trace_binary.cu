@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(kBlock) k_trace_binary(TraceArgs a)
         }
         else
         {
-            const float t = isect_tri(ray, nd.l0, nd.h0, nd.l1, ct);
+            const float t = a.box_leaves ? isect_leaf_box(ray, inv, oxi, nd.l0, nd.h0, ct)
+                                         : isect_tri(ray, nd.l0, nd.h0, nd.l1, ct);
             if (t < ct)
             {
                 if (!kAny)
@@ -108,7 +109,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_binary(TraceArgs a)
                 }
                 else
                 {
-                    write_hit<kFull>(a.hits, gid, ray, t, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                    if (a.box_leaves)
+                        write_box_hit<kFull>(a.hits, gid, 0u, nd.child1, nd.child1);
+                    else
+                        write_hit<kFull>(a.hits, gid, ray, t, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
                     if (kStats) add_stats(a.words, fetches, 0);
                     return;
                 }
@@ -127,7 +131,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_binary(TraceArgs a)
     if (caddr != kInvalid)
     {
         const NodeView nd = load_binary_node(nodes, caddr);
-        write_hit<kFull>(a.hits, gid, ray, ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+        if (a.box_leaves)
+            write_box_hit<kFull>(a.hits, gid, 0u, nd.child1, nd.child1);
+        else
+            write_hit<kFull>(a.hits, gid, ray, ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
     }
     else
         write_miss<kFull>(a.hits, gid);

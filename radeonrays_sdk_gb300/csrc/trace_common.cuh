@@ -131,6 +131,28 @@ __device__ __forceinline__ void write_hit(void* hits, uint32_t gid, const Ray& r
         reinterpret_cast<uint32_t*>(hits)[gid] = id_out;
 }
 
+// Leaf of an AABB-list geometry: the box is stored in the leaf's first two
+// vertex slots (min, max).  The hit distance is the slab entry distance,
+// clamped to min_t; a miss returns t_max.  (The reference declares AABB lists
+// but does not implement them, radeonrays.cpp:286-289; this is this build's
+// definition, shared with the oracle.)
+__device__ __forceinline__ float isect_leaf_box(const Ray& r, F3 inv, F3 oxi, F3 lo, F3 hi, float t_max)
+{
+    float t0, t1;
+    isect_box(lo, hi, inv, oxi, t_max, r.tmin, t0, t1);
+    return t0 <= t1 ? t0 : t_max;
+}
+
+// Hit record of a box leaf: uv = (0, 0).
+template <bool kFull>
+__device__ __forceinline__ void write_box_hit(void* hits, uint32_t gid, uint32_t inst, uint32_t prim, uint32_t id_out)
+{
+    if (kFull)
+        reinterpret_cast<uint4*>(hits)[gid] = make_uint4(0u, 0u, inst, prim);
+    else
+        reinterpret_cast<uint32_t*>(hits)[gid] = id_out;
+}
+
 // A miss writes only inst_id (isect.comp:238-244).
 template <bool kFull>
 __device__ __forceinline__ void write_miss(void* hits, uint32_t gid)

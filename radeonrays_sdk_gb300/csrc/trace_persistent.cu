@@ -18,7 +18,7 @@ namespace rr
 {
 namespace
 {
-template <bool kAny, bool kFull, bool kStats>
+template <bool kAny, bool kFull, bool kStats, bool kBox>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, uint32_t gcap)
 {
     __shared__ uint32_t s_stack[kPBlock * kPShort];
@@ -61,7 +61,11 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                     if (s.caddr != kInvalid)
                     {
                         const NodeView nd = load_binary_node(nodes, s.caddr);
-                        write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                        if (kBox)
+                            write_box_hit<kFull>(a.hits, gid, 0u, nd.child1, nd.child1);
+                        else
+                            write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1,
+                                             nd.child1);
                     }
                     else
                         write_miss<kFull>(a.hits, gid);
@@ -89,7 +93,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        if (active && p_step<kAny>(s, nodes, a.node_limit, st, a.words, nf))
+        if (active && p_step<kAny, false, kBox>(s, nodes, a.node_limit, st, a.words, nf))
         {
             active  = false;
             pending = true;
@@ -97,10 +101,10 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
     }
 }
 
-template <bool kAny, bool kFull, bool kStats>
-cudaError_t go(const TraceArgs& a, cudaStream_t s)
+template <bool kAny, bool kFull, bool kStats, bool kBox>
+cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 {
-    auto kern   = k_trace_persistent<kAny, kFull, kStats>;
+    auto kern   = k_trace_persistent<kAny, kFull, kStats, kBox>;
     int  per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {
@@ -112,6 +116,12 @@ cudaError_t go(const TraceArgs& a, cudaStream_t s)
     if (e != cudaSuccess) return e;
     kern<<<g.blocks, kPBlock, 0, s>>>(a, g.gcap);
     return cudaGetLastError();
+}
+
+template <bool kAny, bool kFull, bool kStats>
+cudaError_t go(const TraceArgs& a, cudaStream_t s)
+{
+    return a.box_leaves ? go2<kAny, kFull, kStats, true>(a, s) : go2<kAny, kFull, kStats, false>(a, s);
 }
 }  // namespace
 

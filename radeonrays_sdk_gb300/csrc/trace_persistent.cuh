@@ -55,10 +55,12 @@ __device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i
 
 // One iteration of the reference's traversal loop.  Returns true when the ray
 // is finished (stack empty, or a hit accepted by an any-hit query).  The
-// query is kAny, or `any` when kRuntimeAny (requests of both kinds mixed).
-template <bool kAny, bool kRuntimeAny = false>
+// query is kAny, or `any` when kRuntime (requests of both kinds mixed); the
+// leaves are boxes (AABB-list geometry) when kBox, or `box` when kRuntime.
+template <bool kAny, bool kRuntime = false, bool kBox = false>
 __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ nodes, uint32_t node_limit,
-                                       const PStack& st, DeviceWords* words, uint32_t& nf, bool any = false)
+                                       const PStack& st, DeviceWords* words, uint32_t& nf, bool any = false,
+                                       bool box = false)
 {
     if (++s.steps > kFetchCap || s.addr >= node_limit)
     {
@@ -106,12 +108,13 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
     }
     else
     {
-        const float t = isect_tri(s.ray, nd.l0, nd.h0, nd.l1, s.ct);
+        const float t = (kBox || (kRuntime && box)) ? isect_leaf_box(s.ray, s.inv, s.oxi, nd.l0, nd.h0, s.ct)
+                                                    : isect_tri(s.ray, nd.l0, nd.h0, nd.l1, s.ct);
         if (t < s.ct)
         {
             s.ct    = t;
             s.caddr = s.addr;
-            if (kAny || (kRuntimeAny && any)) done = true;
+            if (kAny || (kRuntime && any)) done = true;
         }
     }
     if (pop && !done)
