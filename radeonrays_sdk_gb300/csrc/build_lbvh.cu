@@ -179,24 +179,38 @@ __global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, ui
     emit_node<kBits>(codes, n, i, nodes);
 }
 
-__device__ __forceinline__ F3 ldcg3(const float* p) { return f3(__ldcg(p), __ldcg(p + 1), __ldcg(p + 2)); }
 
 // Box of a child node as the fit shader computes it (lbvh_fit_aabb_mesh.comp:94-118).
+// Loads are 16-byte L2-coherent vector loads (the node is four float4).
 __device__ __forceinline__ void child_box(const BvhNode* nodes, uint32_t c, F3& lo, F3& hi)
 {
-    const BvhNode* nd = nodes + c;
-    if (__ldcg(&nd->child0) != kInvalid)
+    const float4* p4 = reinterpret_cast<const float4*>(nodes + c);
+    const float4  w0 = __ldcg(p4), w1 = __ldcg(p4 + 1), w2 = __ldcg(p4 + 2);
+    const F3      a = f3(w0.x, w0.y, w0.z), b = f3(w1.x, w1.y, w1.z), p = f3(w2.x, w2.y, w2.z);
+    if (__float_as_uint(w0.w) != kInvalid)
     {
-        F3 a = ldcg3(nd->a0), b = ldcg3(nd->a1), p = ldcg3(nd->b0), q = ldcg3(nd->b1);
-        lo   = vmin(a, p);
-        hi   = vmax(b, q);
+        const float4 w3 = __ldcg(p4 + 3);
+        const F3     q  = f3(w3.x, w3.y, w3.z);
+        lo              = vmin(a, p);
+        hi              = vmax(b, q);
     }
     else
     {
-        F3 a = ldcg3(nd->a0), b = ldcg3(nd->a1), p = ldcg3(nd->b0);
-        lo   = vmin(vmin(a, b), p);
-        hi   = vmax(vmax(a, b), p);
+        lo = vmin(vmin(a, b), p);
+        hi = vmax(vmax(a, b), p);
     }
+}
+
+// Writes the two child boxes of internal node x as four 16-byte stores; the
+// child, parent and climb-flag words are rewritten with the values given.
+__device__ __forceinline__ void store_boxes4(BvhNode* nodes, uint32_t x, F3 lo0, F3 hi0, F3 lo1, F3 hi1, uint32_t c0,
+                                             uint32_t c1, uint32_t parent, uint32_t flag)
+{
+    float4* o = reinterpret_cast<float4*>(nodes + x);
+    __stcg(o + 0, make_float4(lo0.x, lo0.y, lo0.z, __uint_as_float(c0)));
+    __stcg(o + 1, make_float4(hi0.x, hi0.y, hi0.z, __uint_as_float(c1)));
+    __stcg(o + 2, make_float4(lo1.x, lo1.y, lo1.z, __uint_as_float(parent)));
+    __stcg(o + 3, make_float4(hi1.x, hi1.y, hi1.z, __uint_as_float(flag)));
 }
 
 template <int kBits>
@@ -416,22 +430,13 @@ __device__ __forceinline__ Bx3 box_of(const BvhNode* nodes, uint32_t c)
 __device__ __forceinline__ void store_child_boxes(BvhNode* nodes, uint32_t x)
 {
     BvhNode*       nd = nodes + x;
-    const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
+    const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1), parent = __ldcg(&nd->parent);
     F3             lo0, hi0, lo1, hi1;
     child_box(nodes, c0, lo0, hi0);
     child_box(nodes, c1, lo1, hi1);
-    __stcg(&nd->a0[0], lo0.x);
-    __stcg(&nd->a0[1], lo0.y);
-    __stcg(&nd->a0[2], lo0.z);
-    __stcg(&nd->a1[0], hi0.x);
-    __stcg(&nd->a1[1], hi0.y);
-    __stcg(&nd->a1[2], hi0.z);
-    __stcg(&nd->b0[0], lo1.x);
-    __stcg(&nd->b0[1], lo1.y);
-    __stcg(&nd->b0[2], lo1.z);
-    __stcg(&nd->b1[0], hi1.x);
-    __stcg(&nd->b1[1], hi1.y);
-    __stcg(&nd->b1[2], hi1.z);
+    // Every internal node under the node being restructured has been climbed
+    // through in this pass, so its flag is 1.
+    store_boxes4(nodes, x, lo0, hi0, lo1, hi1, c0, c1, parent, 1u);
 }
 
 __device__ void restructure_treelet(BvhNode* nodes, uint32_t n, uint32_t x)
@@ -631,19 +636,11 @@ __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, ui
         F3 lo0, hi0, lo1, hi1;
         child_box(nodes, c0, lo0, hi0);
         child_box(nodes, c1, lo1, hi1);
-        __stcg(&nd->a0[0], lo0.x);
-        __stcg(&nd->a0[1], lo0.y);
-        __stcg(&nd->a0[2], lo0.z);
-        __stcg(&nd->a1[0], hi0.x);
-        __stcg(&nd->a1[1], hi0.y);
-        __stcg(&nd->a1[2], hi0.z);
-        __stcg(&nd->b0[0], lo1.x);
-        __stcg(&nd->b0[1], lo1.y);
-        __stcg(&nd->b0[2], lo1.z);
-        __stcg(&nd->b1[0], hi1.x);
-        __stcg(&nd->b1[1], hi1.y);
-        __stcg(&nd->b1[2], hi1.z);
-        addr = __ldcg(&nd->parent);
+        // This thread arrived second: the flag is 1 and no other thread
+        // writes this node any more.
+        const uint32_t parent = __ldcg(&nd->parent);
+        store_boxes4(nodes, addr, lo0, hi0, lo1, hi1, c0, c1, parent, 1u);
+        addr = parent;
     }
 }
 

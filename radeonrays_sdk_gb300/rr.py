@@ -78,7 +78,13 @@ class RRTriangleMeshPrimitive(C.Structure):
                 ("triangle_indices", C.c_void_p), ("triangle_count", C.c_uint32), ("index_type", C.c_int)]
 
 
+class RRAABBListPrimitive(C.Structure):
+    _fields_ = [("aabbs", C.c_void_p), ("aabb_count", C.c_uint32), ("aabb_stride", C.c_uint32)]
+
+
 class RRGeometryBuildInput(C.Structure):
+    # The third field is a union of primitive pointers (radeonrays.h:215-226):
+    # for RR_PRIMITIVE_TYPE_AABB_LIST pass C.cast(pointer(RRAABBListPrimitive), ...).
     _fields_ = [("primitive_type", C.c_int), ("primitive_count", C.c_uint32),
                 ("triangle_mesh_primitives", C.POINTER(RRTriangleMeshPrimitive))]
 
@@ -293,6 +299,38 @@ class Context:
         if own:
             self.submit(cs)
             self.release_stream(cs)
+        return result
+
+    def _aabb_input(self, boxes, stride):
+        n = boxes.numel() * 4 // stride if boxes.numel() else 0
+        prim = RRAABBListPrimitive(self.ptr(boxes) if n else None, n, stride)
+        bi = RRGeometryBuildInput(RR_PRIMITIVE_TYPE_AABB_LIST, 1,
+                                  C.cast(C.pointer(prim), C.POINTER(RRTriangleMeshPrimitive)))
+        return bi, prim, n
+
+    def build_aabbs(self, boxes, stride=32, quality=False, stream=None, update_of=None):
+        """Build (or, with update_of = an earlier result, update) an AABB list: `boxes` is a cuda float32
+        tensor of (min.x, min.y, min.z, _, max.x, max.y, max.z, _) records `stride` bytes apart."""
+        torch = _torch()
+        bi, prim, n = self._aabb_input(boxes, stride)
+        opts, keep = self._options(RR_CUDA_NODE_FORMAT_BINARY, 30, quality)
+        req = RRMemoryRequirements()
+        check(self.L.rrGetGeometryBuildMemoryRequirements(self.ctx, C.byref(bi), C.byref(opts), C.byref(req)),
+              "rrGetGeometryBuildMemoryRequirements")
+        op = RR_BUILD_OPERATION_UPDATE if update_of is not None else RR_BUILD_OPERATION_BUILD
+        s_bytes = req.temporary_update_buffer_size if update_of is not None else req.temporary_build_buffer_size
+        scratch = torch.empty(max(s_bytes, 256), dtype=torch.uint8, device="cuda")
+        result = update_of if update_of is not None else torch.empty(req.result_buffer_size, dtype=torch.uint8,
+                                                                      device="cuda")
+        own = stream is None
+        cs = self.command_stream() if own else stream
+        check(self.L.rrCmdBuildGeometry(self.ctx, op, C.byref(bi), C.byref(opts), self.ptr(scratch),
+                                        self.ptr(result), cs), "rrCmdBuildGeometry(aabb list)")
+        if own:
+            self.submit(cs)
+            self.release_stream(cs)
+        else:
+            self._keep = (scratch, bi, prim)
         return result
 
     def update_geometry(self, vertices, indices, result, stream=None, scratch=None):

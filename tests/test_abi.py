@@ -81,8 +81,19 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     assert req_b.temporary_update_buffer_size == 0
     assert 0 < req.temporary_update_buffer_size < req.temporary_build_buffer_size
     # Unsupported primitive type / bad input.
-    bi2 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1, C.pointer(mesh))
-    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi2), None, C.byref(req)) == \
+    # AABB lists: sized like a binary-node build of that many leaves; a box
+    # stride below 32 bytes is rejected; an unknown primitive type is not implemented.
+    boxes = rr.RRAABBListPrimitive(None, 1000, 32)
+    bi2 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1,
+                                  C.cast(C.pointer(boxes), C.POINTER(rr.RRTriangleMeshPrimitive)))
+    req_a = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi2), None, C.byref(req_a)) == rr.RR_SUCCESS
+    assert req_a.result_buffer_size == req_b.result_buffer_size
+    boxes.aabb_stride = 16
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi2), None, C.byref(req_a)) == \
+        rr.RR_ERROR_INVALID_PARAMETER
+    bi5 = rr.RRGeometryBuildInput(7, 1, C.pointer(mesh))
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi5), None, C.byref(req)) == \
         rr.RR_ERROR_NOT_IMPLEMENTED
     bi3 = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_TRIANGLE_MESH, 2, C.pointer(mesh))
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi3), None, C.byref(req)) == \

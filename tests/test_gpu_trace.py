@@ -177,10 +177,14 @@ def test_argument_errors_with_context(ctx):
     from radeonrays_sdk_gb300 import rr
     L = ctx.L
     mesh = rr.RRTriangleMeshPrimitive(None, 0, 12, None, 10, rr.RR_INDEX_TYPE_UINT32)
-    bi = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1, C.pointer(mesh))
+    bi = rr.RRGeometryBuildInput(7, 1, C.pointer(mesh))  # no such primitive type
     cs = ctx.command_stream()
     fake = C.c_void_p(0x1000)
     assert L.rrCmdBuildGeometry(ctx.ctx, 1, C.byref(bi), None, fake, fake, cs) == rr.RR_ERROR_NOT_IMPLEMENTED
+    boxes = rr.RRAABBListPrimitive(None, 10, 12)  # box stride below 32 bytes
+    bi = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_AABB_LIST, 1,
+                                 C.cast(C.pointer(boxes), C.POINTER(rr.RRTriangleMeshPrimitive)))
+    assert L.rrCmdBuildGeometry(ctx.ctx, 1, C.byref(bi), None, fake, fake, cs) == rr.RR_ERROR_INVALID_PARAMETER
     bi = rr.RRGeometryBuildInput(rr.RR_PRIMITIVE_TYPE_TRIANGLE_MESH, 1, C.pointer(mesh))
     assert L.rrCmdBuildGeometry(ctx.ctx, 1, C.byref(bi), None, fake, fake, cs) == rr.RR_ERROR_INVALID_PARAMETER
     assert L.rrCmdBuildGeometry(ctx.ctx, rr.RR_BUILD_OPERATION_UPDATE, C.byref(bi), None, fake, fake, cs) in (

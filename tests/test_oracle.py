@@ -210,6 +210,25 @@ def test_oracle_fit_is_the_build_refit(orc):
     assert np.all(lo >= rlo) and np.all(hi <= rhi)
 
 
+def test_oracle_aabb_leaves(orc):
+    """AABB-list semantics: a ray through a box hits it at the slab entry
+    distance, the nearest entry wins, a ray starting inside hits at min_t,
+    and a ray that misses every box writes only inst_id."""
+    b = np.zeros((3, 8), np.float32)
+    b[0, 0:3], b[0, 4:7] = (0.0, 0.0, 2.0), (1.0, 1.0, 3.0)   # entry t = 2
+    b[1, 0:3], b[1, 4:7] = (0.0, 0.0, 5.0), (1.0, 1.0, 6.0)   # behind box 0
+    b[2, 0:3], b[2, 4:7] = (4.0, 4.0, -1.0), (5.0, 5.0, 1.0)  # holds the origin of ray 2
+    nodes, _, _ = orc.build_aabbs(b)
+    rays = np.array([[0.5, 0.5, 0.0, 0.0, 0.0, 0.0, 1.0, 100.0],
+                     [0.5, 0.5, 0.0, 0.0, 0.0, 0.0, -1.0, 100.0],
+                     [4.5, 4.5, 0.0, 0.25, 0.0, 0.0, 1.0, 100.0]], np.float32)
+    h = orc.trace(nodes, rays, box_leaves=True)
+    assert list(h[0]) == [0, 0, 0, 0] and h[2, 3] == 2 and h[2, 2] == 0
+    assert h[1, 2] == INVALID and h[1, 0] == INVALID  # miss: only inst_id written, the rest keeps the fill
+    hi = orc.trace(nodes, rays, output=1, box_leaves=True)
+    assert list(hi) == [0, INVALID, 2]
+
+
 def _check_tree(nodes, n):
     """Every leaf reached exactly once from the root, parent links consistent,
     every stored child box equal to the child's own box."""
