@@ -243,6 +243,32 @@ RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
                                        RRDevicePtr                   scratch,
                                        RRCommandStream               command_stream);
 
+/* The same launch for requests whose rays and hits live in host memory (page-
+ * locked for asynchronous copies): every request's rays are copied into
+ * `rays` (a device buffer of the total ray count), the hit buffer `hits`
+ * (16 bytes per ray of the total) is filled with 0xFF, one persistent launch
+ * traces all requests, and every request's hits are copied back to its host
+ * buffer (16 or 4 bytes per ray), all on the command stream in that order.
+ * Record fields a miss leaves untouched read back as 0xFFFFFFFF.  One call per
+ * launch replaces one copy and one handle per request in a serving loop. */
+typedef struct
+{
+    RRDevicePtr            geometry;
+    RRIntersectQuery       query;
+    RRIntersectQueryOutput output;
+    const void*            host_rays;  /* RRRay[ray_count] */
+    uint32_t               ray_count;
+    void*                  host_hits;  /* RRHit[ray_count] or uint32_t[ray_count] */
+} RRCudaHostIntersectRequest;
+
+RR_API RRError rrCudaCmdIntersectBatchHost(RRContext                         context,
+                                           uint32_t                          request_count,
+                                           const RRCudaHostIntersectRequest* requests,
+                                           RRDevicePtr                       rays,
+                                           RRDevicePtr                       hits,
+                                           RRDevicePtr                       scratch,
+                                           RRCommandStream                   command_stream);
+
 /* Intersect without allocating anything and without a caller scratch buffer.
  * No counterpart in the reference API.
  *

@@ -1083,6 +1083,83 @@ RR_API RRError rrCudaGetIntersectBatchMemoryRequirements(RRContext context, uint
     return RR_SUCCESS;
 }
 
+namespace
+{
+// One request of a multi-request launch, resolved to device addresses.
+struct DevRequest
+{
+    uint8_t*               bvh;
+    RRIntersectQuery       query;
+    RRIntersectQueryOutput output;
+    uint8_t*               rays;
+    uint32_t               ray_count;
+    uint8_t*               hits;
+};
+
+// The op of one multi-request launch: the request table and ray prefix are
+// staged in pinned host memory (owned by the op) and copied into the scratch
+// before the persistent launch.
+RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t* sc, Op* out)
+{
+    const uint32_t         count = (uint32_t)dq.size();
+    const BatchTraceLayout L0    = batch_trace_layout(count, 0);
+    const size_t           pre   = ((size_t)count + 1) * sizeof(uint32_t);
+    const size_t           gap   = L0.prefix_off - L0.req_off;
+    auto                   stage = std::make_shared<PinnedBlock>(gap + pre);
+    BatchTraceReq*         rq    = reinterpret_cast<BatchTraceReq*>(stage->p);
+    uint32_t*              pf    = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(stage->p) + gap);
+    std::memset(stage->p, 0, gap + pre);
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < count; ++k)
+    {
+        const DevRequest& q = dq[k];
+        if (q.query != RR_INTERSECT_QUERY_CLOSEST && q.query != RR_INTERSECT_QUERY_ANY)
+            return RR_ERROR_INVALID_PARAMETER;
+        if (q.output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && q.output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+            return RR_ERROR_INVALID_PARAMETER;
+        auto    it = ctx->registry.find((uintptr_t)q.bvh);
+        BufInfo bi;
+        if (it != ctx->registry.end()) bi = it->second;
+        if (bi.kind == kKindScene) return RR_ERROR_NOT_IMPLEMENTED;
+        BatchTraceReq r{};
+        r.bvh        = q.bvh;
+        r.rays       = q.ray_count ? q.rays : nullptr;
+        r.hits       = q.ray_count ? q.hits : nullptr;
+        r.ray_count  = q.ray_count;
+        r.node_limit = bi.kind == 0 ? kInvalid : (bi.n == 0 ? 0u : 2u * bi.n - 1u);
+        r.flags      = (q.query == RR_INTERSECT_QUERY_ANY ? kReqAny : 0u) |
+                  (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
+                  (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u) |
+                  (bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs ? kReqBoxes : 0u);
+        rq[k] = r;
+        pf[k] = (uint32_t)total;
+        total += q.ray_count;
+        if (total >= 0xffffffffull) return RR_ERROR_INVALID_PARAMETER;
+    }
+    pf[count]                = (uint32_t)total;
+    const BatchTraceLayout L = batch_trace_layout(count, total);
+    BatchTraceArgs         a{};
+    a.req              = reinterpret_cast<const BatchTraceReq*>(sc + L.req_off);
+    a.prefix           = reinterpret_cast<const uint32_t*>(sc + L.prefix_off);
+    a.count            = count;
+    a.total            = (uint32_t)total;
+    a.scratch          = sc;
+    a.scratch_bytes    = L.total;
+    a.spill_off        = L.spill_off;
+    a.words            = ctx->words;
+    a.sm_count         = ctx->sm_count;
+    a.blocks_per_sm    = (int)ctx->topts.blocks_per_sm;
+    a.collect_stats    = ctx->topts.collect_stats ? 1 : 0;
+    const size_t bytes = gap + pre;
+    *out               = [=](cudaStream_t s) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(sc + L.req_off, stage->p, bytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        return launch_trace_batch(a, s);
+    };
+    return RR_SUCCESS;
+}
+}  // namespace
+
 RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
                                        uint32_t                      request_count,
                                        const RRCudaIntersectRequest* requests,
@@ -1094,65 +1171,78 @@ RR_API RRError rrCudaCmdIntersectBatch(RRContext                     context,
     RR_TRY({
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
-        // Host staging of [request table | prefix], copied into the scratch by the op.
-        const BatchTraceLayout L0    = batch_trace_layout(request_count, 0);
-        const size_t           pre   = ((size_t)request_count + 1) * sizeof(uint32_t);
-        const size_t           gap   = L0.prefix_off - L0.req_off;
-        auto                   stage = std::make_shared<PinnedBlock>(gap + pre);
-        BatchTraceReq*         rq    = reinterpret_cast<BatchTraceReq*>(stage->p);
-        uint32_t*              pf    = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(stage->p) + gap);
-        std::memset(stage->p, 0, gap + pre);
-        uint64_t total = 0;
+        std::vector<DevRequest> dq(request_count);
         for (uint32_t k = 0; k < request_count; ++k)
         {
             const RRCudaIntersectRequest& q = requests[k];
             if (!q.geometry || (q.ray_count && (!q.rays || !q.hits))) return RR_ERROR_INVALID_PARAMETER;
-            if (q.query != RR_INTERSECT_QUERY_CLOSEST && q.query != RR_INTERSECT_QUERY_ANY)
-                return RR_ERROR_INVALID_PARAMETER;
-            if (q.output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && q.output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
-                return RR_ERROR_INVALID_PARAMETER;
-            uint8_t* bvh = P(q.geometry)->addr();
-            auto     it  = ctx->registry.find((uintptr_t)bvh);
-            BufInfo  bi;
-            if (it != ctx->registry.end()) bi = it->second;
-            if (bi.kind == kKindScene) return RR_ERROR_NOT_IMPLEMENTED;
-            BatchTraceReq r{};
-            r.bvh        = bvh;
-            r.rays       = q.ray_count ? P(q.rays)->addr() : nullptr;
-            r.hits       = q.ray_count ? P(q.hits)->addr() : nullptr;
-            r.ray_count  = q.ray_count;
-            r.node_limit = bi.kind == 0 ? kInvalid : (bi.n == 0 ? 0u : 2u * bi.n - 1u);
-            r.flags      = (q.query == RR_INTERSECT_QUERY_ANY ? kReqAny : 0u) |
-                      (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
-                      (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u) |
-                      (bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs ? kReqBoxes : 0u);
-            rq[k] = r;
-            pf[k] = (uint32_t)total;
-            total += q.ray_count;
-            if (total >= 0xffffffffull) return RR_ERROR_INVALID_PARAMETER;
+            dq[k] = DevRequest{P(q.geometry)->addr(), q.query, q.output, q.ray_count ? P(q.rays)->addr() : nullptr,
+                               q.ray_count, q.ray_count ? P(q.hits)->addr() : nullptr};
         }
-        pf[request_count]        = (uint32_t)total;
-        const BatchTraceLayout L = batch_trace_layout(request_count, total);
-        uint8_t*               sc = P(scratch)->addr();
-        BatchTraceArgs         a{};
-        a.req           = reinterpret_cast<const BatchTraceReq*>(sc + L.req_off);
-        a.prefix        = reinterpret_cast<const uint32_t*>(sc + L.prefix_off);
-        a.count         = request_count;
-        a.total         = (uint32_t)total;
-        a.scratch       = sc;
-        a.scratch_bytes = L.total;
-        a.spill_off     = L.spill_off;
-        a.words         = ctx->words;
-        a.sm_count      = ctx->sm_count;
-        a.blocks_per_sm = (int)ctx->topts.blocks_per_sm;
-        a.collect_stats = ctx->topts.collect_stats ? 1 : 0;
-        const size_t bytes = gap + pre;
+        Op      op;
+        RRError e = batch_trace_op(ctx, dq, P(scratch)->addr(), &op);
+        if (e != RR_SUCCESS) return e;
+        record(S(command_stream), std::move(op), true);
+        return RR_SUCCESS;
+    })
+}
+
+RR_API RRError rrCudaCmdIntersectBatchHost(RRContext                         context,
+                                           uint32_t                          request_count,
+                                           const RRCudaHostIntersectRequest* requests,
+                                           RRDevicePtr                       rays,
+                                           RRDevicePtr                       hits,
+                                           RRDevicePtr                       scratch,
+                                           RRCommandStream                   command_stream)
+{
+    RR_LOG_INFO("rrCudaCmdIntersectBatchHost(%u)", request_count);
+    if (!context || !requests || !request_count || !rays || !hits || !scratch || !command_stream)
+        return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        uint8_t*    dr  = P(rays)->addr();
+        uint8_t*    dh  = P(hits)->addr();
+        std::vector<DevRequest> dq(request_count);
+        struct Copy
+        {
+            const void* host_rays;
+            void*       host_hits;
+            uint8_t*    dev_rays;
+            uint8_t*    dev_hits;
+            size_t      ray_bytes, hit_bytes;
+        };
+        std::vector<Copy> copies;
+        uint64_t          off = 0;
+        for (uint32_t k = 0; k < request_count; ++k)
+        {
+            const RRCudaHostIntersectRequest& q = requests[k];
+            if (!q.geometry || (q.ray_count && (!q.host_rays || !q.host_hits))) return RR_ERROR_INVALID_PARAMETER;
+            const size_t hs = q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? 16 : 4;
+            dq[k] = DevRequest{P(q.geometry)->addr(), q.query, q.output, dr + 32 * off, q.ray_count, dh + 16 * off};
+            if (q.ray_count)
+                copies.push_back(Copy{q.host_rays, q.host_hits, dr + 32 * off, dh + 16 * off, 32ull * q.ray_count,
+                                      hs * q.ray_count});
+            off += q.ray_count;
+        }
+        Op      trace;
+        RRError e = batch_trace_op(ctx, dq, P(scratch)->addr(), &trace);
+        if (e != RR_SUCCESS) return e;
+        const size_t hit_total = 16 * off;
         record(
             S(command_stream),
             [=](cudaStream_t s) -> cudaError_t {
-                cudaError_t e = cudaMemcpyAsync(sc + L.req_off, stage->p, bytes, cudaMemcpyHostToDevice, s);
-                if (e != cudaSuccess) return e;
-                return launch_trace_batch(a, s);
+                cudaError_t e = cudaSuccess;
+                for (size_t i = 0; i < copies.size() && e == cudaSuccess; ++i)
+                    e = cudaMemcpyAsync(copies[i].dev_rays, copies[i].host_rays, copies[i].ray_bytes,
+                                        cudaMemcpyHostToDevice, s);
+                // Fields a miss leaves untouched read back as 0xFFFFFFFF.
+                if (e == cudaSuccess) e = cudaMemsetAsync(dh, 0xff, hit_total, s);
+                if (e == cudaSuccess) e = trace(s);
+                for (size_t i = 0; i < copies.size() && e == cudaSuccess; ++i)
+                    e = cudaMemcpyAsync(copies[i].host_hits, copies[i].dev_hits, copies[i].hit_bytes,
+                                        cudaMemcpyDeviceToHost, s);
+                return e;
             },
             true);
         return RR_SUCCESS;

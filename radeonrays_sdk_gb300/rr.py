@@ -130,6 +130,14 @@ class RRCudaIntersectRequest(C.Structure):
 assert C.sizeof(RRGeometryBuildInput) == 16 and C.sizeof(RRInstance) == 56 and C.sizeof(RRMemoryRequirements) == 24
 assert C.sizeof(RRCudaIntersectRequest) == 40
 
+
+class RRCudaHostIntersectRequest(C.Structure):
+    _fields_ = [("geometry", C.c_void_p), ("query", C.c_int), ("output", C.c_int), ("host_rays", C.c_void_p),
+                ("ray_count", C.c_uint32), ("host_hits", C.c_void_p)]
+
+
+assert C.sizeof(RRCudaHostIntersectRequest) == 40
+
 # Every symbol the headers declare, with its ctypes prototype.
 _P = C.c_void_p
 _PP = C.POINTER(C.c_void_p)
@@ -172,6 +180,7 @@ PROTOTYPES = {
     "rrCudaGetIntersectBatchMemoryRequirements": [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_size_t)],
     "rrCudaCmdIntersectHostBuffers": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P, _P, _P, C.c_uint32, _P],
     "rrCudaRegisterGeometry": [_P, _P, C.c_uint32],
+    "rrCudaCmdIntersectBatchHost": [_P, C.c_uint32, C.POINTER(RRCudaHostIntersectRequest), _P, _P, _P, _P],
     "rrCudaCmdIntersectBatch": [_P, C.c_uint32, C.POINTER(RRCudaIntersectRequest), _P, _P],
 }
 

@@ -66,6 +66,7 @@ class ScenePool:
         self.bytes = 0
         self.builds = 0
         self.evictions = 0
+        self.handles: dict = {}  # scene -> RRDevicePtr of its resident buffer
 
     def register(self, scene: int, vertices: np.ndarray, indices: np.ndarray) -> None:
         self.meshes[scene] = (np.ascontiguousarray(vertices, np.float32), np.ascontiguousarray(indices, np.uint32))
@@ -84,8 +85,22 @@ class ScenePool:
                 buf = self.resident.pop(sid)
                 self.bytes -= buf.numel()
                 self.evictions += 1
+                h = self.handles.pop(sid, None)
+                if h is not None:
+                    self.ctx.L.rrReleaseDevicePtr(self.ctx.ctx, h)
                 del buf
         return self.bytes + need <= self.budget
+
+    def handle(self, scene: int):
+        """RRDevicePtr of a resident scene's buffer, made once and kept while it is resident."""
+        import ctypes as C
+        h = self.handles.get(scene)
+        if h is None:
+            h = C.c_void_p()
+            rr.check(self.ctx.L.rrGetDevicePtrFromCudaPtr(self.ctx.ctx, C.c_void_p(self.resident[scene].data_ptr()),
+                                                          0, C.byref(h)), "rrGetDevicePtrFromCudaPtr")
+            self.handles[scene] = h
+        return h
 
     def build(self, scene: int):
         """Build one scene's BVH through rrCmdBuildGeometry; returns the result buffer."""
@@ -126,10 +141,21 @@ class _Slot:
         self.hits = torch.empty((slot_rays, 4), dtype=torch.int32, device="cuda")
         self.scratch = torch.empty(ctx.batch_scratch_bytes(max_requests, slot_rays), dtype=torch.uint8,
                                    device="cuda")
+        # Handles of the arenas, made once (the loop passes them every launch).
+        self.h_rays, self.h_hits, self.h_scratch = (self._handle(ctx, t) for t in (self.rays, self.hits,
+                                                                                  self.scratch))
         self.event = torch.cuda.Event()
         self.busy = False
         self.reqs: list[tuple[Request, int]] = []  # (request, ray offset in the arena)
         self.launches = 0
+
+    @staticmethod
+    def _handle(ctx, t):
+        import ctypes as C
+        h = C.c_void_p()
+        rr.check(ctx.L.rrGetDevicePtrFromCudaPtr(ctx.ctx, C.c_void_p(t.data_ptr()), 0, C.byref(h)),
+                 "rrGetDevicePtrFromCudaPtr")
+        return h
 
 
 class Server:
@@ -161,30 +187,24 @@ class Server:
         return batch
 
     def _launch(self, slot: _Slot, batch: list, now: float) -> None:
-        import torch
+        """One rrCudaCmdIntersectBatchHost on the slot's stream: the library
+        copies every request's rays in, fills the hit arena, traces all
+        requests in one persistent launch and copies every request's hits
+        back to its pinned buffer (misses read 0xFFFFFFFF outside inst_id)."""
+        import ctypes as C
         off = 0
-        reqs = []
         slot.reqs = []
-        base_r, base_h = slot.rays.data_ptr(), slot.hits.data_ptr()
-        with torch.cuda.stream(slot.stream):
-            for r, bvh in batch:
-                n = r.rays.shape[0]
-                slot.rays[off:off + n].copy_(self._pinned[r.rid][0], non_blocking=True)
-                slot.reqs.append((r, off))
-                reqs.append((bvh, (base_r + 32 * off, n), base_h + 16 * off, r.query, r.output))
-                off += n
-            # A miss writes only inst_id: the rest of a missed ray's record
-            # reads back as 0xFFFFFFFF, as in a buffer filled before the call.
-            slot.hits[:off].fill_(-1)
-            self.ctx.cmd_intersect_batch(reqs, slot.scratch, slot.cs)
-            for r, o in slot.reqs:
-                n = r.rays.shape[0]
-                # Instance-id output is one uint32 per ray, packed from the
-                # request's start: its first n / 4 records hold it.
-                m = n if r.output == rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT else (n + 3) // 4
-                self._pinned[r.rid][1][:m].copy_(slot.hits[o:o + m], non_blocking=True)
-            slot.event.record(slot.stream)
-        self.ctx.release_ptrs()
+        arr = (rr.RRCudaHostIntersectRequest * len(batch))()
+        for k, (r, _) in enumerate(batch):
+            n = r.rays.shape[0]
+            rays_h, hits_h = self._pinned[r.rid]
+            arr[k] = rr.RRCudaHostIntersectRequest(self.pool.handle(r.scene), r.query, r.output,
+                                                   C.c_void_p(rays_h.data_ptr()), n, C.c_void_p(hits_h.data_ptr()))
+            slot.reqs.append((r, off))
+            off += n
+        rr.check(self.ctx.L.rrCudaCmdIntersectBatchHost(self.ctx.ctx, len(batch), arr, slot.h_rays, slot.h_hits,
+                                                        slot.h_scratch, slot.cs), "rrCudaCmdIntersectBatchHost")
+        slot.event.record(slot.stream)
         for r, _ in batch:
             r.admitted = now
         slot.busy = True
