@@ -439,7 +439,45 @@ __device__ __forceinline__ void store_child_boxes(BvhNode* nodes, uint32_t x)
     store_boxes4(nodes, x, lo0, hi0, lo1, hi1, c0, c1, parent, 1u);
 }
 
-__device__ void restructure_treelet(BvhNode* nodes, uint32_t n, uint32_t x)
+// Shared tables of one warp's treelet optimisation.
+struct TreeletDp
+{
+    float   area[128];
+    float   cost[128];
+    uint8_t part[128];
+};
+
+// Best split of subset s (first minimum in the order of decreasing p over the
+// proper subsets p of s that hold s's lowest bit), scanning the partitions
+// with index i = j, j + stride, ... in that order.
+__device__ __forceinline__ void best_split(const TreeletDp& t, uint32_t s, uint32_t j, uint32_t stride, float& best,
+                                           uint32_t& bp)
+{
+    const uint32_t low = s & (0u - s);
+    best               = 0.f;
+    bp                 = 0;
+    uint32_t idx       = 0;
+    for (uint32_t p = (s - 1) & s; p; p = (p - 1) & s)
+    {
+        if (!(p & low)) continue;
+        if (idx++ % stride != j) continue;
+        const float c = t.cost[p] + t.cost[s ^ p];
+        if (bp == 0 || c < best)
+        {
+            best = c;
+            bp   = p;
+        }
+    }
+}
+
+// Restructure the treelet rooted at internal node x with the whole warp (all
+// 32 lanes call it with the same x).  Same treelet, same tables, same tie rules
+// as the sequential restatement (oracle rro_restructure), so the tree is
+// identical: every lane forms the treelet (same loads); subset areas are
+// spread over the lanes; subsets are costed by size, one lane per subset, and
+// the largest subset (the whole treelet) by all lanes with a min reduction
+// that keeps the first minimum in enumeration order; lane 0 rebuilds.
+__device__ void restructure_treelet_warp(BvhNode* nodes, uint32_t n, uint32_t x, TreeletDp& t, uint32_t lane)
 {
     uint32_t leaf[7], inner[6];
     float    la[7];
@@ -468,13 +506,11 @@ __device__ void restructure_treelet(BvhNode* nodes, uint32_t n, uint32_t x)
         la[nl]           = half_area3(box_of(nodes, leaf[nl]));
         ++nl;
     }
-    if (nl < 3) return;
+    if (nl < 3) return;  // warp-uniform: every lane formed the same treelet
     const uint32_t full = (1u << nl) - 1;
     Bx3            bx[7];
     for (int k = 0; k < nl; ++k) bx[k] = box_of(nodes, leaf[k]);
-    float   area[128], cost[128];
-    uint8_t part[128];
-    for (uint32_t s = 1; s <= full; ++s)
+    for (uint32_t s = lane + 1; s <= full; s += 32)
     {
         const int lo = __ffs(s) - 1;
         Bx3       u  = bx[lo];
@@ -484,63 +520,92 @@ __device__ void restructure_treelet(BvhNode* nodes, uint32_t n, uint32_t x)
                 u.lo = vmin(u.lo, bx[k].lo);
                 u.hi = vmax(u.hi, bx[k].hi);
             }
-        area[s] = half_area3(u);
+        t.area[s] = half_area3(u);
         if ((s & (s - 1)) == 0)
         {
-            cost[s] = area[s];
-            part[s] = 0;
-            continue;
+            t.cost[s] = t.area[s];
+            t.part[s] = 0;
         }
-        const uint32_t low  = s & (0u - s);
-        float          best = 0.f;
-        uint32_t       bp   = 0;
-        for (uint32_t p = (s - 1) & s; p; p = (p - 1) & s)
-        {
-            if (!(p & low)) continue;
-            const float c = cost[p] + cost[s ^ p];
-            if (bp == 0 || c < best)
-            {
-                best = c;
-                bp   = p;
-            }
-        }
-        cost[s] = area[s] + best;
-        part[s] = (uint8_t)bp;
     }
-    float cur = area[full];
-    for (int k = 1; k < ni; ++k) cur += half_area3(box_of(nodes, inner[k]));
-    for (int k = 0; k < nl; ++k) cur += la[k];
-    if (!(cost[full] < cur)) return;
-    uint32_t sset[6], sslot[6], order[6];
-    int      sp = 0, next = 1, no = 0;
-    sset[sp]    = full;
-    sslot[sp++] = x;
-    while (sp > 0)
+    __syncwarp();
+    for (int size = 2; size < nl; ++size)
     {
-        --sp;
-        const uint32_t s = sset[sp], slot = sslot[sp];
-        order[no++]      = slot;
-        const uint32_t sides[2] = {part[s], s ^ part[s]};
-        uint32_t       ch[2];
-        for (int k = 0; k < 2; ++k)
+        for (uint32_t s = lane + 1; s <= full; s += 32)
         {
-            const uint32_t t = sides[k];
-            if ((t & (t - 1)) == 0)
-                ch[k] = leaf[__ffs(t) - 1];
-            else
+            if (__popc(s) != size) continue;
+            float    best;
+            uint32_t bp;
+            best_split(t, s, 0, 1, best, bp);
+            t.cost[s] = t.area[s] + best;
+            t.part[s] = (uint8_t)bp;
+        }
+        __syncwarp();
+    }
+    {
+        // The whole treelet: lanes split its partitions, then reduce.
+        float    best;
+        uint32_t bp;
+        best_split(t, full, lane, 32, best, bp);
+        for (int o = 16; o; o >>= 1)
+        {
+            const float    ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint32_t op = __shfl_xor_sync(0xffffffffu, bp, o);
+            // Keep the first minimum in enumeration order: the smaller cost,
+            // or on equal cost the larger p (p decreases along the order).
+            if (op != 0 && (bp == 0 || ob < best || (ob == best && op > bp)))
             {
-                ch[k]       = inner[next++];
-                sset[sp]    = t;
-                sslot[sp++] = ch[k];
+                best = ob;
+                bp   = op;
             }
         }
-        __stcg(&nodes[slot].child0, ch[0]);
-        __stcg(&nodes[slot].child1, ch[1]);
-        __stcg(&nodes[ch[0]].parent, slot);
-        __stcg(&nodes[ch[1]].parent, slot);
+        if (lane == 0)
+        {
+            t.cost[full] = t.area[full] + best;
+            t.part[full] = (uint8_t)bp;
+        }
     }
-    __threadfence();
-    for (int k = no - 1; k >= 0; --k) store_child_boxes(nodes, order[k]);
+    __syncwarp();
+    if (lane == 0)
+    {
+        float cur = t.area[full];
+        for (int k = 1; k < ni; ++k) cur += half_area3(box_of(nodes, inner[k]));
+        for (int k = 0; k < nl; ++k) cur += la[k];
+        if (t.cost[full] < cur)
+        {
+            uint32_t sset[6], sslot[6], order[6];
+            int      sp = 0, next = 1, no = 0;
+            sset[sp]    = full;
+            sslot[sp++] = x;
+            while (sp > 0)
+            {
+                --sp;
+                const uint32_t s = sset[sp], slot = sslot[sp];
+                order[no++]      = slot;
+                const uint32_t sides[2] = {t.part[s], s ^ t.part[s]};
+                uint32_t       ch[2];
+                for (int k = 0; k < 2; ++k)
+                {
+                    const uint32_t u = sides[k];
+                    if ((u & (u - 1)) == 0)
+                        ch[k] = leaf[__ffs(u) - 1];
+                    else
+                    {
+                        ch[k]       = inner[next++];
+                        sset[sp]    = u;
+                        sslot[sp++] = ch[k];
+                    }
+                }
+                __stcg(&nodes[slot].child0, ch[0]);
+                __stcg(&nodes[slot].child1, ch[1]);
+                __stcg(&nodes[ch[0]].parent, slot);
+                __stcg(&nodes[ch[1]].parent, slot);
+            }
+            __threadfence();
+            for (int k = no - 1; k >= 0; --k) store_child_boxes(nodes, order[k]);
+            __threadfence();
+        }
+    }
+    __syncwarp();
 }
 
 // One restructure pass of every geometry: leaf threads climb; the second to
@@ -554,32 +619,67 @@ __global__ void __launch_bounds__(kBlk) k_batch_restructure(BatchArgs b, DeviceW
     const BuildItem& it  = b.items[r.g];
     const uint64_t   k64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
     const uint32_t   n   = it.n;
-    if (k64 >= n || n < 3) return;
-    BvhNode*  nodes = reinterpret_cast<BvhNode*>(it.result);
-    uint32_t* cnt   = reinterpret_cast<uint32_t*>(it.scratch + it.s_codes);  // free after emit: 2n-1 counts
-    const uint32_t leaf = n - 1 + (uint32_t)k64;
-    __stcg(&cnt[leaf], 1u);
-    uint32_t addr = __ldcg(&nodes[leaf].parent);
-    for (int level = 0; addr != kInvalid; ++level)
+    if (n < 3) return;  // block-uniform: a block covers one geometry
+    __shared__ TreeletDp dp[kBlk / 32];
+    TreeletDp&     tdp   = dp[threadIdx.x >> 5];
+    const uint32_t lane  = threadIdx.x & 31;
+    BvhNode*       nodes = reinterpret_cast<BvhNode*>(it.result);
+    uint32_t*      cnt   = reinterpret_cast<uint32_t*>(it.scratch + it.s_codes);  // free after emit: 2n-1 counts
+    // The warp climbs together: every round, each live lane takes one step
+    // up; then the warp restructures, one after another, the treelets of the
+    // lanes whose node qualified.
+    bool     alive = k64 < n;
+    uint32_t addr  = kInvalid;
+    if (alive)
     {
-        if (addr >= n - 1 || level > 96)
+        const uint32_t leaf = n - 1 + (uint32_t)k64;
+        __stcg(&cnt[leaf], 1u);
+        addr  = __ldcg(&nodes[leaf].parent);
+        alive = addr != kInvalid;
+    }
+    for (int level = 0; __any_sync(0xffffffffu, alive); ++level)
+    {
+        bool need = false;
+        if (alive)
         {
-            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
-            return;
+            if (addr >= n - 1 || level > 96)
+            {
+                atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+                alive = false;
+            }
+            else
+            {
+                __threadfence();
+                if (atomicExch(&nodes[addr].update, 1u) == 0u)
+                    alive = false;
+                else
+                {
+                    __threadfence();
+                    const uint32_t c0 = __ldcg(&nodes[addr].child0), c1 = __ldcg(&nodes[addr].child1);
+                    if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+                    {
+                        atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+                        alive = false;
+                    }
+                    else
+                    {
+                        const uint32_t c = __ldcg(&cnt[c0]) + __ldcg(&cnt[c1]);
+                        __stcg(&cnt[addr], c);
+                        need = c >= b.restructure_min;
+                    }
+                }
+            }
         }
-        __threadfence();
-        if (atomicExch(&nodes[addr].update, 1u) == 0u) return;
-        __threadfence();
-        const uint32_t c0 = __ldcg(&nodes[addr].child0), c1 = __ldcg(&nodes[addr].child1);
-        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+        for (uint32_t m = __ballot_sync(0xffffffffu, need); m; m &= m - 1)
         {
-            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
-            return;
+            const uint32_t x = __shfl_sync(0xffffffffu, addr, __ffs(m) - 1);
+            restructure_treelet_warp(nodes, n, x, tdp, lane);
         }
-        const uint32_t c = __ldcg(&cnt[c0]) + __ldcg(&cnt[c1]);
-        __stcg(&cnt[addr], c);
-        if (c >= b.restructure_min) restructure_treelet(nodes, n, addr);
-        addr = __ldcg(&nodes[addr].parent);
+        if (alive)
+        {
+            addr  = __ldcg(&nodes[addr].parent);
+            alive = addr != kInvalid;
+        }
     }
 }
 
