@@ -13,6 +13,8 @@ Reported (one JSON line on rank 0):
   latency_ms   p50 / p99 of the per-step (per-batch) latency of the chosen path
   e2e          the same metric through the C-ABI with pinned host buffers:
                H2D of the rays, trace, D2H of the hits inside the timed region
+               (one streamed launch that traces each chunk of rays as it lands
+               and whose hits are copied out part by part as they complete)
   roofline     algorithmic bytes of the chosen kernel per launch (ray + hit +
                node bytes x node fetches + 48 B x triangle fetches, counted by
                the kernel's own counters) / mean launch time, against the
@@ -70,7 +72,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-chunk", type=int, default=0, help="rays per pipelined chunk of the e2e run (0: 2^21)")
+    ap.add_argument("--e2e-chunk", type=int, default=0,
+                    help="rays per copy-in chunk of the e2e run (0: the library's default, 2^17)")
     ap.add_argument("--quality", type=int, default=1,
                     help="1: the chosen path traces a quality build (treelet restructure); 0: the fast build")
     ap.add_argument("--only", default="", help="profiling aid: 'chosen' or 'plain' runs only that kernel")
@@ -400,8 +403,9 @@ def run_ours(args):
         e2e = {"value": R * ws * args.steps / (total_e / 1e3) / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": int(rays_h.numel() * 4), "d2h_bytes_per_step": int(hits_h.numel() * 4),
                "ms_per_step": total_e / args.steps,
-               "api": "rrCudaCmdIntersectHostBuffers (pinned host rays/hits, chunks of "
-                      f"{args.e2e_chunk or 2 ** 21:,} rays over 3 streams)"}
+               "api": "rrCudaCmdIntersectHostBuffers (pinned host rays/hits; one streamed persistent launch: "
+                      f"rays copied in chunks of {args.e2e_chunk or 2 ** 17:,}, hits copied out in parts of 4 "
+                      "chunks as they complete)"}
         e2e_hits = hits_h.numpy().view(np.uint32)
         e2e["hits_identical_to_device_run"] = bool(np.array_equal(e2e_hits, out["chosen"]["hits"])) \
             if "chosen" in out else None

@@ -185,10 +185,18 @@ RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
 
 /* Intersect rays that live in host memory (no counterpart in the reference
  * API, whose rrCmdIntersect takes device buffers, radeonrays.h:391-400).
- * The rays are cut into chunks of `chunk_rays` (0 = 2^21), and each chunk is
- * copied in, traced and its hits copied out on one of three CUDA streams
- * owned by the context.  The copies of one chunk overlap the traversal of the
- * others, so the host transfers hide behind the kernels.
+ * Two plans, with the same hits:
+ *   streamed (2^16 rays or more, persistent binary traversal, the default):
+ *     one kernel launch over all rays; the rays are copied in chunks of
+ *     `chunk_rays` (rounded down to a power of two; 0 = 2^17) on a context
+ *     stream that raises a flag per chunk, the kernel traces each chunk once
+ *     its flag is up, and a second context stream copies the hits out in
+ *     parts of four chunks as each part's rays are all written (stream
+ *     memory operations: cuStreamWriteValue32 / cuStreamWaitValue32);
+ *   chunked (otherwise, inside a stream capture, or RR_CUDA_STREAM_RAYS=0):
+ *     chunks of `chunk_rays` (0 = 2^21), each copied in, traced and copied
+ *     out on one of three context streams.
+ * Either way the host transfers overlap the traversal.
  *   host_rays   RRRay[ray_count] in host memory (page-locked for overlap)
  *   host_hits   RRHit[ray_count] (or uint32_t for INSTANCE_ID) in host memory
  *   rays, hits  device buffers of ray_count records (staging)

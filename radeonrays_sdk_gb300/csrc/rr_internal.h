@@ -225,7 +225,8 @@ SceneLayout scene_layout(uint32_t n);
 struct DeviceWords
 {
     uint32_t error_bits;
-    uint32_t pad[3];
+    uint32_t probe;  // written by the stream memory-operation probe
+    uint32_t pad[2];
     unsigned long long rays;
     unsigned long long node_fetches;
     unsigned long long tri_fetches;
@@ -289,7 +290,26 @@ struct TraceArgs
     int             blocks_per_sm;
     int             sm_count;
     int             box_leaves;   // AABB-list geometry: leaves are boxes
+    // Streamed rays (host-buffer tracing, persistent binary kernel only): the
+    // rays arrive in chunks of 2^stream_shift while the kernel runs, and the
+    // hits leave in parts of 2^stream_part_shift rays (a part is a whole
+    // number of chunks).
+    // stream_words[c] turns non-zero when chunk c is in device memory;
+    // stream_words[stream_chunks + p] counts part p's finished rays;
+    // stream_words[stream_chunks + stream_parts] is set when a lane gave up
+    // waiting for a chunk.
+    uint32_t*       stream_words;
+    uint32_t        stream_shift;
+    uint32_t        stream_chunks;
+    uint32_t        stream_part_shift;
+    uint32_t        stream_parts;
 };
+// Words of a streamed trace (arrival flags, done counters, give-up flag),
+// rounded up to 256 bytes.
+inline size_t stream_words_bytes(uint32_t chunks, uint32_t parts)
+{
+    return ((size_t)(chunks + parts + 1) * 4 + 255) / 256 * 256;
+}
 // One request of a multi-request traversal launch (rrCudaCmdIntersectBatch).
 constexpr uint32_t kReqAny   = 1;  // any-hit query (else closest)
 constexpr uint32_t kReqFull  = 2;  // full RRHit output (else instance id)

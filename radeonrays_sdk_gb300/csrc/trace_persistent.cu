@@ -12,13 +12,148 @@
 // idle while its longest ray finishes; refilling keeps them working.  The
 // stack is a short stack in shared memory (interleaved across the block) that
 // spills to a per-thread region of the caller's scratch buffer.
+//
+// Streamed variant (kStream, host-buffer tracing): one launch over all rays
+// while the copy engine is still bringing them in.  Rays are taken in index
+// order, so a warp only waits (bounded, once per chunk) for the arrival flag
+// of the last chunk its new rays lie in, which the copy stream sets after
+// that chunk's copy.  Each finished ray is counted in the done counter of
+// its part (a copy-out unit of several chunks; release adds, batched per
+// warp and part), and the copy-out stream waits for each counter before it
+// copies that part's hits to the host.  Every claimed ray is counted exactly
+// once, whether it was traced, missed an empty geometry, or gave up waiting,
+// and the last counts are published before the warp exits, so every counter
+// reaches its part's size when the kernel ends.
 #include "trace_persistent.cuh"
 
 namespace rr
 {
 namespace
 {
-template <bool kAny, bool kFull, bool kStats, bool kBox>
+// Bounded wait for a chunk's arrival flag: about 2^21 polls of ~1 us.  After
+// one lane has given up (the copy never landed), every later wait fails at
+// once, so a stuck copy costs one timeout, not one per ray.
+//
+// The polls are relaxed loads, not acquire loads: an acquire at gpu scope
+// would drop the SM's L1 (and with it the cached upper tree levels) each
+// time.  Ordering rests on three facts: the flag is written by the copy
+// stream after the chunk's copy with a system-wide fence before it; the ray
+// loads are control-dependent on the flag value (issued only after it
+// returned); and they are L2 loads (ld.cg), so no stale L1 line can serve
+// them.  Chunks arrive in order, so a warp that saw chunk c need not check
+// any chunk <= c again.
+constexpr uint32_t kArrivalPolls = 1u << 21;
+
+// Highest chunk known to have arrived, starting the search at chunk `hi`
+// (not yet known): flags are read four at a time (the words are 256-byte
+// aligned), so one poll usually also covers the next few chunks, which the
+// copy stream has landed by then.  Returns -1 if chunk `hi` never arrived.
+__device__ __noinline__ int wait_arrival(const TraceArgs& a, uint32_t hi)
+{
+    const uint32_t  g       = hi & ~3u;
+    const uint4*    quad    = reinterpret_cast<const uint4*>(a.stream_words + g);
+    const uint32_t* gave_up = a.stream_words + a.stream_chunks + a.stream_parts;
+    for (uint32_t k = 0; k < kArrivalPolls; ++k)
+    {
+        uint4 f;
+        asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                     : "=r"(f.x), "=r"(f.y), "=r"(f.z), "=r"(f.w)
+                     : "l"(quad)
+                     : "memory");
+        const uint32_t got[4] = {f.x, f.y, f.z, f.w};
+        if (got[hi - g])
+        {
+            // Chunks arrive in order: the highest set flag of the quad (at
+            // most the last chunk) bounds every chunk below it.
+            int top = (int)hi;
+            for (uint32_t j = hi - g + 1; j < 4 && g + j < a.stream_chunks; ++j)
+                if (got[j]) top = (int)(g + j);
+            return top;
+        }
+        uint32_t stop;
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(stop) : "l"(gave_up) : "memory");
+        if (stop) return -1;
+        __nanosleep(1000);
+    }
+    atomicExch(const_cast<uint32_t*>(gave_up), 1u);
+    raise_error(a.words, RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT);
+    return -1;
+}
+
+// Chunk c's done counter += v, ordered after every hit write of the warp's
+// lanes that passed an earlier __syncwarp (release at gpu scope).  Out of
+// line, like wait_arrival: rarely run, and kept out of the loop's code.
+__device__ __noinline__ void add_release(uint32_t* p, uint32_t v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Done counts of a warp: rays finished in the part (copy-out unit, several
+// arrival chunks) the warp is claiming from (cur) and in the one before it
+// (prev), not yet added to the parts' done counters.  `prev` is published
+// when the warp's claims move on to a later part, both at exit; a ray of any
+// other part (a straggler) is added at once.  A release add waits until the
+// SM's earlier stores are visible, which costs microseconds, so a warp
+// issues one about once per part it works on, not at every refill.  The
+// counts live in shared memory (one record per warp, written by lane 0 only)
+// so that no register stays live across the traversal step for them.
+struct DoneCounts
+{
+    uint32_t cur_c, cur_n, prev_c, prev_n;
+};
+
+// Rays finished at this refill (`fin`, part `c`); all 32 lanes call it,
+// after their hits are written.
+__device__ __forceinline__ void note_done(const TraceArgs& a, bool fin, uint32_t c, uint32_t lane,
+                                          volatile DoneCounts& d)
+{
+    if (!__ballot_sync(0xffffffffu, fin)) return;
+    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c;
+    const uint32_t in_cur  = __ballot_sync(0xffffffffu, fin && c == cur_c);
+    const uint32_t in_prev = __ballot_sync(0xffffffffu, fin && c == prev_c && prev_c != cur_c);
+    if (lane == 0)
+    {
+        d.cur_n  = d.cur_n + __popc(in_cur);
+        d.prev_n = d.prev_n + __popc(in_prev);
+    }
+    if (fin && !(((in_cur | in_prev) >> lane) & 1u)) add_release(a.stream_words + a.stream_chunks + c, 1u);
+    __syncwarp();
+}
+
+// The warp's claims reached part `hi` (warp-uniform): publish `prev` and
+// shift.  The counted hits were written before the loop's __syncwarp.
+__device__ __forceinline__ void advance_done(const TraceArgs& a, uint32_t hi, uint32_t lane, volatile DoneCounts& d)
+{
+    if (lane != 0 || hi <= d.cur_c) return;
+    if (d.prev_n) add_release(a.stream_words + a.stream_chunks + d.prev_c, d.prev_n);
+    d.prev_c = d.cur_c;
+    d.prev_n = d.cur_n;
+    d.cur_c  = hi;
+    d.cur_n  = 0;
+}
+
+// Publish both open counts (lane 0); after a __syncwarp that follows the
+// counted hits' writes.
+__device__ __forceinline__ void publish_done(const TraceArgs& a, uint32_t lane, volatile DoneCounts& d)
+{
+    if (lane == 0)
+    {
+        if (d.cur_n) add_release(a.stream_words + a.stream_chunks + d.cur_c, d.cur_n);
+        if (d.prev_n && d.prev_c != d.cur_c) add_release(a.stream_words + a.stream_chunks + d.prev_c, d.prev_n);
+        d.cur_n = d.prev_n = 0;
+    }
+}
+
+// A streamed ray's 32 bytes, read through L2 only: a neighbouring chunk may
+// share a sector with it and must not be served stale from L1.
+__device__ __forceinline__ Ray load_ray_cg(const uint8_t* rays, uint32_t i)
+{
+    const float4* p = reinterpret_cast<const float4*>(rays) + 2ull * i;
+    const float4  x = __ldcg(p), y = __ldcg(p + 1);
+    return Ray{f3(x.x, x.y, x.z), x.w, f3(y.x, y.y, y.z), y.w};
+}
+
+template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, uint32_t gcap)
 {
     __shared__ uint32_t s_stack[kPBlock * kPShort];
@@ -37,6 +172,17 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
     PRay     s;
     uint32_t gid = kInvalid, nf = 0;
     bool     active = false, pending = false, exhausted = false;
+    // kStream: the block's highest chunk known to have arrived, and each
+    // warp's done-count slots (shared memory).
+    __shared__ int        s_seen;
+    __shared__ DoneCounts s_dc[kPBlock / 32];
+    volatile DoneCounts&  dc = s_dc[threadIdx.x >> 5];
+    if (kStream)
+    {
+        if (threadIdx.x == 0) s_seen = -1;
+        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = 0;
+        __syncthreads();
+    }
     for (;;)
     {
         __syncwarp();
@@ -45,6 +191,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
         if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
         {
+            int seen = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
             const uint32_t n    = exhausted ? 0u : __popc(idle);
             uint32_t       base = 0;
             if (n)
@@ -53,7 +200,28 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                 if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
                 base      = __shfl_sync(0xffffffffu, base, leader);
                 exhausted = base + n >= count;
+                if (kStream && base < count)
+                {
+                    // The warp's new rays end in chunk `hi`: known to the
+                    // block already, or waited for (once per block and chunk).
+                    const int hi = (int)((min(base + n, count) - 1u) >> a.stream_shift);
+                    int top = -1;
+                    if ((int)lane == leader)
+                    {
+                        top = *reinterpret_cast<volatile int*>(&s_seen);
+                        if (top < hi)
+                        {
+                            top = wait_arrival(a, (uint32_t)hi);
+                            if (top >= 0) atomicMax(&s_seen, top);
+                        }
+                    }
+                    seen = __shfl_sync(0xffffffffu, top, leader);
+                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, lane, dc);
+                    __syncwarp();
+                }
             }
+            bool     fin   = false;
+            uint32_t fin_c = 0;
             if (!active)
             {
                 if (pending)
@@ -75,12 +243,31 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
                     }
                     pending = false;
+                    fin     = true;
+                    fin_c   = gid >> a.stream_part_shift;
                 }
                 const uint32_t my = base + __popc(idle & lt);
                 if (n && my < count)
                 {
                     gid = my;
-                    if (a.empty)
+                    if (kStream)
+                    {
+                        // Traced once its chunk is in; an empty geometry or a
+                        // chunk that never arrived finishes as a miss at the
+                        // next refill, where it is counted like any other.
+                        if (!a.empty && (int)(gid >> a.stream_shift) <= seen)
+                        {
+                            active = true;
+                            nf     = 0;
+                            p_start(s, load_ray_cg(a.rays, gid));
+                        }
+                        else
+                        {
+                            s.caddr = kInvalid;
+                            pending = true;
+                        }
+                    }
+                    else if (a.empty)
                         write_miss<kFull>(a.hits, gid);
                     else
                     {
@@ -90,6 +277,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                     }
                 }
             }
+            if (kStream) note_done(a, fin, fin_c, lane, dc);
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
@@ -99,12 +287,17 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
             pending = true;
         }
     }
+    if (kStream)
+    {
+        __syncwarp();  // the break above is warp-uniform; order the last hits before their counts
+        publish_done(a, lane, dc);
+    }
 }
 
-template <bool kAny, bool kFull, bool kStats, bool kBox>
+template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream>
 cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 {
-    auto kern   = k_trace_persistent<kAny, kFull, kStats, kBox>;
+    auto kern   = k_trace_persistent<kAny, kFull, kStats, kBox, kStream>;
     int  per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {
@@ -121,7 +314,13 @@ cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 template <bool kAny, bool kFull, bool kStats>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
-    return a.box_leaves ? go2<kAny, kFull, kStats, true>(a, s) : go2<kAny, kFull, kStats, false>(a, s);
+    return a.box_leaves ? go2<kAny, kFull, kStats, true, false>(a, s) : go2<kAny, kFull, kStats, false, false>(a, s);
+}
+
+template <bool kAny, bool kFull>
+cudaError_t go_stream(const TraceArgs& a, cudaStream_t s)
+{
+    return a.box_leaves ? go2<kAny, kFull, false, true, true>(a, s) : go2<kAny, kFull, false, false, true>(a, s);
 }
 }  // namespace
 
@@ -129,6 +328,11 @@ cudaError_t launch_trace_persistent(const TraceArgs& a, cudaStream_t s)
 {
     if (a.ray_count == 0) return cudaSuccess;
     const bool any = a.query == RR_INTERSECT_QUERY_ANY, full = a.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT;
+    if (a.stream_words)
+    {
+        if (any) return full ? go_stream<true, true>(a, s) : go_stream<true, false>(a, s);
+        return full ? go_stream<false, true>(a, s) : go_stream<false, false>(a, s);
+    }
     if (a.collect_stats)
     {
         if (any) return full ? go<true, true, true>(a, s) : go<true, false, true>(a, s);

@@ -41,9 +41,9 @@ struct PStack
     __device__ __forceinline__ uint32_t& at(int k) const { return s[k * kPBlock]; }
 };
 
-__device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i)
+__device__ __forceinline__ void p_start(PRay& s, const Ray& r)
 {
-    s.ray   = load_ray(rays, i);
+    s.ray   = r;
     s.inv   = safe_invdir(s.ray.d);
     s.oxi   = f3(-s.ray.o.x * s.inv.x, -s.ray.o.y * s.inv.y, -s.ray.o.z * s.inv.z);
     s.ct    = s.ray.tmax;
@@ -52,6 +52,7 @@ __device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i
     s.gsp = s.steps = 0;
     s.sp            = 0;
 }
+__device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i) { p_start(s, load_ray(rays, i)); }
 
 // One iteration of the reference's traversal loop.  Returns true when the ray
 // is finished (stack empty, or a hit accepted by an any-hit query).  The
