@@ -98,34 +98,20 @@ __device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
     return n;
 }
 
-constexpr uint32_t kLeafMax = 1;  // triangles per leaf slot (2-bit count in the meta byte)
-
-// Leaves (binary leaf node indices, left to right) of the subtree at `root`,
-// stopping as soon as there are more than kLeafMax; returns their count or
-// kLeafMax + 1.
-__device__ __forceinline__ uint32_t collect_leaves(const BvhNode* nodes, uint32_t root, uint32_t* out)
+// Box of child slot 0 (a0 / a1) or 1 (b0 / b1) of a binary internal node: the
+// refit wrote the exact union of the child's boxes (or its triangle's box)
+// there, so the collapse reads child boxes from the parent and loads a node
+// only to expand it.
+__device__ __forceinline__ Bx child_box(const BvhNode& nd, int side)
 {
-    uint32_t stack[kLeafMax + 1];
-    int      sp  = 0;
-    uint32_t cnt = 0;
-    stack[sp++]  = root;
-    while (sp > 0)
+    Bx r;
+    for (int k = 0; k < 3; ++k)
     {
-        const uint32_t a  = stack[--sp];
-        const uint32_t c0 = __ldg(&nodes[a].child0);
-        if (c0 == kInvalid)
-        {
-            if (cnt == kLeafMax) return kLeafMax + 1;
-            out[cnt++] = a;
-            continue;
-        }
-        if (sp + 2 > (int)kLeafMax + 1) return kLeafMax + 1;
-        stack[sp++] = __ldg(&nodes[a].child1);
-        stack[sp++] = c0;
+        r.lo[k] = side ? nd.b0[k] : nd.a0[k];
+        r.hi[k] = side ? nd.b1[k] : nd.a1[k];
     }
-    return cnt;
+    return r;
 }
-
 
 // Exponent e (biased) of the smallest power of two s with ceil(ext / s) <= 255.
 __device__ __forceinline__ int pick_exp(float lo, float hi)
@@ -294,17 +280,19 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
         Item       item{0, 0};
         if (active)
         {
+            // Binary layout: internal nodes [0, n-2], leaves [n-1, 2n-2], so
+            // a child's kind follows from its index; each expansion of the
+            // largest internal child is one node load.
+            const uint32_t first_leaf = bi->n - 1;
             item          = qin[local];
             BvhNode root  = load_node(nodes, item.b);
             ch[0]         = root.child0;
             ch[1]         = root.child1;
+            cb[0]         = child_box(root, 0);
+            cb[1]         = child_box(root, 1);
+            cint[0]       = ch[0] < first_leaf;
+            cint[1]       = ch[1] < first_leaf;
             nc            = 2;
-            for (int k = 0; k < 2; ++k)
-            {
-                BvhNode c = load_node(nodes, ch[k]);
-                cb[k]     = node_union(c);
-                cint[k]   = c.child0 != kInvalid;
-            }
             while (nc < 8)
             {
                 int   best = -1;
@@ -320,34 +308,20 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
                         }
                     }
                 if (best < 0) break;
-                BvhNode  nd = load_node(nodes, ch[best]);
-                uint32_t l = nd.child0, r = nd.child1;
-                BvhNode  ln = load_node(nodes, l), rn = load_node(nodes, r);
-                ch[best]   = l;
-                cb[best]   = node_union(ln);
-                cint[best] = ln.child0 != kInvalid;
-                ch[nc]     = r;
-                cb[nc]     = node_union(rn);
-                cint[nc]   = rn.child0 != kInvalid;
+                const BvhNode nd = load_node(nodes, ch[best]);
+                ch[best]   = nd.child0;
+                cb[best]   = child_box(nd, 0);
+                cint[best] = nd.child0 < first_leaf;
+                ch[nc]     = nd.child1;
+                cb[nc]     = child_box(nd, 1);
+                cint[nc]   = nd.child1 < first_leaf;
                 ++nc;
             }
         }
-        // Leaf clusters: an internal child left over with at most kLeafMax
-        // triangles becomes one leaf slot holding them (a wide node for it
-        // would cost a fetch for a few triangle slots).
-        uint32_t ctri[8][kLeafMax];
+        // Leaf slots hold one triangle each (the meta byte's count field
+        // allows up to 3; one measured fastest).
         uint32_t ccnt[8];
-        for (int k = 0; k < nc; ++k)
-        {
-            if (!cint[k])
-            {
-                ctri[k][0] = ch[k];
-                ccnt[k]    = 1;
-                continue;
-            }
-            ccnt[k] = collect_leaves(nodes, ch[k], ctri[k]);
-            if (ccnt[k] <= kLeafMax) cint[k] = false;
-        }
+        for (int k = 0; k < nc; ++k) ccnt[k] = cint[k] ? 0u : 1u;
         uint32_t n_int = 0, n_leaf = 0;
         for (int k = 0; k < nc; ++k)
         {
@@ -448,7 +422,7 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
                     w.meta[slot] = (uint8_t)((ccnt[k] << 5) | rl);
                     for (uint32_t j = 0; j < ccnt[k]; ++j)
                     {
-                        BvhNode lf = load_node(nodes, ctri[k][j]);
+                        BvhNode lf = load_node(nodes, ch[k]);
                         WideTri t;
                         t.v0[0] = lf.a0[0];
                         t.v0[1] = lf.a0[1];
