@@ -83,6 +83,18 @@ __device__ __forceinline__ void tri_verts(const BuildItem& m, uint32_t t, F3& a,
     c = vtx(m, i2);
 }
 
+// The climb's arrival flag: exchange with acquire-release semantics at gpu
+// scope.  The release half publishes this thread's stores below the node
+// (its child's boxes) before the flag; the acquire half, for the second
+// arriver, makes the partner's stores visible to the loads that follow.
+// One ordered atomic replaces a fence on either side of a relaxed exchange.
+__device__ __forceinline__ uint32_t climb_exch(uint32_t* flag)
+{
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(flag), "r"(1u) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ uint32_t expand_bits(uint32_t r)
 {
     r = (r * 0x00010001u) & 0xFF0000FFu;
@@ -649,12 +661,10 @@ __global__ void __launch_bounds__(kBlk) k_batch_restructure(BatchArgs b, DeviceW
             }
             else
             {
-                __threadfence();
-                if (atomicExch(&nodes[addr].update, 1u) == 0u)
+                if (climb_exch(&nodes[addr].update) == 0u)
                     alive = false;
                 else
                 {
-                    __threadfence();
                     const uint32_t c0 = __ldcg(&nodes[addr].child0), c1 = __ldcg(&nodes[addr].child1);
                     if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
                     {
@@ -723,9 +733,7 @@ __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, ui
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
             return;
         }
-        __threadfence();
-        if (atomicExch(&nodes[addr].update, 1u) == 0u) return;
-        __threadfence();
+        if (climb_exch(&nodes[addr].update) == 0u) return;
         BvhNode*       nd = nodes + addr;
         const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
         if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
