@@ -57,7 +57,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "incoherent closest-hit Mrays/s + p99 batch latency, chosen vs plain on same GB300"
 # RRCudaTraversal value -> kernel name (the key of profiles/traffic.json)
-KERNELS = {1: "k_trace_binary", 2: "k_trace_wide", 3: "k_trace_persistent"}
+KERNELS = {1: "k_trace_binary", 2: "k_trace_wide", 3: "k_trace_persistent", 4: "k_trace_bvh4"}
 
 
 def parse():
@@ -92,9 +92,11 @@ def parse():
     ap.add_argument("--slots", type=int, default=3)
     ap.add_argument("--slot-rays", type=int, default=1 << 22)
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0)
+    ap.add_argument("--chosen-format", default="bvh4", choices=["wide8", "bvh4"],
+                    help="node format of the chosen path's tree (the binary nodes are always there)")
     ap.add_argument("--chosen", type=int, default=0,
-                    help="chosen traversal: 0 autotuned (rrCudaAutotuneTraversal), 2 wide (8-wide nodes), "
-                         "3 binary persistent")
+                    help="chosen traversal: 0 autotuned (rrCudaAutotuneTraversal), 2 wide (8-wide nodes, "
+                         "--chosen-format wide8), 3 binary persistent, 4 4-wide fp32 nodes (--chosen-format bvh4)")
     return ap.parse_args()
 
 
@@ -193,9 +195,10 @@ def describe(args, ntri):
                         "rays per GPU (origins uniform in the mesh box, directions uniform on the sphere), "
                         "closest hit, full RRHit output",
             "triangles": ntri, "rays_per_gpu": args.rays, "query": "closest", "output": "full_hit",
-            "chosen": "autotuned (rrCudaAutotuneTraversal) among: plain binary, persistent lane-refill binary "
-                      "(reference visit order), persistent 8-wide nodes with 8-bit conservative child bounds "
-                      "(rays in given or sorted order)",
+            "chosen": "autotuned (rrCudaAutotuneTraversal) among the kernels the chosen tree's format allows: "
+                      "plain binary, persistent lane-refill binary (reference visit order), and persistent 4-wide "
+                      f"fp32 nodes (format bvh4) or 8-wide 8-bit nodes (format wide8); format here: "
+                      f"{args.chosen_format}",
             "plain": "64-byte binary nodes, one thread per ray, reference visit order",
             "l2": "inputs larger than L2 (rays 32 B x rays, BVH > 129 MB); no flush needed",
             "parallelism": "replicas (rays sharded per GPU, BVH replicated)"}
@@ -329,12 +332,16 @@ def run_ours(args):
     # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
     # LBVH + treelet restructure); the plain path the reference's fast LBVH.
     bvh_c = bvh
-    if args.quality:
-        bvh_c = torch.empty(r_bytes, dtype=torch.uint8, device="cuda")
+    cfmt = rr.RR_CUDA_NODE_FORMAT_BVH4 if args.chosen_format == "bvh4" else rr.RR_CUDA_NODE_FORMAT_WIDE8
+    if args.quality or cfmt != rr.RR_CUDA_NODE_FORMAT_WIDE8:
+        cs_bytes, cr_bytes = ctx.geometry_requirements(ntri, cfmt, 30, v.shape[0], 12)
+        bvh_c = torch.empty(cr_bytes, dtype=torch.uint8, device="cuda")
+        scratch_c = scratch_b if cs_bytes <= scratch_b.numel() else torch.empty(cs_bytes, dtype=torch.uint8,
+                                                                                  device="cuda")
 
         def qbuild_step():
-            ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_WIDE8, stream=ext, scratch=scratch_b,
-                               result=bvh_c, quality=True)
+            ctx.build_geometry(v_d, i_d, node_format=cfmt, stream=ext, scratch=scratch_c, result=bvh_c,
+                               quality=bool(args.quality))
             ctx.release_ptrs()
         q_per, _ = time_steps(qbuild_step, 3, 1, 1, stream)
         build["quality"] = {"ms": statistics.median(q_per), "mtris_s": ntri / statistics.median(q_per) / 1e3,
@@ -373,7 +380,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         st = ctx.stats()
         ctx.set_traversal(trav, *shape, ray_order=order)
-        node_b = 80 if trav == rr.RR_CUDA_TRAVERSAL_WIDE else 64
+        # Bytes per fetch: binary node 64; 8-wide node 80 (+ 48-byte triangles);
+        # 4-wide node 128 (+ the 48 bytes of a binary leaf's three vertices).
+        node_b = {rr.RR_CUDA_TRAVERSAL_WIDE: 80, rr.RR_CUDA_TRAVERSAL_BVH4: 128}.get(trav, 64)
         alg = R * (32 + 16) + st["node_fetches"] * node_b + st["triangle_fetches"] * 48
         clocks = Clocks(local)
         with clocks:

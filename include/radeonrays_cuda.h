@@ -27,12 +27,15 @@ typedef enum
     /* Binary 64-byte nodes in the reference layout only ("plain" path). */
     RR_CUDA_NODE_FORMAT_BINARY = 0,
     /* Binary nodes plus 8-wide nodes with 8-bit conservatively quantised child
-     * bounds and a 48-byte triangle array (the default). */
-    RR_CUDA_NODE_FORMAT_WIDE8 = 1
+     * bounds and a 48-byte triangle array. */
+    RR_CUDA_NODE_FORMAT_WIDE8 = 1,
+    /* Binary nodes plus 4-wide 128-byte nodes with exact fp32 child boxes
+     * whose leaf children are the binary leaf nodes (the default). */
+    RR_CUDA_NODE_FORMAT_BVH4 = 2
 } RRCudaNodeFormat;
 
 /* Passed through RRBuildOptions::backend_specific_info.  A null
- * backend_specific_info selects the defaults (WIDE8, 30-bit Morton codes). */
+ * backend_specific_info selects the defaults (BVH4, 30-bit Morton codes). */
 typedef struct
 {
     uint32_t struct_size;   /* sizeof(RRCudaBuildOptions) */
@@ -54,7 +57,10 @@ typedef enum
     RR_CUDA_TRAVERSAL_WIDE = 2,
     /* Persistent warp-scheduled kernel over the binary nodes, reference visit
      * order (hits bit-identical to RR_CUDA_TRAVERSAL_BINARY). */
-    RR_CUDA_TRAVERSAL_BINARY_PERSISTENT = 3
+    RR_CUDA_TRAVERSAL_BINARY_PERSISTENT = 3,
+    /* Persistent warp-scheduled kernel over the 4-wide fp32 nodes of an
+     * RR_CUDA_NODE_FORMAT_BVH4 buffer, nearest child first. */
+    RR_CUDA_TRAVERSAL_BVH4 = 4
 } RRCudaTraversal;
 
 typedef struct
@@ -131,11 +137,12 @@ RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
 /* Pick the fastest traversal for a workload and make it this context's
  * traversal option (no reference counterpart: the reference has one kernel
  * per query variant).  Times every applicable kernel -- plain binary, binary
- * persistent, 8-wide with the rays in the given order and, for batches of
- * 2^20 rays or more, 8-wide with the rays sorted -- on the caller's rays
- * (their count is the sample size), three runs each on the context's stream,
- * and keeps the fastest.  Results are cached per (GPU, buffer kind and size,
- * query, output, ray-count octave) in the context and, when the environment
+ * persistent, and by the buffer's format 4-wide (BVH4) or 8-wide with the
+ * rays in the given order and, for batches of 2^20 rays or more, with the
+ * rays sorted (WIDE8) -- on the caller's rays (their count is the sample
+ * size), three runs each on the context's stream, and keeps the fastest.
+ * Results are cached per (GPU, buffer kind, node format and size, query,
+ * output, ray-count octave) in the context and, when the environment
  * variable RR_CUDA_TUNE_CACHE names a file, in that file across processes.
  * Synchronous; hits and scratch (rrGetTraceMemoryRequirements(ray_count))
  * are overwritten.  `chosen` (optional) receives the selection. */
@@ -186,7 +193,8 @@ RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
 /* Intersect rays that live in host memory (no counterpart in the reference
  * API, whose rrCmdIntersect takes device buffers, radeonrays.h:391-400).
  * Two plans, with the same hits:
- *   streamed (2^16 rays or more, persistent binary traversal, the default):
+ *   streamed (2^16 rays or more with the persistent binary traversal, the
+ *     default, or the 4-wide traversal):
  *     one kernel launch over all rays; the rays are copied in chunks of
  *     `chunk_rays` (rounded down to a power of two; 0 = 2^17) on a context
  *     stream that raises a flag per chunk, the kernel traces each chunk once

@@ -85,6 +85,7 @@ struct BufInfo
     uint32_t n      = 0;
     uint32_t format = RR_CUDA_NODE_FORMAT_BINARY;
     size_t   trailer_off = 0, wide_off = 0, tris_off = 0, xforms_off = 0, inst_off = 0;
+    size_t   wide_capacity = 0;  // geometry: 8-wide or 4-wide node capacity
     bool     scene_wide = false;
     uint32_t prim_kind  = kPrimTriangles;  // geometry: triangles or AABB list
 };
@@ -377,7 +378,7 @@ void record(CommandStream* cs, Op op, bool owns = false)
 
 struct BuildParams
 {
-    uint32_t format      = RR_CUDA_NODE_FORMAT_WIDE8;
+    uint32_t format      = RR_CUDA_NODE_FORMAT_BVH4;
     uint32_t bits        = 30;
     bool     restructure = false;
 };
@@ -392,7 +393,9 @@ bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
     if (!o || !o->backend_specific_info) return true;
     const RRCudaBuildOptions* c = reinterpret_cast<const RRCudaBuildOptions*>(o->backend_specific_info);
     if (c->struct_size < sizeof(RRCudaBuildOptions)) return false;
-    if (c->node_format != RR_CUDA_NODE_FORMAT_BINARY && c->node_format != RR_CUDA_NODE_FORMAT_WIDE8) return false;
+    if (c->node_format != RR_CUDA_NODE_FORMAT_BINARY && c->node_format != RR_CUDA_NODE_FORMAT_WIDE8 &&
+        c->node_format != RR_CUDA_NODE_FORMAT_BVH4)
+        return false;
     if (c->morton_bits != 0 && c->morton_bits != 30 && c->morton_bits != 63) return false;
     bp.format = c->node_format;
     bp.bits   = c->morton_bits == 63 ? 63 : 30;
@@ -474,6 +477,7 @@ void register_geometry(Context* ctx, const PendingGeom& pg)
     bi.trailer_off                      = pg.L.trailer_off;
     bi.wide_off                         = pg.L.wide_off;
     bi.tris_off                         = pg.L.tris_off;
+    bi.wide_capacity                    = pg.L.wide_capacity;
     bi.prim_kind                        = pg.ma.prim_kind;
     ctx->registry[(uintptr_t)pg.result] = bi;
 }
@@ -640,8 +644,8 @@ struct StreamPlan
 
 // The launch of one rrCmdIntersect: arguments from the buffers and the
 // traversal options, kernel chosen by the buffer kind and options.  With a
-// stream plan, returns an empty Op unless the persistent binary kernel would
-// run (the only kernel with a streamed variant).
+// stream plan, returns an empty Op unless the persistent binary or the
+// 4-wide kernel would run (the kernels with a streamed variant).
 Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count, const uint32_t* indirect, void* hits,
             uint8_t* scratch, int query, int output, const RRCudaTraversalOptions& o,
             const StreamPlan* sp = nullptr)
@@ -707,6 +711,22 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         }
         return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
     }
+    if (trav == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0)
+    {
+        a.bvh4_nodes = reinterpret_cast<const Bvh4Node*>(bvh + bi.wide_off);
+        a.wide_limit = (uint32_t)bi.wide_capacity;
+        if (sp)
+        {
+            if (a.collect_stats || a.indirect) return Op();
+            a.stream_words      = sp->words;
+            a.stream_shift      = sp->shift;
+            a.stream_chunks     = sp->chunks;
+            a.stream_part_shift = sp->part_shift;
+            a.stream_parts      = sp->parts;
+            a.scratch_bytes     = sp->scratch_bytes;
+        }
+        return [=](cudaStream_t s) { return launch_trace_bvh4(a, s); };
+    }
     if (sp) return Op();
     if (has_wide && trav == RR_CUDA_TRAVERSAL_WIDE)
     {
@@ -720,7 +740,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
 
 // Host-buffer trace as one persistent launch over all rays (empty Op when the
 // plan does not apply: fewer than 2^16 rays, no stream memory operations, or
-// a traversal other than the persistent binary kernel).  On stream s:
+// a traversal other than the persistent binary or 4-wide kernel).  On stream s:
 //   s:        clear the words, fork;
 //   pipe[0]:  per chunk, copy its rays in, then set its arrival flag;
 //   s:        the streamed kernel (waits, bounded, for each chunk's flag);
@@ -963,7 +983,8 @@ RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_bu
         if (t.magic != kMagic || t.version != kVersion || t.kind != kKindGeom || t.leaf_count != n ||
             t.node_count != (n == 0 ? 0u : 2u * n - 1u))
             return RR_ERROR_INVALID_PARAMETER;
-        if (t.node_format != RR_CUDA_NODE_FORMAT_BINARY && t.node_format != RR_CUDA_NODE_FORMAT_WIDE8)
+        if (t.node_format != RR_CUDA_NODE_FORMAT_BINARY && t.node_format != RR_CUDA_NODE_FORMAT_WIDE8 &&
+            t.node_format != RR_CUDA_NODE_FORMAT_BVH4)
             return RR_ERROR_INVALID_PARAMETER;
         const GeomLayout L = geom_layout(n, t.node_format, t.morton_bits);
         if (t.wide_nodes_off != L.wide_off || t.wide_tris_off != L.tris_off) return RR_ERROR_INVALID_PARAMETER;
@@ -1644,7 +1665,7 @@ RR_API RRError rrUnmapDevicePtr(RRContext context, RRDevicePtr device_ptr, void*
 RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversalOptions* options)
 {
     if (!context || !options || options->struct_size < sizeof(RRCudaTraversalOptions)) return RR_ERROR_INVALID_PARAMETER;
-    if (options->traversal > RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || options->ray_order > 2)
+    if (options->traversal > RR_CUDA_TRAVERSAL_BVH4 || options->ray_order > 2)
         return RR_ERROR_INVALID_PARAMETER;
     if (options->block_size && (options->block_size % 32 || options->block_size > 1024)) return RR_ERROR_INVALID_PARAMETER;
     C(context)->topts = *options;
@@ -1722,12 +1743,13 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
         if (it != ctx->registry.end()) bi = it->second;
         const bool has_wide = (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0) ||
                               (bi.kind == kKindScene && bi.scene_wide);
-        // Workload key: device, buffer kind and size, query, output, ray-count octave.
+        // Workload key: device, buffer kind, node format and size, query,
+        // output, ray-count octave (the format decides the candidates).
         uint32_t octave = 0;
         while ((1ull << (octave + 1)) <= ray_count) ++octave;
-        const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.n) + "|" +
-                                std::to_string((int)query) + "|" + std::to_string((int)query_output) + "|" +
-                                std::to_string(octave);
+        const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.format) +
+                                "|" + std::to_string(bi.n) + "|" + std::to_string((int)query) + "|" +
+                                std::to_string((int)query_output) + "|" + std::to_string(octave);
         auto hit = ctx->tuned.find(key);
         const char* cache_path = std::getenv("RR_CUDA_TUNE_CACHE");
         if (hit == ctx->tuned.end() && cache_path)
@@ -1767,6 +1789,8 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);
             add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
+            if (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0)
+                add(RR_CUDA_TRAVERSAL_BVH4, 0);
             if (has_wide)
             {
                 add(RR_CUDA_TRAVERSAL_WIDE, 1);

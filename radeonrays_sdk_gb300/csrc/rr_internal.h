@@ -72,6 +72,20 @@ struct __align__(16) WideTri
 };
 static_assert(sizeof(WideTri) == 48, "triangle layout");
 
+// 4-wide node with exact fp32 child boxes (128 bytes, eight 16-byte words):
+// the boxes as structure of arrays, then the child references.  A reference
+// is a 4-wide node index, kBvh4Leaf | a binary leaf node index (that node
+// holds the triangle), or kInvalid for an empty slot.
+struct __align__(16) Bvh4Node
+{
+    float    lo[3][4];  // [axis][slot]
+    float    hi[3][4];
+    uint32_t child[4];
+    uint32_t pad[4];
+};
+static_assert(sizeof(Bvh4Node) == 128, "4-wide node layout");
+constexpr uint32_t kBvh4Leaf = 0x80000000u;
+
 // Trailer written after the binary node array of every result buffer; it
 // makes the buffer self-describing (kind, counts, section offsets).
 struct __align__(16) Trailer
@@ -270,6 +284,7 @@ struct TraceArgs
     const uint8_t*  bvh;          // result buffer base (binary nodes at offset 0)
     const WideNode* wide_nodes;   // wide path
     const WideTri*  wide_tris;
+    const Bvh4Node* bvh4_nodes;   // 4-wide path
     const uint8_t*  rays;         // RRRay[]
     uint32_t        ray_count;
     const uint32_t* indirect;     // optional device count
@@ -280,7 +295,7 @@ struct TraceArgs
     int             output;       // RRIntersectQueryOutput
     int             empty;        // geometry with no triangles
     uint32_t        node_limit;   // binary nodes in the buffer (kInvalid: unknown)
-    uint32_t        wide_limit;   // wide-node capacity
+    uint32_t        wide_limit;   // wide-node (8-wide or 4-wide) capacity
     uint32_t        tri_limit;    // wide-triangle capacity
     const uint32_t* bounds;       // mesh box (order-preserving uint encoding) for ray ordering; may be null
     int             ray_order;    // RRCudaTraversalOptions::ray_order
@@ -357,6 +372,7 @@ cudaError_t launch_trace_batch(const BatchTraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_binary(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_wide(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_persistent(const TraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_bvh4(const TraceArgs& a, cudaStream_t s);
 
 struct SceneTraceArgs
 {

@@ -1,0 +1,365 @@
+// trace_bvh4.cu -- persistent lane-refill traversal over the 4-wide fp32
+// nodes of an RR_CUDA_NODE_FORMAT_BVH4 buffer (no reference counterpart: the
+// reference traverses its binary nodes only, vlk/kernels/isect.comp).
+//
+// A step fetches one reference of the lane's ray: a 4-wide node (128 bytes:
+// four exact child boxes and their references) or a binary leaf node (the
+// triangle).  A node's children are slab-tested with the reference's formula
+// (vlk/kernels/common.h:150-164; the same arithmetic as the binary kernels);
+// the hit ones are ordered by entry distance, the nearest is visited next
+// and the others are pushed, farthest first.  A leaf gets the reference's
+// triangle test (common.h:103-137) and is accepted iff t < closest t.  The
+// closest hit is therefore the reference's except where two triangles are
+// hit at exactly the same t (then the visit order decides), and any-hit
+// hit/miss flags are the reference's.
+//
+// Compared with the binary kernels a 4-wide node covers about two binary
+// levels: half as many dependent fetches, and the internal nodes are a third
+// of the binary node array.  Scheduling is that of the persistent binary
+// kernel (trace_persistent.cu): lanes refill from a ray counter as their ray
+// finishes; the short stack lives in shared memory and spills to scratch.
+#include "trace_persistent.cuh"
+#include "trace_stream.cuh"
+
+namespace rr
+{
+namespace
+{
+using namespace stream_detail;
+struct B4Ray
+{
+    Ray      ray;
+    F3       inv, oxi;
+    float    ct;
+    uint32_t best;   // binary leaf node of the closest hit (kInvalid: none)
+    uint32_t ref;    // reference to fetch next
+    uint32_t gsp;    // entries spilled to global
+    uint32_t steps;
+    int      sp;     // entries in the short stack
+};
+
+__device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
+{
+    s.ray  = r;
+    s.inv  = safe_invdir(r.d);
+    s.oxi  = f3(-r.o.x * s.inv.x, -r.o.y * s.inv.y, -r.o.z * s.inv.z);
+    s.ct   = r.tmax;
+    s.best = kInvalid;
+    s.ref  = 0;  // the root 4-wide node
+    s.gsp = s.steps = 0;
+    s.sp            = 0;
+}
+
+// The short stack spills and refills in blocks of kB4Spill entries (every
+// block in the global region is full).
+constexpr int kB4Spill = 8;
+
+// Make room for `k` (at most 3) more short-stack entries: when they would not
+// fit, the bottom kB4Spill entries go to the global region and the rest move
+// down.
+__device__ __forceinline__ void b4_reserve(B4Ray& s, const PStack& st, DeviceWords* words, int k)
+{
+    if (s.sp + k <= kPShort) return;
+    if (s.gsp + kB4Spill > st.gcap)
+    {
+        raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
+        s.sp = kPShort - k;  // overwrite the top entries: result flagged invalid
+        return;
+    }
+    for (int j = 0; j < kB4Spill; ++j) st.g[s.gsp + j] = st.at(j);
+    for (int j = kB4Spill; j < s.sp; ++j) st.at(j - kB4Spill) = st.at(j);
+    s.gsp += kB4Spill;
+    s.sp -= kB4Spill;
+}
+
+// Three-input min / max (one instruction each on sm_100 and later); with
+// NaN operands they return the minimum / maximum of the others, like a chain
+// of fminf / fmaxf.
+__device__ __forceinline__ float max3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Order (key, ref) pairs ascending by key (misses carry +inf).
+__device__ __forceinline__ void cas(float& ka, uint32_t& ra, float& kb, uint32_t& rb)
+{
+    const bool sw = kb < ka;
+    const float    k = sw ? kb : ka;
+    const uint32_t r = sw ? rb : ra;
+    kb               = sw ? ka : kb;
+    rb               = sw ? ra : rb;
+    ka               = k;
+    ra               = r;
+}
+
+// One step; returns true when the ray is finished (stack empty, or a hit
+// accepted by an any-hit query).  nf / tf count node and leaf fetches.
+template <bool kAny>
+__device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ wn, const BvhNode* __restrict__ nodes,
+                                        uint32_t wlim, uint32_t first_leaf, uint32_t node_limit, const PStack& st,
+                                        DeviceWords* words, uint32_t& nf, uint32_t& tf)
+{
+    const uint32_t ref = s.ref;
+    const bool     leaf = (ref & kBvh4Leaf) != 0;
+    const uint32_t idx  = ref & ~kBvh4Leaf;
+    if (++s.steps > kFetchCap || (leaf ? (idx < first_leaf || idx >= node_limit) : idx >= wlim))
+    {
+        raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+        s.best = kInvalid;
+        return true;
+    }
+    bool pop = true, done = false;
+    if (leaf)
+    {
+        const float4* p = reinterpret_cast<const float4*>(nodes + idx);
+        const float4  a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+        ++tf;
+        const float t = isect_tri(s.ray, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), s.ct);
+        if (t < s.ct)
+        {
+            s.ct   = t;
+            s.best = idx;
+            if (kAny) done = true;
+        }
+    }
+    else
+    {
+        // Near and far planes per axis by the sign of the inverse direction
+        // (the boxes are stored as lo[3][4] then hi[3][4], so the choice is
+        // an offset): for inv > 0, fma(hi, inv, oxi) >= fma(lo, inv, oxi),
+        // and the reference's min / max of the two picks exactly these.
+        const float4* p  = reinterpret_cast<const float4*>(wn + idx);
+        const int     ox = s.inv.x < 0.f ? 3 : 0, oy = s.inv.y < 0.f ? 3 : 0, oz = s.inv.z < 0.f ? 3 : 0;
+        const float4  nx = __ldg(p + ox), ny = __ldg(p + 1 + oy), nz = __ldg(p + 2 + oz);
+        const float4  fx = __ldg(p + 3 - ox), fy = __ldg(p + 4 - oy), fz = __ldg(p + 5 - oz);
+        const uint4   cr = __ldg(reinterpret_cast<const uint4*>(p + 6));
+        ++nf;
+        const F3    inv = s.inv, oxi = s.oxi;
+        const float tmin = s.ray.tmin, ct = s.ct;
+        auto        key = [&](float ax, float ay, float az, float bx, float by, float bz, uint32_t r) {
+            const float t0 = fmaxf(max3(fmaf(ax, inv.x, oxi.x), fmaf(ay, inv.y, oxi.y), fmaf(az, inv.z, oxi.z)), tmin);
+            const float t1 = fminf(min3(fmaf(bx, inv.x, oxi.x), fmaf(by, inv.y, oxi.y), fmaf(bz, inv.z, oxi.z)), ct);
+            return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
+        };
+        float    k0 = key(nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, cr.x);
+        float    k1 = key(nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, cr.y);
+        float    k2 = key(nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, cr.z);
+        float    k3 = key(nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, cr.w);
+        uint32_t r0 = cr.x, r1 = cr.y, r2 = cr.z, r3 = cr.w;
+        // A box hit has a finite entry distance: tmin <= t0 <= t1 <= closest t.
+        const int nhit = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
+        if (nhit)
+        {
+            cas(k0, r0, k1, r1);
+            cas(k2, r2, k3, r3);
+            cas(k0, r0, k2, r2);
+            cas(k1, r1, k3, r3);
+            cas(k1, r1, k2, r2);
+            b4_reserve(s, st, words, nhit - 1);
+            if (nhit > 3) st.at(s.sp++) = r3;
+            if (nhit > 2) st.at(s.sp++) = r2;
+            if (nhit > 1) st.at(s.sp++) = r1;
+            s.ref = r0;
+            pop   = false;
+        }
+    }
+    if (pop && !done)
+    {
+        if (s.sp == 0 && s.gsp == 0)
+            done = true;
+        else
+        {
+            if (s.sp == 0)
+            {
+                s.gsp -= kB4Spill;
+                for (int k = 0; k < kB4Spill; ++k) st.at(k) = st.g[s.gsp + k];
+                s.sp = kB4Spill;
+            }
+            s.ref = st.at(--s.sp);
+        }
+    }
+    return done;
+}
+
+// kStream: the streamed variant for host-buffer tracing (trace_stream.cuh),
+// with the same arrival waits and done counts as the persistent binary
+// kernel's streamed variant.
+template <bool kAny, bool kFull, bool kStats, bool kStream>
+__global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t gcap)
+{
+    __shared__ uint32_t s_stack[kPBlock * kPShort];
+    const uint32_t      tglob = blockIdx.x * blockDim.x + threadIdx.x;
+    PStack              st;
+    st.s    = s_stack + threadIdx.x;
+    st.g    = reinterpret_cast<uint32_t*>(a.scratch + kTraceScratchHeader) + (uint64_t)tglob * gcap;
+    st.gcap = gcap;
+    uint32_t*       ray_ctr    = reinterpret_cast<uint32_t*>(a.scratch);
+    const uint32_t  lane       = threadIdx.x & 31;
+    const uint32_t  lt         = (1u << lane) - 1u;
+    uint32_t        count      = a.ray_count;
+    if (a.indirect) count = min(count, __ldg(a.indirect));
+    const BvhNode*  nodes      = reinterpret_cast<const BvhNode*>(a.bvh);
+    const Bvh4Node* wn         = a.bvh4_nodes;
+    const uint32_t  first_leaf = a.tri_limit - 1;  // binary leaves [n-1, 2n-2]
+
+    B4Ray    s;
+    uint32_t gid = kInvalid, nf = 0, tf = 0;
+    bool     active = false, pending = false, exhausted = false;
+    __shared__ int        s_seen;
+    __shared__ DoneCounts s_dc[kPBlock / 32];
+    volatile DoneCounts&  dc = s_dc[threadIdx.x >> 5];
+    if (kStream)
+    {
+        if (threadIdx.x == 0) s_seen = -1;
+        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = 0;
+        __syncthreads();
+    }
+    for (;;)
+    {
+        __syncwarp();
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
+        {
+            int            seen = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
+            const uint32_t n    = exhausted ? 0u : __popc(idle);
+            uint32_t       base = 0;
+            if (n)
+            {
+                const int leader = __ffs(idle) - 1;
+                if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+                base      = __shfl_sync(0xffffffffu, base, leader);
+                exhausted = base + n >= count;
+                if (kStream && base < count)
+                {
+                    const int hi  = (int)((min(base + n, count) - 1u) >> a.stream_shift);
+                    int       top = -1;
+                    if ((int)lane == leader)
+                    {
+                        top = *reinterpret_cast<volatile int*>(&s_seen);
+                        if (top < hi)
+                        {
+                            top = wait_arrival(a, (uint32_t)hi);
+                            if (top >= 0) atomicMax(&s_seen, top);
+                        }
+                    }
+                    seen = __shfl_sync(0xffffffffu, top, leader);
+                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, lane, dc);
+                    __syncwarp();
+                }
+            }
+            bool     fin   = false;
+            uint32_t fin_c = 0;
+            if (!active)
+            {
+                if (pending)
+                {
+                    if (s.best != kInvalid)
+                    {
+                        const NodeView nd = load_binary_node(nodes, s.best);
+                        write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                    }
+                    else
+                        write_miss<kFull>(a.hits, gid);
+                    if (kStats)
+                    {
+                        atomicAdd(&a.words->rays, 1ull);
+                        atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
+                        atomicAdd(&a.words->tri_fetches, (unsigned long long)tf);
+                    }
+                    pending = false;
+                    fin     = true;
+                    fin_c   = gid >> a.stream_part_shift;
+                }
+                const uint32_t my = base + __popc(idle & lt);
+                if (n && my < count)
+                {
+                    gid = my;
+                    if (kStream)
+                    {
+                        // Traced once its chunk is in; an empty geometry or a
+                        // chunk that never arrived finishes as a miss at the
+                        // next refill, where it is counted like any other.
+                        if (!a.empty && (int)(gid >> a.stream_shift) <= seen)
+                        {
+                            active = true;
+                            nf = tf = 0;
+                            b4_start(s, load_ray_cg(a.rays, gid));
+                        }
+                        else
+                        {
+                            s.best  = kInvalid;
+                            pending = true;
+                        }
+                    }
+                    else if (a.empty)
+                        write_miss<kFull>(a.hits, gid);
+                    else
+                    {
+                        active = true;
+                        nf = tf = 0;
+                        b4_start(s, load_ray(a.rays, gid));
+                    }
+                }
+            }
+            if (kStream) note_done(a, fin, fin_c, lane, dc);
+        }
+        const uint32_t amask = __ballot_sync(0xffffffffu, active);
+        if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
+        if (active && b4_step<kAny>(s, wn, nodes, a.wide_limit, first_leaf, a.node_limit, st, a.words, nf, tf))
+        {
+            active  = false;
+            pending = true;
+        }
+    }
+    if (kStream)
+    {
+        __syncwarp();  // the break above is warp-uniform; order the last hits before their counts
+        publish_done(a, lane, dc);
+    }
+}
+
+template <bool kAny, bool kFull, bool kStats, bool kStream>
+cudaError_t go(const TraceArgs& a, cudaStream_t s)
+{
+    auto kern   = k_trace_bvh4<kAny, kFull, kStats, kStream>;
+    int  per_sm = a.blocks_per_sm;
+    if (per_sm <= 0)
+    {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0) != cudaSuccess) per_sm = 1;
+        per_sm = per_sm > 0 ? per_sm : 1;
+    }
+    const PGrid g = persistent_grid(a.sm_count, per_sm, a.ray_count, a.scratch_bytes, kTraceScratchHeader);
+    cudaError_t e = cudaMemsetAsync(a.scratch, 0, kTraceScratchHeader, s);
+    if (e != cudaSuccess) return e;
+    kern<<<g.blocks, kPBlock, 0, s>>>(a, g.gcap);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_trace_bvh4(const TraceArgs& a, cudaStream_t s)
+{
+    if (a.ray_count == 0) return cudaSuccess;
+    const bool any = a.query == RR_INTERSECT_QUERY_ANY, full = a.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT;
+    if (a.stream_words)
+    {
+        if (any) return full ? go<true, true, false, true>(a, s) : go<true, false, false, true>(a, s);
+        return full ? go<false, true, false, true>(a, s) : go<false, false, false, true>(a, s);
+    }
+    if (a.collect_stats)
+    {
+        if (any) return full ? go<true, true, true, false>(a, s) : go<true, false, true, false>(a, s);
+        return full ? go<false, true, true, false>(a, s) : go<false, false, true, false>(a, s);
+    }
+    if (any) return full ? go<true, true, false, false>(a, s) : go<true, false, false, false>(a, s);
+    return full ? go<false, true, false, false>(a, s) : go<false, false, false, false>(a, s);
+}
+
+}  // namespace rr

@@ -1,11 +1,14 @@
 // wide.cu -- collapse of the binary LBVH into 8-wide nodes with 8-bit child
-// bounds (the "chosen" traversal format; no reference counterpart: the
-// reference traverses its binary nodes only, vlk/kernels/isect.comp).
+// bounds, or into 4-wide nodes with exact fp32 child boxes (traversal
+// formats of this build; no reference counterpart: the reference traverses
+// its binary nodes only, vlk/kernels/isect.comp).
 //
 // Collapse: top-down and level-synchronous.  A work item is (binary node b,
 // wide slot w).  The children of w start as b's two children; the internal
 // child with the largest surface area is replaced by its two children until
-// there are 8 children or only triangles remain.  Internal children become
+// there are W (8 or 4) children or only triangles remain.  A 4-wide node
+// keeps each child's exact box and refers to leaf children by their binary
+// leaf node; the 8-wide format is described below.  Internal children become
 // the next level's work items; triangle children are written to a contiguous
 // 48-byte triangle array.  Every level is one launch whose item count is read
 // on the device, so the whole build records into a stream without a host
@@ -177,6 +180,25 @@ __global__ void k_collapse_init(BatchArgs b)
     WideNode*      wn    = reinterpret_cast<WideNode*>(it.result + it.wide_off);
     WideTri*       wt    = reinterpret_cast<WideTri*>(it.result + it.tris_off);
     for (int i = 0; i < kMaxLevels + 2; ++i) ctl->level_count[i] = 0;
+    if (n == 1 && b.format == RR_CUDA_NODE_FORMAT_BVH4)
+    {
+        // A one-triangle mesh: one 4-wide node whose only child is the leaf.
+        const Bx  bx = node_union(nodes[0]);
+        Bvh4Node  o{};
+        for (int k = 0; k < 4; ++k)
+        {
+            for (int a = 0; a < 3; ++a)
+            {
+                o.lo[a][k] = k == 0 ? bx.lo[a] : 0.f;
+                o.hi[a][k] = k == 0 ? bx.hi[a] : 0.f;
+            }
+            o.child[k] = k == 0 ? kBvh4Leaf : kInvalid;
+        }
+        reinterpret_cast<Bvh4Node*>(it.result + it.wide_off)[0] = o;
+        ctl->wide_count = 1;
+        ctl->tri_count  = 0;
+        return;
+    }
     if (n == 1)
     {
         // A one-triangle mesh: one wide node with a single triangle slot.
@@ -254,6 +276,7 @@ __global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int leve
 // One level of the collapse for every geometry: work item `it` of the level
 // belongs to the geometry found in the level prefix (a batch of one reads
 // its count directly).
+template <int W>
 __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, DeviceWords* words)
 {
     const uint32_t total = b.count == 1 ? *((volatile uint32_t*)&ctl_of(b.items[0])->level_count[level])
@@ -293,7 +316,7 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
             cint[0]       = ch[0] < first_leaf;
             cint[1]       = ch[1] < first_leaf;
             nc            = 2;
-            while (nc < 8)
+            while (nc < W)
             {
                 int   best = -1;
                 float ba   = -1.f;
@@ -321,7 +344,7 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
         // Leaf slots hold one triangle each (the meta byte's count field
         // allows up to 3; one measured fastest).
         uint32_t ccnt[8];
-        for (int k = 0; k < nc; ++k) ccnt[k] = cint[k] ? 0u : 1u;
+        for (int k = 0; k < nc; ++k) ccnt[k] = (cint[k] || W == 4) ? 0u : 1u;  // 4-wide: no triangle array
         uint32_t n_int = 0, n_leaf = 0;
         for (int k = 0; k < nc; ++k)
         {
@@ -339,6 +362,36 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
         if (child_base + n_int > wide_capacity || tri_base + n_leaf > tri_capacity)
         {
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            continue;
+        }
+        if (W == 4)
+        {
+            // 4-wide node: exact child boxes (read from the parents), internal
+            // children numbered in slot order, leaf children by their binary
+            // leaf node.
+            Bvh4Node o;
+            uint32_t ri = 0;
+            for (int k = 0; k < 4; ++k)
+            {
+                const bool used = k < nc;
+                for (int a = 0; a < 3; ++a)
+                {
+                    o.lo[a][k] = used ? cb[k].lo[a] : 0.f;
+                    o.hi[a][k] = used ? cb[k].hi[a] : 0.f;
+                }
+                if (!used)
+                    o.child[k] = kInvalid;
+                else if (cint[k])
+                {
+                    o.child[k]      = child_base + ri;
+                    qout[qpos + ri] = Item{ch[k], child_base + ri};
+                    ++ri;
+                }
+                else
+                    o.child[k] = kBvh4Leaf | ch[k];
+                o.pad[k] = 0;
+            }
+            reinterpret_cast<Bvh4Node*>(bi->result + bi->wide_off)[item.w] = o;
             continue;
         }
         // Quantisation frame.
@@ -488,8 +541,11 @@ cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm
             const uint64_t cap    = std::min<uint64_t>(bound, b.total_prims);
             const int      blocks = (int)std::max<uint64_t>(
                 1, std::min<uint64_t>((cap + 127) / 128, (uint64_t)sm_count * 16));
-            k_collapse_level<<<blocks, 128, 0, s>>>(b, level, words);
-            bound = std::min<uint64_t>(bound * 8, b.total_prims);
+            if (b.format == RR_CUDA_NODE_FORMAT_BVH4)
+                k_collapse_level<4><<<blocks, 128, 0, s>>>(b, level, words);
+            else
+                k_collapse_level<8><<<blocks, 128, 0, s>>>(b, level, words);
+            bound = std::min<uint64_t>(bound * (b.format == RR_CUDA_NODE_FORMAT_BVH4 ? 4 : 8), b.total_prims);
         }
     }
     k_collapse_finish<<<per_geom, 128, 0, s>>>(b, words);

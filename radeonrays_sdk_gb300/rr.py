@@ -41,8 +41,9 @@ RR_INDEX_TYPE_UINT32, RR_INDEX_TYPE_UINT16 = 0, 1
 RR_INTERSECT_QUERY_CLOSEST, RR_INTERSECT_QUERY_ANY = 0, 1
 RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID = 0, 1
 RR_LOG_LEVEL_DEBUG, RR_LOG_LEVEL_INFO, RR_LOG_LEVEL_WARN, RR_LOG_LEVEL_ERROR, RR_LOG_LEVEL_OFF = 1, 2, 3, 4, 5
-RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8 = 0, 1
+RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8, RR_CUDA_NODE_FORMAT_BVH4 = 0, 1, 2
 RR_CUDA_TRAVERSAL_AUTO, RR_CUDA_TRAVERSAL_BINARY, RR_CUDA_TRAVERSAL_WIDE = 0, 1, 2
+RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, RR_CUDA_TRAVERSAL_BVH4 = 3, 4
 RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW = 1
 RR_CUDA_DEVICE_ERROR_BAD_BUFFER = 2
 RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH = 4

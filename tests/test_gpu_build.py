@@ -22,7 +22,7 @@ def same_nodes(a, b):
 
 
 @pytest.mark.parametrize("name", MESH_FIXTURES)
-@pytest.mark.parametrize("fmt", [0, 1])
+@pytest.mark.parametrize("fmt", [0, 1, 2])
 def test_build_matches_oracle_on_fixtures(ctx, orc, name, fmt):
     g = golden(name)
     n = g["indices"].shape[0]

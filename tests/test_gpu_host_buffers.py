@@ -102,3 +102,21 @@ def test_streamed_and_chunked_plans_agree(ctx, monkeypatch):
         assert c2.device_errors() == 0
     assert np.array_equal(chunked, streamed)
     assert ctx.device_errors() == 0
+
+
+@pytest.mark.parametrize("q,o", [(0, 0), (1, 1)])
+def test_streamed_host_trace_bvh4(ctx, q, o):
+    """The 4-wide kernel's streamed variant gives the hits of its device run."""
+    import torch
+    v, i, rays = _heightfield_case(300_001, 11)
+    if q == 1:
+        rays[:, 7] = np.float32(0.05)
+    bvh = ctx.build_geometry(to_dev(v), to_dev(i), node_format=2)
+    ctx.set_traversal(4)
+    try:
+        want = hits_np(ctx.intersect(bvh, to_dev(rays), query=q, output=o))
+        got = ctx.intersect_host(bvh, torch.from_numpy(rays).pin_memory(), query=q, output=o, chunk_rays=16384)
+    finally:
+        ctx.set_traversal(0)
+    assert np.array_equal(got.numpy().view(np.uint32), want)
+    assert ctx.device_errors() == 0

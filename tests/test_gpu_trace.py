@@ -207,7 +207,7 @@ def test_autotuner_selects_a_kernel_and_results_stay_exact(ctx, orc, tmp_path, m
     res = build(ctx, v, i, node_format=1)
     rays_d = to_dev(rays)
     choice = ctx.autotune(res, rays_d)
-    assert choice["traversal"] in (BINARY, WIDE, PERSISTENT)
+    assert choice["traversal"] in (BINARY, WIDE, PERSISTENT)  # a WIDE8 buffer: no 4-wide candidate
     assert (tmp_path / "tune.tsv").exists()
     nodes, _, _ = orc.build_mesh(v, i)
     want = orc.trace(nodes, rays, threads=16)
