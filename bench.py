@@ -318,22 +318,23 @@ def run_ours(args):
     i_d = torch.from_numpy(i.view(np.int32)).cuda()
 
     # ---- build (LBVH + wide collapse) through rrCmdBuildGeometry
-    s_bytes, r_bytes = ctx.geometry_requirements(ntri, rr.RR_CUDA_NODE_FORMAT_WIDE8, 30, v.shape[0], 12)
+    # The library's default node format (binary + 4-wide nodes).
+    s_bytes, r_bytes = ctx.geometry_requirements(ntri, rr.RR_CUDA_NODE_FORMAT_BVH4, 30, v.shape[0], 12)
     scratch_b = torch.empty(s_bytes, dtype=torch.uint8, device="cuda")
     bvh = torch.empty(r_bytes, dtype=torch.uint8, device="cuda")
 
     def build_step():
-        ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_WIDE8, stream=ext, scratch=scratch_b,
+        ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_BVH4, stream=ext, scratch=scratch_b,
                            result=bvh)
         ctx.release_ptrs()
     b_per, b_total = time_steps(build_step, 5, 2, 1, stream)
     build = {"ms": statistics.median(b_per), "mtris_s": ntri / statistics.median(b_per) / 1e3,
-             "format": "binary + wide8", "triangles": ntri, "flags": "PREFER_FAST_BUILD (reference LBVH)"}
+             "format": "binary + bvh4", "triangles": ntri, "flags": "PREFER_FAST_BUILD (reference LBVH)"}
     # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
     # LBVH + treelet restructure); the plain path the reference's fast LBVH.
     bvh_c = bvh
     cfmt = rr.RR_CUDA_NODE_FORMAT_BVH4 if args.chosen_format == "bvh4" else rr.RR_CUDA_NODE_FORMAT_WIDE8
-    if args.quality or cfmt != rr.RR_CUDA_NODE_FORMAT_WIDE8:
+    if args.quality or cfmt != rr.RR_CUDA_NODE_FORMAT_BVH4:
         cs_bytes, cr_bytes = ctx.geometry_requirements(ntri, cfmt, 30, v.shape[0], 12)
         bvh_c = torch.empty(cr_bytes, dtype=torch.uint8, device="cuda")
         scratch_c = scratch_b if cs_bytes <= scratch_b.numel() else torch.empty(cs_bytes, dtype=torch.uint8,
@@ -509,7 +510,7 @@ def run_batch(args):
         meshes.append((v_all[vo:vo + v.shape[0]], i_all[io:io + i.shape[0]]))
         vo, io = vo + v.shape[0], io + i.shape[0]
     ctx = rr.Context()
-    fmt = rr.RR_CUDA_NODE_FORMAT_WIDE8
+    fmt = rr.RR_CUDA_NODE_FORMAT_BVH4  # the library default
 
     def timed(fn, k, w):
         for _ in range(w):
@@ -565,7 +566,7 @@ def run_batch(args):
                       "separate_ms": 1e3 * statistics.median(s_t),
                       "separate_mtris_s": ntri / statistics.median(s_t) / 1e6,
                       "fused_speedup": statistics.median(s_t) / statistics.median(f_t),
-                      "tlas_ms": 1e3 * statistics.median(tl_t), "format": "binary + wide8",
+                      "tlas_ms": 1e3 * statistics.median(tl_t), "format": "binary + bvh4",
                       "fused_timing": "host clock around rrSumbitCommandStream + rrWaitEvent (CUDA graph replay)"},
             "trace": out, "speedup_vs_plain": out["plain"]["ms"] / out["chosen"]["ms"],
             "hit_flags_identical": flags_equal, "hit_mismatches_vs_plain": mism, "device_errors": int(errors)}

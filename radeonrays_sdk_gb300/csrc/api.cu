@@ -711,7 +711,8 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         }
         return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
     }
-    if (trav == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0)
+    if (trav == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+        bi.prim_kind == kPrimTriangles)
     {
         a.bvh4_nodes = reinterpret_cast<const Bvh4Node*>(bvh + bi.wide_off);
         a.wide_limit = (uint32_t)bi.wide_capacity;
@@ -1789,7 +1790,8 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);
             add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
-            if (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0)
+            if (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+                bi.prim_kind == kPrimTriangles)
                 add(RR_CUDA_TRAVERSAL_BVH4, 0);
             if (has_wide)
             {
