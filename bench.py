@@ -548,7 +548,10 @@ def run_batch(args):
         rr.check(ctx.L.rrCmdIntersect(ctx.ctx, hb, rr.RR_INTERSECT_QUERY_CLOSEST, rb, R, None,
                                       rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hitb, sb, ext), "rrCmdIntersect")
     out = {}
-    for name, trav in (("chosen", rr.RR_CUDA_TRAVERSAL_AUTO), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
+    # Chosen: the autotuner's pick among the two-level kernels the scene allows
+    # (plain, persistent binary, 4-wide BLASes).
+    tuned = ctx.autotune(scene, rays_d, hits=hits_d, scratch=scratch_t)
+    for name, trav in (("chosen", tuned["traversal"]), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
         ctx.set_traversal(trav)
         per, total = time_steps(trace_step, max(3, args.steps // 3), max(3, args.warmup), 1, stream)
         out[name] = {"ms": statistics.median(per), "mrays_s": R / statistics.median(per) / 1e3,
@@ -568,7 +571,11 @@ def run_batch(args):
                       "fused_speedup": statistics.median(s_t) / statistics.median(f_t),
                       "tlas_ms": 1e3 * statistics.median(tl_t), "format": "binary + bvh4",
                       "fused_timing": "host clock around rrSumbitCommandStream + rrWaitEvent (CUDA graph replay)"},
-            "trace": out, "speedup_vs_plain": out["plain"]["ms"] / out["chosen"]["ms"],
+            "trace": out, "chosen_traversal": {"traversal": tuned["traversal"],
+                                               "kernel": {1: "k_trace_scene_binary", 3: "k_trace_scene_persistent",
+                                                          4: "k_trace_scene_bvh4"}.get(tuned["traversal"], "?"),
+                                               "selected_by": "rrCudaAutotuneTraversal"},
+            "speedup_vs_plain": out["plain"]["ms"] / out["chosen"]["ms"],
             "hit_flags_identical": flags_equal, "hit_mismatches_vs_plain": mism, "device_errors": int(errors)}
     print(json.dumps(line), flush=True)
     del keep

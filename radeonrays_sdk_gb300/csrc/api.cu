@@ -86,7 +86,8 @@ struct BufInfo
     uint32_t format = RR_CUDA_NODE_FORMAT_BINARY;
     size_t   trailer_off = 0, wide_off = 0, tris_off = 0, xforms_off = 0, inst_off = 0;
     size_t   wide_capacity = 0;  // geometry: 8-wide or 4-wide node capacity
-    bool     scene_wide = false;
+    bool     scene_wide = false;  // scene: every instance has 8-wide nodes
+    bool     scene_bvh4 = false;  // scene: every instance has 4-wide nodes
     uint32_t prim_kind  = kPrimTriangles;  // geometry: triangles or AABB list
 };
 
@@ -687,6 +688,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         // rays; the 8-wide BLAS kernel stays selectable as WIDE).
         sa.use_wide       = bi.scene_wide && trav == RR_CUDA_TRAVERSAL_WIDE;
         sa.use_persistent = trav == RR_CUDA_TRAVERSAL_AUTO || trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT;
+        sa.use_bvh4       = bi.scene_bvh4 && trav == RR_CUDA_TRAVERSAL_BVH4;
         if (sp) return Op();
         return [=](cudaStream_t s) { return launch_trace_scene(sa, s); };
     }
@@ -1076,6 +1078,7 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
         float*       xf     = reinterpret_cast<float*>(stage->p);
         InstanceDesc* id    = reinterpret_cast<InstanceDesc*>(reinterpret_cast<uint8_t*>(stage->p) + xbytes);
         bool          all_wide = n > 0;
+        bool          all_bvh4 = n > 0;  // every instance 4-wide (or empty)
         for (uint32_t i = 0; i < n; ++i)
         {
             const RRInstance& in = build_input->instances[i];
@@ -1098,12 +1101,17 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
                 }
                 else
                     all_wide = false;
+                if (it->second.format == RR_CUDA_NODE_FORMAT_BVH4 && it->second.n > 0)
+                    d.wide_nodes = (uint64_t)(uintptr_t)(blas + it->second.wide_off);  // its 4-wide nodes
+                else if (it->second.n > 0)
+                    all_bvh4 = false;
                 d.flags = 1;  // known geometry
             }
             else
             {
                 d.leaf_count = 0xffffffffu;  // unknown: traverse binary nodes from the root
                 all_wide     = false;
+                all_bvh4     = false;
             }
             id[i] = d;
         }
@@ -1136,6 +1144,7 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
         bi.xforms_off  = L.xforms_off;
         bi.inst_off    = L.inst_off;
         bi.scene_wide  = all_wide;
+        bi.scene_bvh4  = all_bvh4;
         ctx->registry[(uintptr_t)result] = bi;
         return RR_SUCCESS;
     })
@@ -1790,8 +1799,9 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);
             add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
-            if (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
-                bi.prim_kind == kPrimTriangles)
+            if ((bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+                 bi.prim_kind == kPrimTriangles) ||
+                (bi.kind == kKindScene && bi.scene_bvh4))
                 add(RR_CUDA_TRAVERSAL_BVH4, 0);
             if (has_wide)
             {

@@ -382,9 +382,11 @@ struct SceneTraceArgs
     uint32_t            inst_count;
     int                 use_wide;        // 8-wide BLAS kernel
     int                 use_persistent;  // persistent binary two-level kernel
+    int                 use_bvh4;        // persistent kernel over 4-wide BLASes (all instances BVH4)
 };
 cudaError_t launch_trace_scene(const SceneTraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_scene_persistent(const SceneTraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_scene_bvh4(const SceneTraceArgs& a, cudaStream_t s);
 
 struct SceneBuildArgs
 {

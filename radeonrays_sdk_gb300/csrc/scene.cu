@@ -575,6 +575,7 @@ cudaError_t launch_trace_scene(const SceneTraceArgs& sa, cudaStream_t s)
 {
     const TraceArgs& a = sa.base;
     if (a.ray_count == 0) return cudaSuccess;
+    if (sa.use_bvh4) return launch_trace_scene_bvh4(sa, s);
     if (sa.use_persistent) return launch_trace_scene_persistent(sa, s);
     const bool any = a.query == RR_INTERSECT_QUERY_ANY, full = a.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT;
     if (a.collect_stats)

@@ -18,7 +18,7 @@
 // of the binary node array.  Scheduling is that of the persistent binary
 // kernel (trace_persistent.cu): lanes refill from a ray counter as their ray
 // finishes; the short stack lives in shared memory and spills to scratch.
-#include "trace_persistent.cuh"
+#include "trace_bvh4.cuh"
 #include "trace_stream.cuh"
 
 namespace rr
@@ -48,56 +48,6 @@ __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
     s.ref  = 0;  // the root 4-wide node
     s.gsp = s.steps = 0;
     s.sp            = 0;
-}
-
-// The short stack spills and refills in blocks of kB4Spill entries (every
-// block in the global region is full).
-constexpr int kB4Spill = 8;
-
-// Make room for `k` (at most 3) more short-stack entries: when they would not
-// fit, the bottom kB4Spill entries go to the global region and the rest move
-// down.
-__device__ __forceinline__ void b4_reserve(B4Ray& s, const PStack& st, DeviceWords* words, int k)
-{
-    if (s.sp + k <= kPShort) return;
-    if (s.gsp + kB4Spill > st.gcap)
-    {
-        raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
-        s.sp = kPShort - k;  // overwrite the top entries: result flagged invalid
-        return;
-    }
-    for (int j = 0; j < kB4Spill; ++j) st.g[s.gsp + j] = st.at(j);
-    for (int j = kB4Spill; j < s.sp; ++j) st.at(j - kB4Spill) = st.at(j);
-    s.gsp += kB4Spill;
-    s.sp -= kB4Spill;
-}
-
-// Three-input min / max (one instruction each on sm_100 and later); with
-// NaN operands they return the minimum / maximum of the others, like a chain
-// of fminf / fmaxf.
-__device__ __forceinline__ float max3(float a, float b, float c)
-{
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float min3(float a, float b, float c)
-{
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
-// Order (key, ref) pairs ascending by key (misses carry +inf).
-__device__ __forceinline__ void cas(float& ka, uint32_t& ra, float& kb, uint32_t& rb)
-{
-    const bool sw = kb < ka;
-    const float    k = sw ? kb : ka;
-    const uint32_t r = sw ? rb : ra;
-    kb               = sw ? ka : kb;
-    rb               = sw ? ra : rb;
-    ka               = k;
-    ra               = r;
 }
 
 // One step; returns true when the ray is finished (stack empty, or a hit
@@ -132,60 +82,15 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        // Near and far planes per axis by the sign of the inverse direction
-        // (the boxes are stored as lo[3][4] then hi[3][4], so the choice is
-        // an offset): for inv > 0, fma(hi, inv, oxi) >= fma(lo, inv, oxi),
-        // and the reference's min / max of the two picks exactly these.
-        const float4* p  = reinterpret_cast<const float4*>(wn + idx);
-        const int     ox = s.inv.x < 0.f ? 3 : 0, oy = s.inv.y < 0.f ? 3 : 0, oz = s.inv.z < 0.f ? 3 : 0;
-        const float4  nx = __ldg(p + ox), ny = __ldg(p + 1 + oy), nz = __ldg(p + 2 + oz);
-        const float4  fx = __ldg(p + 3 - ox), fy = __ldg(p + 4 - oy), fz = __ldg(p + 5 - oz);
-        const uint4   cr = __ldg(reinterpret_cast<const uint4*>(p + 6));
+        const B4Hits h = b4_children(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
-        const F3    inv = s.inv, oxi = s.oxi;
-        const float tmin = s.ray.tmin, ct = s.ct;
-        auto        key = [&](float ax, float ay, float az, float bx, float by, float bz, uint32_t r) {
-            const float t0 = fmaxf(max3(fmaf(ax, inv.x, oxi.x), fmaf(ay, inv.y, oxi.y), fmaf(az, inv.z, oxi.z)), tmin);
-            const float t1 = fminf(min3(fmaf(bx, inv.x, oxi.x), fmaf(by, inv.y, oxi.y), fmaf(bz, inv.z, oxi.z)), ct);
-            return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
-        };
-        float    k0 = key(nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, cr.x);
-        float    k1 = key(nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, cr.y);
-        float    k2 = key(nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, cr.z);
-        float    k3 = key(nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, cr.w);
-        uint32_t r0 = cr.x, r1 = cr.y, r2 = cr.z, r3 = cr.w;
-        // A box hit has a finite entry distance: tmin <= t0 <= t1 <= closest t.
-        const int nhit = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
-        if (nhit)
+        if (h.n)
         {
-            cas(k0, r0, k1, r1);
-            cas(k2, r2, k3, r3);
-            cas(k0, r0, k2, r2);
-            cas(k1, r1, k3, r3);
-            cas(k1, r1, k2, r2);
-            b4_reserve(s, st, words, nhit - 1);
-            if (nhit > 3) st.at(s.sp++) = r3;
-            if (nhit > 2) st.at(s.sp++) = r2;
-            if (nhit > 1) st.at(s.sp++) = r1;
-            s.ref = r0;
+            s.ref = b4_descend(h, s.sp, s.gsp, st, words);
             pop   = false;
         }
     }
-    if (pop && !done)
-    {
-        if (s.sp == 0 && s.gsp == 0)
-            done = true;
-        else
-        {
-            if (s.sp == 0)
-            {
-                s.gsp -= kB4Spill;
-                for (int k = 0; k < kB4Spill; ++k) st.at(k) = st.g[s.gsp + k];
-                s.sp = kB4Spill;
-            }
-            s.ref = st.at(--s.sp);
-        }
-    }
+    if (pop && !done && !b4_pop(s.sp, s.gsp, st, s.ref)) done = true;
     return done;
 }
 

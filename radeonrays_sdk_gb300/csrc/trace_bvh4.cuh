@@ -1,0 +1,135 @@
+// trace_bvh4.cuh -- device helpers for the 4-wide fp32 node format, shared
+// by the single-level (trace_bvh4.cu) and two-level (trace_scene_bvh4.cu)
+// kernels: the node test with its nearest-first ordering, and a short stack
+// that spills and refills in full blocks.
+#pragma once
+#include "trace_persistent.cuh"
+
+namespace rr
+{
+// The short stack spills and refills in blocks of kB4Spill entries (every
+// block in the global region is full).
+constexpr int kB4Spill = 8;
+
+// Make room for `k` (at most 3) more short-stack entries: when they would not
+// fit, the bottom kB4Spill entries go to the global region and the rest move
+// down.
+__device__ __forceinline__ void b4_reserve(int& sp, uint32_t& gsp, const PStack& st, DeviceWords* words, int k)
+{
+    if (sp + k <= kPShort) return;
+    if (gsp + kB4Spill > st.gcap)
+    {
+        raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
+        sp = kPShort - k;  // overwrite the top entries: result flagged invalid
+        return;
+    }
+    for (int j = 0; j < kB4Spill; ++j) st.g[gsp + j] = st.at(j);
+    for (int j = kB4Spill; j < sp; ++j) st.at(j - kB4Spill) = st.at(j);
+    gsp += kB4Spill;
+    sp -= kB4Spill;
+}
+
+// Pops into `out`; false when the stack is empty.
+__device__ __forceinline__ bool b4_pop(int& sp, uint32_t& gsp, const PStack& st, uint32_t& out)
+{
+    if (sp == 0 && gsp == 0) return false;
+    if (sp == 0)
+    {
+        gsp -= kB4Spill;
+        for (int k = 0; k < kB4Spill; ++k) st.at(k) = st.g[gsp + k];
+        sp = kB4Spill;
+    }
+    out = st.at(--sp);
+    return true;
+}
+
+// Three-input min / max (one instruction each on sm_100 and later); with
+// NaN operands they return the minimum / maximum of the others, like a chain
+// of fminf / fmaxf.
+__device__ __forceinline__ float b4_max3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float b4_min3(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Order (key, ref) pairs ascending by key (misses carry +inf).
+__device__ __forceinline__ void b4_cas(float& ka, uint32_t& ra, float& kb, uint32_t& rb)
+{
+    const bool     sw = kb < ka;
+    const float    k  = sw ? kb : ka;
+    const uint32_t r  = sw ? rb : ra;
+    kb                = sw ? ka : kb;
+    rb                = sw ? ra : rb;
+    ka                = k;
+    ra                = r;
+}
+
+// The hit children of a 4-wide node, nearest first: r[0..n).
+struct B4Hits
+{
+    int      n;
+    uint32_t r0, r1, r2, r3;
+};
+
+// Slab test of the four children with the reference's formula
+// (vlk/kernels/common.h:150-164), evaluated on the near and far planes
+// picked by the signs of the inverse direction: for inv > 0,
+// fma(hi, inv, oxi) >= fma(lo, inv, oxi), so the reference's min / max of
+// the two are exactly these.  The boxes are stored lo[3][4] then hi[3][4],
+// so the choice is a load offset.
+__device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 oxi, float tmin, float ct)
+{
+    const float4* p  = reinterpret_cast<const float4*>(node);
+    const int     ox = inv.x < 0.f ? 3 : 0, oy = inv.y < 0.f ? 3 : 0, oz = inv.z < 0.f ? 3 : 0;
+    const float4  nx = __ldg(p + ox), ny = __ldg(p + 1 + oy), nz = __ldg(p + 2 + oz);
+    const float4  fx = __ldg(p + 3 - ox), fy = __ldg(p + 4 - oy), fz = __ldg(p + 5 - oz);
+    const uint4   cr = __ldg(reinterpret_cast<const uint4*>(p + 6));
+    auto          key = [&](float ax, float ay, float az, float bx, float by, float bz, uint32_t r) {
+        const float t0 = fmaxf(b4_max3(fmaf(ax, inv.x, oxi.x), fmaf(ay, inv.y, oxi.y), fmaf(az, inv.z, oxi.z)), tmin);
+        const float t1 = fminf(b4_min3(fmaf(bx, inv.x, oxi.x), fmaf(by, inv.y, oxi.y), fmaf(bz, inv.z, oxi.z)), ct);
+        return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
+    };
+    float  k0 = key(nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, cr.x);
+    float  k1 = key(nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, cr.y);
+    float  k2 = key(nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, cr.z);
+    float  k3 = key(nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, cr.w);
+    B4Hits h;
+    h.r0 = cr.x;
+    h.r1 = cr.y;
+    h.r2 = cr.z;
+    h.r3 = cr.w;
+    // A box hit has a finite entry distance: tmin <= t0 <= t1 <= closest t.
+    h.n = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
+    if (h.n > 1)
+    {
+        b4_cas(k0, h.r0, k1, h.r1);
+        b4_cas(k2, h.r2, k3, h.r3);
+        b4_cas(k0, h.r0, k2, h.r2);
+        b4_cas(k1, h.r1, k3, h.r3);
+        b4_cas(k1, h.r1, k2, h.r2);
+    }
+    else if (h.n == 1)
+        h.r0 = k0 < INFINITY ? h.r0 : (k1 < INFINITY ? h.r1 : (k2 < INFINITY ? h.r2 : h.r3));
+    return h;
+}
+
+// Pushes the hit children after the nearest (farthest first) and returns the
+// nearest; the caller has h.n >= 1.
+__device__ __forceinline__ uint32_t b4_descend(const B4Hits& h, int& sp, uint32_t& gsp, const PStack& st,
+                                               DeviceWords* words)
+{
+    b4_reserve(sp, gsp, st, words, h.n - 1);
+    if (h.n > 3) st.at(sp++) = h.r3;
+    if (h.n > 2) st.at(sp++) = h.r2;
+    if (h.n > 1) st.at(sp++) = h.r1;
+    return h.r0;
+}
+
+}  // namespace rr
