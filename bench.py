@@ -21,6 +21,9 @@ Reported (one JSON line on rank 0):
                measured HBM copy bandwidth
   build        LBVH + wide collapse of the mesh through rrCmdBuildGeometry
   hit_id_identity  chosen vs plain on every ray
+  precision_wide8  the 8-wide nodes with 8-bit conservative bounds on the fast
+               tree: Mrays/s, hit identity against the plain kernel on
+               every ray, and its own fp64 t / uv error
   fp64_t_error t / uv error of the chosen hits against an fp64 evaluation of
                the same ray-triangle pairs on the first 1,048,576 rays
   cpu_baseline the oracle's C++ restatement of the reference traversal on the
@@ -72,6 +75,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the 8-wide 8-bit-bounds run (hit identity and fp64 error of that format)")
     ap.add_argument("--e2e-chunk", type=int, default=0,
                     help="rays per copy-in chunk of the e2e run (0: the library's default, 2^17)")
     ap.add_argument("--quality", type=int, default=1,
@@ -393,6 +398,52 @@ def run_ours(args):
                      "hits": hits_d.cpu().numpy().view(np.uint32).copy(), "trav": trav, "order": order}
     assert ctx.device_errors() == 0, "device error word set during the benchmark"
 
+    # ---- 8-wide nodes with 8-bit conservative child bounds (the precision
+    # configuration): the fast tree in the WIDE8 format, traced by the 8-wide
+    # kernel, against the plain kernel's hits on the same binary tree.
+    wide8 = None
+    if not args.no_precision and "plain" in out and not args.only:
+        s8, r8 = ctx.geometry_requirements(ntri, rr.RR_CUDA_NODE_FORMAT_WIDE8, 30, v.shape[0], 12)
+        scratch8 = scratch_b if s8 <= scratch_b.numel() else torch.empty(s8, dtype=torch.uint8, device="cuda")
+        bvh8 = torch.empty(r8, dtype=torch.uint8, device="cuda")
+        ctx.build_geometry(v_d, i_d, node_format=rr.RR_CUDA_NODE_FORMAT_WIDE8, stream=ext, scratch=scratch8,
+                           result=bvh8)
+        cur["bvh"] = ctx.ptr(bvh8)
+        ctx.set_traversal(rr.RR_CUDA_TRAVERSAL_WIDE, collect_stats=1, ray_order=1)
+        trace_step()
+        torch.cuda.synchronize()
+        st8 = ctx.stats()
+        ctx.set_traversal(rr.RR_CUDA_TRAVERSAL_WIDE, ray_order=1)
+        per8, total8 = time_steps(trace_step, max(3, args.steps // 3), args.warmup, ws, stream)
+        h8 = hits_d.cpu().numpy().view(np.uint32).copy()
+        ph = out["plain"]["hits"]
+        hit = ph[:, 2] != 0xFFFFFFFF
+        d8 = np.where(hit & (h8[:, 3] != ph[:, 3]))[0]
+        ties8, gap8, closer8 = None, None, None
+        if d8.size and d8.size < 100000:
+            import oracle
+            idx = i.astype(np.int64)
+            ta = oracle.tri_test(rays[d8], v[idx[h8[d8, 3]]].reshape(-1, 9))[:, 0]
+            tb = oracle.tri_test(rays[d8], v[idx[ph[d8, 3]]].reshape(-1, 9))[:, 0]
+            ties8 = bool(np.array_equal(ta, tb))
+            gap8 = float((np.abs(ta.astype(np.float64) - tb) / np.spacing(np.maximum(np.abs(ta), np.abs(tb)))).max())
+            closer8 = int(np.sum(ta < tb))
+        wide8 = {"kernel": "k_trace_wide", "format": "binary + 8-wide nodes, 8-bit child bounds rounded outward "
+                                                     "against a per-node fp32 origin and power-of-two scale",
+                 "tree": "fast LBVH (the plain kernel's tree)",
+                 "value": R * ws * max(3, args.steps // 3) / (total8 / 1e3) / 1e6, "unit": "Mrays/s",
+                 "wide_node_fetches_per_ray": st8["node_fetches"] / R,
+                 "triangle_fetches_per_ray": st8["triangle_fetches"] / R,
+                 "hit_id_identity": {"rays": int(R),
+                                     "hit_flags_identical": bool(np.array_equal(h8[:, 2] != 0xFFFFFFFF, hit)),
+                                     "mismatches": int(d8.size), "mismatches_are_equal_t_ties": ties8,
+                                     "mismatch_t_gap_ulp_max": gap8, "mismatches_where_8wide_t_is_smaller": closer8,
+                                     "note": "the conservative 8-bit boxes reach every triangle the reference's "
+                                             "fp32 slab test reaches; a mismatch is an equal-t tie or a grazing "
+                                             "hit whose box the reference's non-conservative test rejects"},
+                 "hits": h8}
+        assert ctx.device_errors() == 0, "device error word set during the 8-wide run"
+
     # ---- end to end through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and not args.only:
@@ -487,6 +538,11 @@ def run_ours(args):
         cb, nodes = cpu_baseline(v, i, rays, args.cpu_seconds)
         line["cpu_baseline"] = cb
         line["fp64_t_error"] = precision_report(v, i, rays, c["hits"], nodes)
+    if wide8:
+        h8 = wide8.pop("hits")
+        if not args.no_cpu:
+            wide8["fp64_t_error"] = precision_report(v, i, rays, h8, nodes)
+        line["precision_wide8"] = wide8
     print(json.dumps(line), flush=True)
     ctx.close()
 
