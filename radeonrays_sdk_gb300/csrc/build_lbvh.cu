@@ -707,9 +707,34 @@ __global__ void __launch_bounds__(kBlk) k_batch_reset_flags(BatchArgs b)
     }
 }
 
+// Box of node s for its parent's slot, read without a dependent load: a
+// node's kind follows from its index (binary layout: leaves [n-1, 2n-2]).
+__device__ __forceinline__ void node_box(const BvhNode* nodes, uint32_t s, uint32_t n, F3& lo, F3& hi)
+{
+    const float4* p4 = reinterpret_cast<const float4*>(nodes + s);
+    const float4  w0 = __ldcg(p4), w1 = __ldcg(p4 + 1), w2 = __ldcg(p4 + 2);
+    const F3      a = f3(w0.x, w0.y, w0.z), b = f3(w1.x, w1.y, w1.z), p = f3(w2.x, w2.y, w2.z);
+    if (s >= n - 1)
+    {
+        lo = vmin(vmin(a, b), p);
+        hi = vmax(vmax(a, b), p);
+    }
+    else
+    {
+        const float4 w3 = __ldcg(p4 + 3);
+        lo              = vmin(a, p);
+        hi              = vmax(b, f3(w3.x, w3.y, w3.z));
+    }
+}
+
 // Leaf k of a geometry takes triangle `prim`'s vertices, then climbs: the
 // second child to arrive at a node (atomic flag) writes the node's two child
-// boxes and goes on to its parent (lbvh_fit_aabb_mesh.comp:94-205).
+// boxes and goes on to its parent (lbvh_fit_aabb_mesh.comp:94-205).  The
+// thread carries the box of the subtree it completed, so at a node it reads
+// only the sibling's box; the node's child and parent words (written by the
+// emit, unchanged by the climb) are read before the flag, so those loads
+// overlap the atomic.  The boxes are the reference's: a node's box is the
+// union of its two child boxes, slot 0 first.
 __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, uint32_t n, uint32_t k, uint32_t prim,
                                          DeviceWords* words)
 {
@@ -722,9 +747,10 @@ __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, ui
     __stcg(dst + 1, make_float4(bb.x, bb.y, bb.z, __uint_as_float(prim)));
     __stcg(dst + 2, make_float4(c.x, c.y, c.z, __uint_as_float(parent)));
     __stcg(dst + 3, make_float4(0.f, 0.f, 0.f, __uint_as_float(0u)));
-    uint32_t addr = parent;
+    F3       lo = vmin(vmin(a, bb), c), hi = vmax(vmax(a, bb), c);
+    uint32_t x = leaf, addr = parent;
     // A Karras tree over 2^30 leaves with 32-bit index tie-breaks is at most
-    // 64 levels deep; the bound and the range check only guard against a
+    // 64 levels deep; the bound and the range checks only guard against a
     // corrupted tree (they raise NODE_RANGE instead of faulting or spinning).
     for (int level = 0; addr != kInvalid; ++level)
     {
@@ -733,22 +759,25 @@ __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, ui
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
             return;
         }
-        if (climb_exch(&nodes[addr].update) == 0u) return;
         BvhNode*       nd = nodes + addr;
-        const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1);
-        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1)
+        const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1), up = __ldcg(&nd->parent);
+        if (climb_exch(&nd->update) == 0u) return;
+        if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1 || (c0 != x && c1 != x))
         {
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
             return;
         }
-        F3 lo0, hi0, lo1, hi1;
-        child_box(nodes, c0, lo0, hi0);
-        child_box(nodes, c1, lo1, hi1);
-        // This thread arrived second: the flag is 1 and no other thread
-        // writes this node any more.
-        const uint32_t parent = __ldcg(&nd->parent);
-        store_boxes4(nodes, addr, lo0, hi0, lo1, hi1, c0, c1, parent, 1u);
-        addr = parent;
+        // This thread arrived second: the flag is 1, the sibling's box is
+        // complete, and no other thread writes this node any more.
+        F3 slo, shi;
+        node_box(nodes, c0 == x ? c1 : c0, n, slo, shi);
+        const F3 lo0 = c0 == x ? lo : slo, hi0 = c0 == x ? hi : shi;
+        const F3 lo1 = c0 == x ? slo : lo, hi1 = c0 == x ? shi : hi;
+        store_boxes4(nodes, addr, lo0, hi0, lo1, hi1, c0, c1, up, 1u);
+        lo   = vmin(lo0, lo1);
+        hi   = vmax(hi0, hi1);
+        x    = addr;
+        addr = up;
     }
 }
 
