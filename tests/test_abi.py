@@ -76,7 +76,20 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts), C.byref(req_b)) == 0
     nodes = (2 * 1000 - 1) * 64
     assert req_b.result_buffer_size == (nodes + 255) // 256 * 256 + 256
-    assert req.result_buffer_size > req_b.result_buffer_size  # wide nodes + triangles appended
+    # Default (null options): binary nodes + trailer + 4-wide nodes of 128 B,
+    # capacity (n-1)//3 + n//3 + 1, 256-byte aligned.
+    cap4 = (1000 - 1) // 3 + 1000 // 3 + 1
+    assert req.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 128 + 255) // 256 * 256
+    w8_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_WIDE8, 30, 0)
+    opts8 = rr.RRBuildOptions(1, C.cast(C.pointer(w8_opts), C.c_void_p))
+    req_8 = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts8), C.byref(req_8)) == 0
+    assert req_8.result_buffer_size > req.result_buffer_size > req_b.result_buffer_size
+    # An unknown node format is rejected.
+    bad_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), 3, 30, 0)
+    optsx = rr.RRBuildOptions(1, C.cast(C.pointer(bad_opts), C.c_void_p))
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsx), C.byref(req_8)) == \
+        rr.RR_ERROR_INVALID_PARAMETER
     # An update needs scratch only to collapse the wide nodes again.
     assert req_b.temporary_update_buffer_size == 0
     assert 0 < req.temporary_update_buffer_size < req.temporary_build_buffer_size
