@@ -21,6 +21,8 @@ Reported (one JSON line on rank 0):
                measured HBM copy bandwidth
   build        LBVH + wide collapse of the mesh through rrCmdBuildGeometry
   hit_id_identity  chosen vs plain on every ray
+  any_hit      occlusion rays (same rays, tmax ~ U[0.01, 0.5]): chosen (autotuned
+               for any hit) and plain Mrays/s, hit-flag identity
   precision_wide8  the 8-wide nodes with 8-bit conservative bounds on the fast
                tree: Mrays/s, hit identity against the plain kernel on
                every ray, and its own fp64 t / uv error
@@ -75,6 +77,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-anyhit", action="store_true", help="skip the any-hit (occlusion) measurement")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the 8-wide 8-bit-bounds run (hit identity and fp64 error of that format)")
     ap.add_argument("--e2e-chunk", type=int, default=0,
@@ -444,6 +447,38 @@ def run_ours(args):
                  "hits": h8}
         assert ctx.device_errors() == 0, "device error word set during the 8-wide run"
 
+    # ---- any hit (occlusion): the same origins and directions with
+    # tmax ~ U[0.01, 0.5]; the chosen kernel autotuned for the any-hit query
+    # on the chosen tree, the plain kernel on the fast tree.
+    anyhit = None
+    if not args.no_anyhit and "plain" in out and not args.only:
+        rays_a = rays.copy()
+        rays_a[:, 7] = np.random.default_rng(0x52520001).uniform(0.01, 0.5, R).astype(np.float32)
+        rays_d.copy_(torch.from_numpy(rays_a))
+
+        def any_step():
+            rr.check(L.rrCmdIntersect(ctx.ctx, cur["bvh"], rr.RR_INTERSECT_QUERY_ANY, rb, R, None,
+                                      rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, hitb, sb, ext), "rrCmdIntersect")
+        tuned_a = ctx.autotune(bvh_c, rays_d, query=rr.RR_INTERSECT_QUERY_ANY, hits=hits_d, scratch=scratch_t)
+        res_a = {}
+        for name, trav, tree in (("chosen", tuned_a["traversal"], hcb), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY, hb)):
+            cur["bvh"] = tree
+            ctx.set_traversal(trav, ray_order=tuned_a["ray_order"] if name == "chosen" else 0)
+            per_a, total_a = time_steps(any_step, max(3, args.steps // 3), args.warmup, ws, stream)
+            res_a[name] = {"value": R * ws * max(3, args.steps // 3) / (total_a / 1e3) / 1e6, "unit": "Mrays/s",
+                           "p50_ms": statistics.median(per_a), "p99_ms": float(np.percentile(per_a, 99)),
+                           "hits": hits_d.cpu().numpy().view(np.uint32).copy()}
+        ha, pa = res_a["chosen"].pop("hits"), res_a["plain"].pop("hits")
+        anyhit = {"query": "any hit (occlusion), tmax ~ U[0.01, 0.5], full RRHit output",
+                  "chosen": res_a["chosen"], "plain": res_a["plain"],
+                  "chosen_kernel": KERNELS.get(tuned_a["traversal"], "?"),
+                  "speedup_vs_plain": res_a["chosen"]["value"] / res_a["plain"]["value"],
+                  "hit_flags_identical": bool(np.array_equal(ha[:, 2] != 0xFFFFFFFF, pa[:, 2] != 0xFFFFFFFF)),
+                  "occluded_fraction": float(np.mean(pa[:, 2] != 0xFFFFFFFF))}
+        rays_d.copy_(torch.from_numpy(rays))
+        ctx.set_traversal(chosen_trav, args.block, args.per_sm, ray_order=chosen_order)
+        assert ctx.device_errors() == 0, "device error word set during the any-hit run"
+
     # ---- end to end through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and not args.only:
@@ -538,6 +573,8 @@ def run_ours(args):
         cb, nodes = cpu_baseline(v, i, rays, args.cpu_seconds)
         line["cpu_baseline"] = cb
         line["fp64_t_error"] = precision_report(v, i, rays, c["hits"], nodes)
+    if anyhit:
+        line["any_hit"] = anyhit
     if wide8:
         h8 = wide8.pop("hits")
         if not args.no_cpu:

@@ -16,7 +16,7 @@ def _moved(v, seed):
     return (v * np.float32(1.5) + g.normal(0, 0.003, size=v.shape).astype(np.float32)).astype(np.float32)
 
 
-@pytest.mark.parametrize("fmt", [0, 1])
+@pytest.mark.parametrize("fmt", [0, 1, 2])
 @pytest.mark.parametrize("n", [1, 2, 3, 1000, 40000])
 def test_update_matches_oracle_refit(ctx, orc, fmt, n):
     from radeonrays_sdk_gb300 import scenes
@@ -38,8 +38,9 @@ def test_update_matches_oracle_refit(ctx, orc, fmt, n):
     ref = orc.trace(want, rays)
     assert np.array_equal(trace(ctx, res, rays, traversal=1), ref)
     assert np.array_equal(trace(ctx, res, rays, traversal=3), ref)
-    if fmt == 1:
-        wide = trace(ctx, res, rays, traversal=2)
+    if fmt in (1, 2):
+        # The re-collapsed wide nodes (8-wide or 4-wide) follow the new boxes.
+        wide = trace(ctx, res, rays, traversal=2 if fmt == 1 else 4)
         assert np.array_equal(wide[:, 2] != INVALID, ref[:, 2] != INVALID)
 
 
