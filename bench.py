@@ -205,7 +205,8 @@ def describe(args, ntri):
             "triangles": ntri, "rays_per_gpu": args.rays, "query": "closest", "output": "full_hit",
             "chosen": "autotuned (rrCudaAutotuneTraversal) among the kernels the chosen tree's format allows: "
                       "plain binary, persistent lane-refill binary (reference visit order), and persistent 4-wide "
-                      f"fp32 nodes (format bvh4) or 8-wide 8-bit nodes (format wide8); format here: "
+                      f"fp32 nodes (format bvh4) or 8-wide 8-bit nodes (format wide8), then the winner's resident "
+                      "blocks per SM and (4-wide) shared-stack depth; format here: "
                       f"{args.chosen_format}",
             "plain": "64-byte binary nodes, one thread per ray, reference visit order",
             "l2": "inputs larger than L2 (rays 32 B x rays, BVH > 129 MB); no flush needed",
@@ -372,23 +373,27 @@ def run_ours(args):
     # Chosen path: the autotuner's pick (untimed tuning on the workload's rays)
     # unless a kernel is forced on the command line.
     chosen_trav, chosen_order, tuned = args.chosen, args.ray_order, None
+    chosen_per_sm, chosen_stack = args.per_sm, 0
     if args.chosen == 0 and args.only != "plain":
         tuned = ctx.autotune(bvh_c, rays_d, hits=hits_d, scratch=scratch_t)
         chosen_trav, chosen_order = tuned["traversal"], tuned["ray_order"]
+        chosen_per_sm = args.per_sm or tuned["blocks_per_sm"]
+        chosen_stack = tuned["short_stack"]
     # Fetch counters of each kernel (untimed run) -> algorithmic bytes.
     for name, trav in (("chosen", chosen_trav), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
         if args.only and args.only != name:
             continue
         if name == "plain" and args.no_plain:
             continue
-        shape = (args.block, args.per_sm) if name == "chosen" else (0, 0)
+        shape = (args.block, chosen_per_sm) if name == "chosen" else (0, 0)
         order = chosen_order if name == "chosen" else 0
+        depth = chosen_stack if name == "chosen" else 0
         cur["bvh"] = hcb if name == "chosen" else hb
-        ctx.set_traversal(trav, *shape, collect_stats=1, ray_order=order)
+        ctx.set_traversal(trav, *shape, collect_stats=1, ray_order=order, short_stack=depth)
         trace_step()
         torch.cuda.synchronize()
         st = ctx.stats()
-        ctx.set_traversal(trav, *shape, ray_order=order)
+        ctx.set_traversal(trav, *shape, ray_order=order, short_stack=depth)
         # Bytes per fetch: binary node 64; 8-wide node 80 (+ 48-byte triangles);
         # 4-wide node 128 (+ the 48 bytes of a binary leaf's three vertices).
         node_b = {rr.RR_CUDA_TRAVERSAL_WIDE: 80, rr.RR_CUDA_TRAVERSAL_BVH4: 128}.get(trav, 64)
@@ -463,7 +468,11 @@ def run_ours(args):
         res_a = {}
         for name, trav, tree in (("chosen", tuned_a["traversal"], hcb), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY, hb)):
             cur["bvh"] = tree
-            ctx.set_traversal(trav, ray_order=tuned_a["ray_order"] if name == "chosen" else 0)
+            if name == "chosen":
+                ctx.set_traversal(trav, 0, tuned_a["blocks_per_sm"], ray_order=tuned_a["ray_order"],
+                                  short_stack=tuned_a["short_stack"])
+            else:
+                ctx.set_traversal(trav)
             per_a, total_a = time_steps(any_step, max(3, args.steps // 3), args.warmup, ws, stream)
             res_a[name] = {"value": R * ws * max(3, args.steps // 3) / (total_a / 1e3) / 1e6, "unit": "Mrays/s",
                            "p50_ms": statistics.median(per_a), "p99_ms": float(np.percentile(per_a, 99)),
@@ -476,7 +485,7 @@ def run_ours(args):
                   "hit_flags_identical": bool(np.array_equal(ha[:, 2] != 0xFFFFFFFF, pa[:, 2] != 0xFFFFFFFF)),
                   "occluded_fraction": float(np.mean(pa[:, 2] != 0xFFFFFFFF))}
         rays_d.copy_(torch.from_numpy(rays))
-        ctx.set_traversal(chosen_trav, args.block, args.per_sm, ray_order=chosen_order)
+        ctx.set_traversal(chosen_trav, args.block, chosen_per_sm, ray_order=chosen_order, short_stack=chosen_stack)
         assert ctx.device_errors() == 0, "device error word set during the any-hit run"
 
     # ---- end to end through the C-ABI with pinned host buffers
@@ -485,7 +494,7 @@ def run_ours(args):
         # The chosen kernel, through the host-buffer entry point: H2D of the
         # rays, the traversal and D2H of the hits, in chunks pipelined over
         # three streams, all inside the timed region.
-        ctx.set_traversal(chosen_trav, args.block, args.per_sm, ray_order=chosen_order)
+        ctx.set_traversal(chosen_trav, args.block, chosen_per_sm, ray_order=chosen_order, short_stack=chosen_stack)
         rays_h = torch.from_numpy(rays).pin_memory()
         hits_h = torch.empty((R, 4), dtype=torch.int32).pin_memory()
         rh, hh = C.c_void_p(rays_h.data_ptr()), C.c_void_p(hits_h.data_ptr())
@@ -538,6 +547,8 @@ def run_ours(args):
                      "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R},
         "clocks": c["clocks"], "gpu_launches": args.steps, "build": build, "traversal": key,
         "chosen_kernel": {"kernel": kernel, "traversal": c["trav"], "ray_order": c["order"],
+                          "blocks_per_sm": chosen_per_sm or "occupancy maximum",
+                          "short_stack": chosen_stack or 16,
                           "selected_by": "rrCudaAutotuneTraversal" if tuned else "command line"},
     }
     if "plain" in out and "chosen" in out:
@@ -645,7 +656,11 @@ def run_batch(args):
     # (plain, persistent binary, 4-wide BLASes).
     tuned = ctx.autotune(scene, rays_d, hits=hits_d, scratch=scratch_t)
     for name, trav in (("chosen", tuned["traversal"]), ("plain", rr.RR_CUDA_TRAVERSAL_BINARY)):
-        ctx.set_traversal(trav)
+        if name == "chosen":
+            ctx.set_traversal(trav, 0, tuned["blocks_per_sm"], ray_order=tuned["ray_order"],
+                              short_stack=tuned["short_stack"])
+        else:
+            ctx.set_traversal(trav)
         per, total = time_steps(trace_step, max(3, args.steps // 3), max(3, args.warmup), 1, stream)
         out[name] = {"ms": statistics.median(per), "mrays_s": R / statistics.median(per) / 1e3,
                      "p99_ms": float(np.percentile(per, 99)), "hits": hits_d.cpu().numpy().view(np.uint32).copy()}

@@ -72,7 +72,9 @@ typedef struct
     uint32_t collect_stats;   /* 1 = count node and triangle fetches */
     uint32_t ray_order;       /* wide kernel: 0 = default, 1 = trace in the given order, 2 = sort rays by
                                  direction octant and origin first (batches of 2^20 rays or more) */
-    uint32_t reserved[2];
+    uint32_t short_stack;     /* RR_CUDA_TRAVERSAL_BVH4 single-level kernel: shared-memory stack entries
+                                 per ray, 0 = default (16), else 12..32 (deeper entries spill to scratch) */
+    uint32_t reserved[1];
 } RRCudaTraversalOptions;
 
 /* Fetch counters accumulated while collect_stats is 1. */
@@ -141,6 +143,10 @@ RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
  * rays in the given order and, for batches of 2^20 rays or more, with the
  * rays sorted (WIDE8) -- on the caller's rays (their count is the sample
  * size), three runs each on the context's stream, and keeps the fastest.
+ * Then the winner's launch shape: 4 and 6 resident blocks per SM against
+ * the occupancy maximum (persistent kernels), and for the single-level
+ * 4-wide kernel short stacks of 12 and 24 entries against 16; a variant
+ * replaces the default only when it is at least 1 % faster.
  * Results are cached per (GPU, buffer kind, node format and size, query,
  * output, ray-count octave) in the context and, when the environment
  * variable RR_CUDA_TUNE_CACHE names a file, in that file across processes.

@@ -665,6 +665,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     a.collect_stats = o.collect_stats ? 1 : 0;
     a.block_size    = (int)o.block_size;
     a.blocks_per_sm = (int)o.blocks_per_sm;
+    a.short_stack   = (int)o.short_stack;
     a.ray_order     = (int)o.ray_order;
     a.sm_count      = ctx->sm_count;
     auto    it      = ctx->registry.find((uintptr_t)bvh);
@@ -1678,6 +1679,7 @@ RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversa
     if (options->traversal > RR_CUDA_TRAVERSAL_BVH4 || options->ray_order > 2)
         return RR_ERROR_INVALID_PARAMETER;
     if (options->block_size && (options->block_size % 32 || options->block_size > 1024)) return RR_ERROR_INVALID_PARAMETER;
+    if (options->short_stack && (options->short_stack < 12 || options->short_stack > 32)) return RR_ERROR_INVALID_PARAMETER;
     C(context)->topts = *options;
     return RR_SUCCESS;
 }
@@ -1770,16 +1772,17 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
                 while (std::fgets(line, sizeof(line), f))
                 {
                     char*    tab = std::strchr(line, '\t');
-                    unsigned t = 0, ro = 0, bps = 0;
+                    unsigned t = 0, ro = 0, bps = 0, depth = 0;
                     if (!tab) continue;
                     *tab = 0;
-                    if (key == line && std::sscanf(tab + 1, "%u %u %u", &t, &ro, &bps) == 3)
+                    if (key == line && std::sscanf(tab + 1, "%u %u %u %u", &t, &ro, &bps, &depth) >= 3)
                     {
                         RRCudaTraversalOptions o{};
                         o.struct_size   = sizeof(o);
                         o.traversal     = t;
                         o.ray_order     = ro;
                         o.blocks_per_sm = bps;
+                        o.short_stack   = depth;
                         ctx->tuned[key] = o;
                     }
                 }
@@ -1813,8 +1816,7 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
             check(cudaEventCreate(&e1), "event");
             float best_ms = 1e30f;
             RRCudaTraversalOptions best = cand[0];
-            for (const auto& o : cand)
-            {
+            auto try_cand = [&](const RRCudaTraversalOptions& o, float margin) {
                 Op op = trace_op(ctx, bvh, P(rays)->addr(), ray_count, nullptr, P(hits)->addr(), P(scratch)->addr(),
                                  query, query_output, o);
                 check(op(ctx->stream), "tune warm-up");
@@ -1824,21 +1826,43 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
                 check(cudaEventSynchronize(e1), "event");
                 float ms = 0.f;
                 check(cudaEventElapsedTime(&ms, e0, e1), "event");
-                RR_LOG_INFO("autotune %s: traversal %u order %u -> %.3f ms", key.c_str(), o.traversal, o.ray_order,
-                            ms / 3.f);
-                if (ms < best_ms)
+                RR_LOG_INFO("autotune %s: traversal %u order %u blocks/SM %u stack %u -> %.3f ms", key.c_str(),
+                            o.traversal, o.ray_order, o.blocks_per_sm, o.short_stack, ms / 3.f);
+                if (ms < best_ms * margin)
                 {
                     best_ms = ms;
                     best    = o;
                 }
-            }
+            };
+            // Stage 1: kernel and node width.  Stage 2: the winner's launch
+            // shape (resident blocks per SM, against the occupancy maximum)
+            // and, for the 4-wide kernel, its shared-stack depth; a stage-2
+            // variant must be 1 % faster to replace the default shape, so
+            // run-to-run noise does not move it.
+            for (const auto& o : cand) try_cand(o, 1.0f);
+            const RRCudaTraversalOptions w = best;
+            if (w.traversal != RR_CUDA_TRAVERSAL_BINARY)
+                for (uint32_t bps : {4u, 6u})
+                {
+                    RRCudaTraversalOptions o = w;
+                    o.blocks_per_sm          = bps;
+                    try_cand(o, 0.99f);
+                }
+            if (w.traversal == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom)
+                for (uint32_t depth : {12u, 24u})
+                {
+                    RRCudaTraversalOptions o = w;
+                    o.short_stack            = depth;
+                    try_cand(o, 0.99f);
+                }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             ctx->tuned[key] = best;
             if (cache_path)
                 if (FILE* f = std::fopen(cache_path, "a"))
                 {
-                    std::fprintf(f, "%s\t%u %u %u\n", key.c_str(), best.traversal, best.ray_order, best.blocks_per_sm);
+                    std::fprintf(f, "%s\t%u %u %u %u\n", key.c_str(), best.traversal, best.ray_order,
+                                 best.blocks_per_sm, best.short_stack);
                     std::fclose(f);
                 }
             hit = ctx->tuned.find(key);

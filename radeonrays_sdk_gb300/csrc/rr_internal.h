@@ -303,6 +303,7 @@ struct TraceArgs
     int             collect_stats;
     int             block_size;
     int             blocks_per_sm;
+    int             short_stack;  // 4-wide kernel's shared stack entries per ray (0: kPShort)
     int             sm_count;
     int             box_leaves;   // AABB-list geometry: leaves are boxes
     // Streamed rays (host-buffer tracing, persistent binary kernel only): the

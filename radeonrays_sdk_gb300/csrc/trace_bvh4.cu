@@ -97,15 +97,18 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
 // kStream: the streamed variant for host-buffer tracing (trace_stream.cuh),
 // with the same arrival waits and done counts as the persistent binary
 // kernel's streamed variant.
+// The short stack is dynamic shared memory of kPBlock x depth entries; the
+// depth (12..32, default kPShort) is a launch parameter the autotuner picks.
 template <bool kAny, bool kFull, bool kStats, bool kStream>
-__global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t gcap)
+__global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t gcap, int depth)
 {
-    __shared__ uint32_t s_stack[kPBlock * kPShort];
-    const uint32_t      tglob = blockIdx.x * blockDim.x + threadIdx.x;
-    PStack              st;
-    st.s    = s_stack + threadIdx.x;
-    st.g    = reinterpret_cast<uint32_t*>(a.scratch + kTraceScratchHeader) + (uint64_t)tglob * gcap;
-    st.gcap = gcap;
+    extern __shared__ uint32_t s_stack[];
+    const uint32_t             tglob = blockIdx.x * blockDim.x + threadIdx.x;
+    PStack                     st;
+    st.s     = s_stack + threadIdx.x;
+    st.g     = reinterpret_cast<uint32_t*>(a.scratch + kTraceScratchHeader) + (uint64_t)tglob * gcap;
+    st.gcap  = gcap;
+    st.depth = depth;
     uint32_t*       ray_ctr    = reinterpret_cast<uint32_t*>(a.scratch);
     const uint32_t  lane       = threadIdx.x & 31;
     const uint32_t  lt         = (1u << lane) - 1u;
@@ -234,17 +237,19 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
 template <bool kAny, bool kFull, bool kStats, bool kStream>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
-    auto kern   = k_trace_bvh4<kAny, kFull, kStats, kStream>;
-    int  per_sm = a.blocks_per_sm;
+    auto         kern   = k_trace_bvh4<kAny, kFull, kStats, kStream>;
+    const int    depth  = a.short_stack > 0 ? a.short_stack : kPShort;
+    const size_t smem   = (size_t)kPBlock * depth * sizeof(uint32_t);
+    int          per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, 0) != cudaSuccess) per_sm = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPBlock, smem) != cudaSuccess) per_sm = 1;
         per_sm = per_sm > 0 ? per_sm : 1;
     }
     const PGrid g = persistent_grid(a.sm_count, per_sm, a.ray_count, a.scratch_bytes, kTraceScratchHeader);
     cudaError_t e = cudaMemsetAsync(a.scratch, 0, kTraceScratchHeader, s);
     if (e != cudaSuccess) return e;
-    kern<<<g.blocks, kPBlock, 0, s>>>(a, g.gcap);
+    kern<<<g.blocks, kPBlock, smem, s>>>(a, g.gcap, depth);
     return cudaGetLastError();
 }
 }  // namespace

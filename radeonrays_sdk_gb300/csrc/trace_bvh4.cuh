@@ -13,14 +13,15 @@ constexpr int kB4Spill = 8;
 
 // Make room for `k` (at most 3) more short-stack entries: when they would not
 // fit, the bottom kB4Spill entries go to the global region and the rest move
-// down.
+// down.  A spill happens with sp >= st.depth - 2 >= kB4Spill entries (the
+// depth is at least 12).
 __device__ __forceinline__ void b4_reserve(int& sp, uint32_t& gsp, const PStack& st, DeviceWords* words, int k)
 {
-    if (sp + k <= kPShort) return;
+    if (sp + k <= st.depth) return;
     if (gsp + kB4Spill > st.gcap)
     {
         raise_error(words, RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW);
-        sp = kPShort - k;  // overwrite the top entries: result flagged invalid
+        sp = st.depth - k;  // overwrite the top entries: result flagged invalid
         return;
     }
     for (int j = 0; j < kB4Spill; ++j) st.g[gsp + j] = st.at(j);

@@ -38,6 +38,7 @@ struct PStack
     uint32_t* s;  // this thread's first short-stack entry (shared), entries kPBlock apart
     uint32_t* g;  // global spill region
     uint32_t  gcap;
+    int       depth = kPShort;  // short-stack entries (the 4-wide kernels' helpers read it)
     __device__ __forceinline__ uint32_t& at(int k) const { return s[k * kPBlock]; }
 };
 

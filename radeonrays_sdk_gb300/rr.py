@@ -115,7 +115,7 @@ class RRSceneBuildInput(C.Structure):
 class RRCudaTraversalOptions(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("collect_stats", C.c_uint32), ("ray_order", C.c_uint32),
-                ("reserved", C.c_uint32 * 2)]
+                ("short_stack", C.c_uint32), ("reserved", C.c_uint32 * 1)]
 
 
 class RRCudaTraversalStats(C.Structure):
@@ -543,9 +543,9 @@ class Context:
 
     # -- options and diagnostics
     def set_traversal(self, traversal=RR_CUDA_TRAVERSAL_AUTO, block_size=0, blocks_per_sm=0, collect_stats=0,
-                      ray_order=0):
+                      ray_order=0, short_stack=0):
         o = RRCudaTraversalOptions(C.sizeof(RRCudaTraversalOptions), traversal, block_size, blocks_per_sm,
-                                   collect_stats, ray_order)
+                                   collect_stats, ray_order, short_stack)
         check(self.L.rrCudaSetTraversalOptions(self.ctx, C.byref(o)), "rrCudaSetTraversalOptions")
 
     def autotune(self, bvh, rays, query=RR_INTERSECT_QUERY_CLOSEST, output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT,
@@ -563,7 +563,8 @@ class Context:
         check(self.L.rrCudaAutotuneTraversal(self.ctx, self.ptr(bvh), query, self.ptr(rays), R, output,
                                              self.ptr(hits), self.ptr(scratch), C.byref(o)),
               "rrCudaAutotuneTraversal")
-        return {"traversal": o.traversal, "ray_order": o.ray_order, "blocks_per_sm": o.blocks_per_sm}
+        return {"traversal": o.traversal, "ray_order": o.ray_order, "blocks_per_sm": o.blocks_per_sm,
+                "short_stack": o.short_stack}
 
     def device_errors(self) -> int:
         v = C.c_uint32()

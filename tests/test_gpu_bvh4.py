@@ -108,6 +108,7 @@ def test_bvh4_quality_build_and_autotuner(ctx, orc):
     rd = to_dev(rays)
     tuned = ctx.autotune(res, rd)
     assert tuned["traversal"] in (1, 3, 4)
+    assert tuned["blocks_per_sm"] in (0, 4, 6) and tuned["short_stack"] in (0, 12, 24)
     h = ctx.intersect(res, rd).cpu().numpy().view(np.uint32)
     compare(orc, rays, h, plain, v, i)
     ctx.set_traversal(0)
@@ -132,4 +133,35 @@ def test_bvh4_deep_stacks_spill_and_refill(ctx, orc):
     anyw = orc.trace(nodes, rays, query=1, threads=16)
     got = trace(ctx, res, rays, query=1, traversal=BVH4)
     assert np.array_equal(got[:, 2] != INVALID, anyw[:, 2] != INVALID)
+    assert ctx.device_errors() == 0
+
+
+def test_bvh4_stack_depth_and_launch_shape_keep_hits(ctx, orc):
+    """The short-stack depth (12..32 entries) and the resident blocks per SM
+    are launch parameters the autotuner picks: they change where entries
+    live and how rays are spread over the SMs, never the visit order, so
+    hits are bit-identical to the default launch on the deep-stack mesh
+    (which spills at every depth).  Depths outside 12..32 are rejected."""
+    from gpu_util import to_dev
+    from radeonrays_sdk_gb300 import rr, scenes
+    g = scenes.rng(64)
+    c = np.float32(0.5) + (g.random((20000, 1, 3), dtype=np.float32) - np.float32(0.5)) * np.float32(0.02)
+    v = (c + (g.random((20000, 3, 3), dtype=np.float32) - np.float32(0.5)) * np.float32(0.01)).reshape(-1, 3)
+    i = np.arange(60000, dtype=np.uint32).reshape(-1, 3)
+    rays = scenes.incoherent_rays(20000, (0.49, 0.49, 0.49), (0.51, 0.51, 0.51), scenes.rng(64, 1))
+    res = build(ctx, v, i, node_format=BVH4_FORMAT)
+    rd = to_dev(rays)
+    for query in (0, 1):
+        base = trace(ctx, res, rays, query=query, traversal=BVH4)
+        for bps, depth in ((0, 12), (0, 24), (0, 32), (4, 0), (6, 20)):
+            ctx.set_traversal(BVH4, 0, bps, short_stack=depth)
+            got = ctx.intersect(res, rd, query=query).cpu().numpy().view(np.uint32)
+            ctx.set_traversal(0)
+            assert np.array_equal(got, base), (query, bps, depth)
+    nodes, _, _ = orc.build_mesh(v, i)
+    compare(orc, rays, trace(ctx, res, rays, traversal=BVH4), orc.trace(nodes, rays, threads=16), v, i)
+    for bad in (1, 11, 33, 64):
+        with pytest.raises(rr.RRException):
+            ctx.set_traversal(BVH4, short_stack=bad)
+    ctx.set_traversal(0)
     assert ctx.device_errors() == 0
