@@ -682,6 +682,7 @@ def run_batch(args):
             "trace": out, "chosen_traversal": {"traversal": tuned["traversal"],
                                                "kernel": {1: "k_trace_scene_binary", 3: "k_trace_scene_persistent",
                                                           4: "k_trace_scene_bvh4"}.get(tuned["traversal"], "?"),
+                                               "blocks_per_sm": tuned["blocks_per_sm"] or "occupancy maximum",
                                                "selected_by": "rrCudaAutotuneTraversal"},
             "speedup_vs_plain": out["plain"]["ms"] / out["chosen"]["ms"],
             "hit_flags_identical": flags_equal, "hit_mismatches_vs_plain": mism, "device_errors": int(errors)}
