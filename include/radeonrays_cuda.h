@@ -302,21 +302,40 @@ RR_API RRError rrCudaCmdIntersectBatchHost(RRContext                         con
  * cudaStream_t as void* (0 = default stream); no RRContext is needed.
  *
  * Runs the plain binary-node traversal (the rrCmdIntersect plain kernel, same
- * hits) over `geometry`, a non-empty geometry result buffer written by
- * rrCmdBuildGeometry (binary nodes at offset 0).  Its traversal scratch is a
- * fixed device array of about 32 MiB inside librr.so, which every GPU that
- * loads the library keeps until the process exits; a call takes at most
- * 131072 rays (more returns RR_ERROR_INVALID_PARAMETER).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress): make that
- * first call before any stream capture.  All calls share the one array, so
- * calls that overlap on the GPU race with each other. */
+ * hits) over `geometry`, a geometry result buffer of a TRIANGLE mesh written
+ * by rrCmdBuildGeometry (binary nodes at offset 0; AABB-list geometries and
+ * scene buffers are not supported).  `triangle_count` is the mesh's triangle
+ * count: node indices outside its 2 * triangle_count - 1 binary nodes stop the
+ * ray and raise RR_CUDA_DEVICE_ERROR_NODE_RANGE; 0 is an empty geometry, where
+ * every ray misses.  Its traversal scratch is a fixed device array of about
+ * 32 MiB inside librr.so, which every GPU that loads the library keeps until
+ * the process exits; a call takes at most 131072 rays (more returns
+ * RR_ERROR_INVALID_PARAMETER).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress): make that first call before
+ * any stream capture.  All calls share the one array, so calls that overlap on
+ * the GPU race with each other.
+ *
+ * Device-side errors (RRCudaDeviceError bits: a stack overflow, a node index
+ * out of range) mean the hits of the call are invalid although it returned
+ * RR_SUCCESS; read them with rrCudaGetNoAllocDeviceErrors. */
 RR_API RRError rrCudaIntersectNoAlloc(const void*            geometry,
+                                      uint32_t               triangle_count,
                                       RRIntersectQuery       query,
                                       const void*            rays,
                                       uint32_t               ray_count,
                                       RRIntersectQueryOutput query_output,
                                       void*                  hits,
                                       void*                  cuda_stream);
+
+/* Read and clear the device error word of rrCudaIntersectNoAlloc on the
+ * current device (RRCudaDeviceError bits; no counterpart in the reference
+ * API).  The word lives in the same fixed array: it is zero when the library
+ * loads, every rrCudaIntersectNoAlloc call ORs its errors into it, and this
+ * call reads it after the work already enqueued on `cuda_stream` (synchronises
+ * that stream), then clears it.  Like the calls it reports on, it shares the
+ * one word: a call that overlaps on the GPU with another stream's calls sees
+ * their bits too.  Allocates nothing. */
+RR_API RRError rrCudaGetNoAllocDeviceErrors(void* cuda_stream, uint32_t* error_bits);
 
 #ifdef __cplusplus
 }

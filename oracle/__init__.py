@@ -16,7 +16,11 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF = HERE / "_ref" / "librr_ref.so"
-REF_DIR = Path(os.environ.get("RR_REFERENCE_DIR", "/root/reference")) / "bvh_analyzer"
+# The reference checkout, named only by the environment (no default): where it
+# is unset, the harness around the reference's own traversal is not built and
+# the checks that need it skip.
+_REF_ROOT = os.environ.get("RR_REFERENCE_DIR")
+REF_DIR = Path(_REF_ROOT) / "bvh_analyzer" if _REF_ROOT else None
 
 NODE_DTYPE = np.dtype([("a0", "<f4", 3), ("child0", "<u4"), ("a1", "<f4", 3), ("child1", "<u4"),
                        ("b0", "<f4", 3), ("parent", "<u4"), ("b1", "<f4", 3), ("update", "<u4")])
@@ -28,7 +32,10 @@ _ref = None
 
 def build() -> None:
     """Compile liboracle.so (and _ref/librr_ref.so where the reference checkout exists)."""
-    subprocess.run(["make", "-s", "-C", str(HERE), f"REF_DIR={REF_DIR}"], check=True)
+    args = ["make", "-s", "-C", str(HERE)]
+    if REF_DIR is not None:
+        args.append(f"REF_DIR={REF_DIR}")
+    subprocess.run(args, check=True)
 
 
 def _p(a):

@@ -10,6 +10,9 @@
 // pass their own rays, BVH and hit buffers; only the traversal scratch (the
 // per-ray spill stack and the device error word) comes from here.
 //
+// The device error word of these calls lives in the array too (no context
+// holds it): rrCudaGetNoAllocDeviceErrors reads and clears it.
+//
 // The array is a file-scope static __device__ variable: every GPU that loads
 // librr.so holds kNoAllocScratchBytes for it until the process exits.  Host
 // code may not use the array's name as a device address; the first call on
@@ -62,14 +65,15 @@ cudaError_t scratch_address(uint8_t** out)
 
 using namespace rr;
 
-extern "C" RR_API RRError rrCudaIntersectNoAlloc(const void* geometry, RRIntersectQuery query, const void* rays,
-                                                 uint32_t ray_count, RRIntersectQueryOutput query_output, void* hits,
-                                                 void* cuda_stream)
+extern "C" RR_API RRError rrCudaIntersectNoAlloc(const void* geometry, uint32_t triangle_count, RRIntersectQuery query,
+                                                 const void* rays, uint32_t ray_count,
+                                                 RRIntersectQueryOutput query_output, void* hits, void* cuda_stream)
 {
     if (!geometry || !rays || !hits) return RR_ERROR_INVALID_PARAMETER;
     if (query != RR_INTERSECT_QUERY_CLOSEST && query != RR_INTERSECT_QUERY_ANY) return RR_ERROR_INVALID_PARAMETER;
     if (query_output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && query_output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
         return RR_ERROR_INVALID_PARAMETER;
+    if (triangle_count > 0x7fffffffu) return RR_ERROR_INVALID_PARAMETER;  // 2N - 1 binary nodes must fit 32 bits
     if (ray_count > kNoAllocMaxRays)
     {
         std::fprintf(stderr,
@@ -87,9 +91,9 @@ extern "C" RR_API RRError rrCudaIntersectNoAlloc(const void* geometry, RRInterse
         return RR_ERROR_INTERNAL;
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
-    // The error/counter words carry the previous call's values: clear them.
-    e = cudaMemsetAsync(base, 0, kNoAllocWordsBytes, s);
-    if (e != cudaSuccess) return RR_ERROR_INTERNAL;
+    // The error word is sticky (zero when the library loads, read and cleared
+    // by rrCudaGetNoAllocDeviceErrors); the plain kernel keeps no other state
+    // between calls: its spill stacks are written before they are read.
     TraceArgs a{};
     a.bvh           = reinterpret_cast<const uint8_t*>(geometry);
     a.rays          = reinterpret_cast<const uint8_t*>(rays);
@@ -99,10 +103,35 @@ extern "C" RR_API RRError rrCudaIntersectNoAlloc(const void* geometry, RRInterse
     a.scratch_bytes = kNoAllocScratchBytes - kNoAllocWordsBytes;
     a.query         = query;
     a.output        = query_output;
-    a.node_limit    = kInvalid;
+    a.empty         = triangle_count == 0;
+    a.node_limit    = triangle_count == 0 ? 0u : 2u * triangle_count - 1u;
     a.words         = reinterpret_cast<DeviceWords*>(base);
     static_assert(sizeof(DeviceWords) <= kNoAllocWordsBytes, "words fit in front of the scratch");
     e = launch_trace_binary(a, s);
     if (e != cudaSuccess) return RR_ERROR_INTERNAL;
+    return RR_SUCCESS;
+}
+
+extern "C" RR_API RRError rrCudaGetNoAllocDeviceErrors(void* cuda_stream, uint32_t* error_bits)
+{
+    if (!error_bits) return RR_ERROR_INVALID_PARAMETER;
+    uint8_t*    base = nullptr;
+    cudaError_t e    = scratch_address(&base);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return RR_ERROR_INTERNAL;
+    }
+    cudaStream_t s    = reinterpret_cast<cudaStream_t>(cuda_stream);
+    uint32_t*    word = &reinterpret_cast<DeviceWords*>(base)->error_bits;
+    uint32_t     v    = 0;
+    // Ordered after the calls on this stream; the clear is ordered after the read.
+    if (cudaMemcpyAsync(&v, word, sizeof(v), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemsetAsync(word, 0, sizeof(v), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return RR_ERROR_INTERNAL;
+    }
+    *error_bits = v;
     return RR_SUCCESS;
 }

@@ -173,7 +173,8 @@ PROTOTYPES = {
     "rrCudaGetDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaGetTraversalStats": [_P, C.POINTER(RRCudaTraversalStats)],
     "rrCudaSetWaitTimeout": [_P, C.c_uint32],
-    "rrCudaIntersectNoAlloc": [_P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
+    "rrCudaIntersectNoAlloc": [_P, C.c_uint32, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
+    "rrCudaGetNoAllocDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaAutotuneTraversal": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P,
                                 C.POINTER(RRCudaTraversalOptions)],
     "rrCudaCmdBuildGeometries": [_P, C.c_uint32, C.POINTER(RRGeometryBuildInput), C.POINTER(RRBuildOptions), _PP,

@@ -130,3 +130,24 @@ def test_log_controls(rrlib, tmp_path):
     assert rrlib.rrSetLogLevel(rr.RR_LOG_LEVEL_ERROR) == 0
     assert rrlib.rrSetLogFile(str(tmp_path / "rr.log").encode()) == 0
     assert rrlib.rrSetLogLevel(rr.RR_LOG_LEVEL_WARN) == 0
+
+
+def test_no_alloc_argument_checks(rrlib):
+    """rrCudaIntersectNoAlloc and its error reader reject bad arguments before
+    any device call; an empty batch is a successful no-op."""
+    from radeonrays_sdk_gb300 import rr
+    E = rr.RR_ERROR_INVALID_PARAMETER
+    fake = C.c_void_p(0x1000)  # never dereferenced: every call below returns before touching a device
+    f = rrlib.rrCudaIntersectNoAlloc
+    CL, FULL = rr.RR_INTERSECT_QUERY_CLOSEST, rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT
+    assert f(None, 10, CL, fake, 1, FULL, fake, None) == E
+    assert f(fake, 10, CL, None, 1, FULL, fake, None) == E
+    assert f(fake, 10, CL, fake, 1, FULL, None, None) == E
+    assert f(fake, 10, 7, fake, 1, FULL, fake, None) == E
+    assert f(fake, 10, CL, fake, 1, 9, fake, None) == E
+    assert f(fake, 0x80000000, CL, fake, 1, FULL, fake, None) == E  # 2N - 1 nodes would not fit 32 bits
+    assert f(fake, 10, CL, fake, 131_073, FULL, fake, None) == E    # beyond the fixed scratch
+    assert f(fake, 10, CL, fake, 0, FULL, fake, None) == rr.RR_SUCCESS
+    assert f(fake, 10, rr.RR_INTERSECT_QUERY_ANY, fake, 0, rr.RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID, fake,
+             None) == rr.RR_SUCCESS
+    assert rrlib.rrCudaGetNoAllocDeviceErrors(None, None) == E

@@ -52,7 +52,8 @@ def test_reference_bvh_analyzer_accepts_exported_tree(orc, tmp_path):
     buf, nodes = _host_buffer(orc, 5000)
     rays = scenes.pinhole_rays(64, 64)
     cfg = bvh_io.export_bvh_analyzer(tmp_path, "soup", buf, 5000, rays, width=64)
-    r = subprocess.run([str(ANALYZER), str(cfg)], capture_output=True, text=True, timeout=300)
+    # The tool writes its images into its working directory: keep them in tmp_path.
+    r = subprocess.run([str(ANALYZER), str(cfg)], capture_output=True, text=True, timeout=300, cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert "is_valid: 1" in r.stdout
     assert "Triangles: 5000" in r.stdout and "Internal nodes: 4999" in r.stdout
