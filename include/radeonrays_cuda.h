@@ -47,9 +47,12 @@ typedef struct
 /* ---- traversal kernel selection ---------------------------------------- */
 typedef enum
 {
-    /* The persistent binary kernel (single- or two-level); its hits are
-     * bit-identical to RR_CUDA_TRAVERSAL_BINARY.  rrCudaAutotuneTraversal
-     * replaces it with the fastest kernel for a workload. */
+    /* The default: on a triangle geometry buffer with 4-wide nodes
+     * (RR_CUDA_NODE_FORMAT_BVH4, the default build format) the 4-wide kernel
+     * (RR_CUDA_TRAVERSAL_BVH4); on every other buffer (scenes included) the
+     * persistent binary kernel, whose hits are bit-identical to
+     * RR_CUDA_TRAVERSAL_BINARY.  rrCudaAutotuneTraversal replaces it with the
+     * fastest kernel for a workload. */
     RR_CUDA_TRAVERSAL_AUTO = 0,
     /* One thread per ray, 64-byte binary nodes, reference visit order. */
     RR_CUDA_TRAVERSAL_BINARY = 1,
@@ -94,7 +97,8 @@ typedef enum
     RR_CUDA_DEVICE_ERROR_BAD_BUFFER       = 2, /* the BVH buffer header did not match */
     RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH   = 4, /* wide collapse ran out of levels */
     RR_CUDA_DEVICE_ERROR_NODE_RANGE       = 8, /* a node index left the node array */
-    RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT     = 16 /* a bounded device wait ran out (result invalid) */
+    RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT     = 16 /* a bounded device wait ran out (rrCudaSetWaitLimits says which
+                                                  results stay valid) */
 } RRCudaDeviceError;
 
 /* Wrap a CUDA device pointer (plus byte offset) as an RRDevicePtr.  The caller
@@ -135,6 +139,32 @@ RR_API RRError rrCudaGetTraversalStats(RRContext context, RRCudaTraversalStats* 
 /* Milliseconds rrWaitEvent polls before it gives up with RR_ERROR_INTERNAL
  * (default 600000).  The reference waits forever (vlk/device.cpp:249-272). */
 RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds);
+
+/* Limits of the bounded device waits, and hooks that make them run out in
+ * tests (no reference counterpart: the reference's waits are host-side and
+ * unbounded, vlk/device.cpp:249-272).  Every device-side wait of this build
+ * gives up after its limit, raises RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT in the
+ * context's error word (rrCudaGetDeviceErrors) and carries on:
+ *   the onesweep look-back of the LBVH sort (a tile waiting for an earlier
+ *     tile's digit counts) then counts the earlier tiles' keys itself, so the
+ *     sort stays exact;
+ *   the streamed host-buffer trace (a warp waiting for its rays' arrival
+ *     flag) finishes those rays as misses (inst_id = ~0), and the hits are
+ *     invalid.
+ * A zero limit selects the default.  The test_* fields never occur in normal
+ * use: they withhold a signal so that a test can watch a wait run out. */
+typedef struct
+{
+    uint32_t struct_size;             /* sizeof(RRCudaWaitLimits) */
+    uint32_t lookback_polls;          /* look-back polls per earlier tile, 0 = 2^22 */
+    uint32_t arrival_polls;           /* arrival-flag polls of about 1 us each, 0 = 2^21 */
+    uint32_t test_hold_sort_tile;     /* this sort tile never publishes its counts; RR_INAVLID_VALUE = none */
+    uint32_t test_drop_arrival_chunk; /* this chunk's arrival flag is never raised; RR_INAVLID_VALUE = none */
+} RRCudaWaitLimits;
+
+/* Set the context's wait limits (and test hooks) for later work; it waits
+ * for the work already submitted on the context's internal stream. */
+RR_API RRError rrCudaSetWaitLimits(RRContext context, const RRCudaWaitLimits* limits);
 
 /* Pick the fastest traversal for a workload and make it this context's
  * traversal option (no reference counterpart: the reference has one kernel

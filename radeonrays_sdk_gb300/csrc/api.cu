@@ -202,6 +202,11 @@ struct Context
     void* write_value = nullptr;
     void* wait_value  = nullptr;
     bool  stream_rays = true;
+    // Bounded device waits (rrCudaSetWaitLimits): arrival polls of a streamed
+    // trace (0: default) and the test hook that never raises one chunk's
+    // arrival flag (kInvalid: none).  The look-back limit lives in `words`.
+    uint32_t arrival_polls = 0;
+    uint32_t drop_arrival  = kInvalid;
     void ensure_pipe()
     {
         if (pipe_fork) return;
@@ -668,6 +673,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     a.short_stack   = (int)o.short_stack;
     a.ray_order     = (int)o.ray_order;
     a.sm_count      = ctx->sm_count;
+    a.stream_polls  = ctx->arrival_polls;
     auto    it      = ctx->registry.find((uintptr_t)bvh);
     BufInfo bi;
     if (it != ctx->registry.end()) bi = it->second;
@@ -697,10 +703,13 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     // from the root like the reference (vlk/intersector.cpp:290).
     a.empty             = (bi.kind == kKindGeom && bi.n == 0);
     const bool has_wide = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0;
-    // AUTO: the persistent binary kernel (the fastest on incoherent rays,
-    // bit-identical to BINARY); rrCudaAutotuneTraversal refines the choice
-    // per workload.
-    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || trav == RR_CUDA_TRAVERSAL_AUTO)
+    // AUTO: the 4-wide kernel on a triangle geometry with 4-wide nodes (the
+    // default format; the fastest kernel on incoherent rays), else the
+    // persistent binary kernel (bit-identical to BINARY);
+    // rrCudaAutotuneTraversal refines the choice per workload.
+    const bool has_bvh4 = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+                          bi.prim_kind == kPrimTriangles;
+    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || (trav == RR_CUDA_TRAVERSAL_AUTO && !has_bvh4))
     {
         if (sp)
         {
@@ -714,8 +723,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         }
         return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
     }
-    if (trav == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
-        bi.prim_kind == kPrimTriangles)
+    if ((trav == RR_CUDA_TRAVERSAL_BVH4 || trav == RR_CUDA_TRAVERSAL_AUTO) && has_bvh4)
     {
         a.bvh4_nodes = reinterpret_cast<const Bvh4Node*>(bvh + bi.wide_off);
         a.wide_limit = (uint32_t)bi.wide_capacity;
@@ -785,6 +793,7 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
     cudaEvent_t    fork = ctx->pipe_fork, j_in = ctx->pipe_join[0], j_out = ctx->pipe_join[1];
     uint32_t*      words = sp.words;
     const uint32_t nch = sp.chunks, nparts = sp.parts, pshift = sp.part_shift;
+    const uint32_t drop = ctx->drop_arrival;  // test hook: this chunk's flag is never raised
     const size_t   hs  = output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? 16 : 4;
     return [=](cudaStream_t s) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(words, 0, wbytes, s);
@@ -797,7 +806,7 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
             const uint64_t off = (uint64_t)c << shift;
             const uint64_t n   = std::min<uint64_t>(1ull << shift, ray_count - off);
             e = cudaMemcpyAsync(dr + 32 * off, host_rays + 32 * off, 32 * n, cudaMemcpyHostToDevice, in);
-            if (e == cudaSuccess &&
+            if (e == cudaSuccess && c != drop &&
                 wr((CUstream)in, (CUdeviceptr)(uintptr_t)(words + c), 1u, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
                 e = cudaErrorUnknown;
         }
@@ -1730,6 +1739,24 @@ RR_API RRError rrCudaSetWaitTimeout(RRContext context, uint32_t milliseconds)
     if (!context) return RR_ERROR_INVALID_PARAMETER;
     C(context)->wait_ms = milliseconds;
     return RR_SUCCESS;
+}
+
+RR_API RRError rrCudaSetWaitLimits(RRContext context, const RRCudaWaitLimits* limits)
+{
+    if (!context || !limits || limits->struct_size < sizeof(RRCudaWaitLimits)) return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        // The device words are read by kernels: change them in stream order.
+        const uint32_t w[2] = {limits->lookback_polls,
+                               limits->test_hold_sort_tile == kInvalid ? 0u : limits->test_hold_sort_tile + 1u};
+        check(cudaMemcpyAsync(&ctx->words->lookback_polls, w, sizeof(w), cudaMemcpyHostToDevice, ctx->stream),
+              "wait limits");
+        check(cudaStreamSynchronize(ctx->stream), "wait limits");
+        ctx->arrival_polls = limits->arrival_polls;
+        ctx->drop_arrival  = limits->test_drop_arrival_chunk;
+        return RR_SUCCESS;
+    })
 }
 
 RR_API RRError rrCudaAutotuneTraversal(RRContext              context,

@@ -239,8 +239,9 @@ SceneLayout scene_layout(uint32_t n);
 struct DeviceWords
 {
     uint32_t error_bits;
-    uint32_t probe;  // written by the stream memory-operation probe
-    uint32_t pad[2];
+    uint32_t probe;           // written by the stream memory-operation probe
+    uint32_t lookback_polls;  // onesweep look-back polls before giving up (0: kLookbackPolls)
+    uint32_t hold_tile;       // test only: 1 + the sort tile that never publishes its counts (0: none)
     unsigned long long rays;
     unsigned long long node_fetches;
     unsigned long long tri_fetches;
@@ -306,6 +307,7 @@ struct TraceArgs
     int             short_stack;  // 4-wide kernel's shared stack entries per ray (0: kPShort)
     int             sm_count;
     int             box_leaves;   // AABB-list geometry: leaves are boxes
+    int             triangle_test;  // RRCudaTriangleTest
     // Streamed rays (host-buffer tracing, persistent binary kernel only): the
     // rays arrive in chunks of 2^stream_shift while the kernel runs, and the
     // hits leave in parts of 2^stream_part_shift rays (a part is a whole
@@ -319,6 +321,7 @@ struct TraceArgs
     uint32_t        stream_chunks;
     uint32_t        stream_part_shift;
     uint32_t        stream_parts;
+    uint32_t        stream_polls;  // arrival-flag polls (about 1 us each) before giving up (0: default)
 };
 // Words of a streamed trace (arrival flags, done counters, give-up flag),
 // rounded up to 256 bytes.

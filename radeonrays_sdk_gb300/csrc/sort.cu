@@ -13,8 +13,11 @@
 //      primitives, publishes its per-digit counts, looks back over earlier
 //      tiles (decoupled look-back) for its per-digit prefix, and scatters
 //      through shared memory.
-// Every look-back wait is bounded; on exhaustion the kernel raises
-// RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT and carries on (no hang, result invalid).
+// Every look-back wait is bounded (DeviceWords::lookback_polls, default
+// kLookbackPolls).  A block whose wait runs out raises
+// RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT and finds its digit prefix the slow way:
+// it counts the digits of every key of the earlier tiles itself.  No hang,
+// and the sort stays exact.
 #include <algorithm>
 #include <utility>
 
@@ -31,7 +34,7 @@ constexpr int      kWarps     = kBlock / 32;
 constexpr uint32_t kFlagAgg   = 1u << 30;
 constexpr uint32_t kFlagInc   = 2u << 30;
 constexpr uint32_t kValMask   = (1u << 30) - 1;
-constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kLookbackPolls = 1u << 22;
 
 template <class K>
 struct Cfg;
@@ -194,6 +197,10 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(Seg seg, int shift, uint32_
     uint32_t*             lookback      = sv.lookback;
     const uint32_t        tile          = sv.tile;
     const uint64_t base = (uint64_t)tile * kTile + (uint64_t)w * 32 * kKpt;
+    // Wait limit of the look-back, and the test hook of the bounded wait (a
+    // tile that never publishes its counts, so that later tiles run out).
+    const uint32_t polls = words->lookback_polls ? words->lookback_polls : kLookbackPolls;
+    const bool     held  = words->hold_tile == tile + 1u;
 
     K        key[kKpt];
     uint32_t rank[kKpt];
@@ -236,8 +243,12 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(Seg seg, int shift, uint32_
             tot += c;
         }
         // Publish this tile's count (tile 0 publishes its inclusive prefix).
+        // A held tile (test of the bounded wait) publishes nothing.
         uint32_t* mine = lookback + (uint64_t)tile * kRadix + d;
-        if (tile == 0)
+        if (held)
+        {
+        }
+        else if (tile == 0)
             atomicExch(mine, kFlagInc | tot);
         else
             atomicExch(mine, kFlagAgg | tot);
@@ -258,32 +269,53 @@ __global__ void __launch_bounds__(kBlock) k_onesweep(Seg seg, int shift, uint32_
     }
     // Decoupled look-back for this digit.
     {
-        const int d    = tid;
-        uint32_t  excl = 0;
+        const int d         = tid;
+        uint32_t  excl      = 0;
+        bool      timed_out = false;
         if (tile > 0)
         {
             int64_t j = (int64_t)tile - 1;
-            while (j >= 0)
+            while (j >= 0 && !timed_out)
             {
                 const volatile uint32_t* p = lookback + (uint64_t)j * kRadix + d;
                 uint32_t                 v = *p;
                 uint32_t                 spins = 0;
                 while ((v & ~kValMask) == 0)
                 {
-                    if (++spins > kSpinLimit)
+                    if (++spins > polls)
                     {
-                        atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT);
-                        v = kFlagInc;
+                        timed_out = true;
                         break;
                     }
                     if (spins > 64) __nanosleep(32);
                     v = *p;
                 }
+                if (timed_out) break;
                 excl += v & kValMask;
                 if ((v & ~kValMask) == kFlagInc) break;
                 --j;
             }
-            atomicExch(lookback + (uint64_t)tile * kRadix + d, kFlagInc | (excl + tot));
+            if (!timed_out && !held) atomicExch(lookback + (uint64_t)tile * kRadix + d, kFlagInc | (excl + tot));
+        }
+        // A wait that ran out (an earlier tile never published): the block
+        // counts the digits of every key before this tile (global_base is a
+        // free 256-bin histogram here) and the timed-out digits take their
+        // prefix from it.  Exact, only slow.
+        if (__syncthreads_or(timed_out))
+        {
+            global_base[d] = 0;
+            __syncthreads();
+            const uint64_t before = (uint64_t)tile * kTile;
+            for (uint64_t i = (uint64_t)tid; i < before; i += kBlock)
+                atomicAdd(&global_base[(uint32_t)(kin[i] >> shift) & 0xffu], 1u);
+            __syncthreads();
+            if (timed_out)
+            {
+                excl = global_base[d];
+                atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_WAIT_TIMEOUT);
+                if (!held) atomicExch(lookback + (uint64_t)tile * kRadix + d, kFlagInc | (excl + tot));
+            }
+            __syncthreads();  // every digit read its count before global_base is rewritten
         }
         global_base[d] = digit_offsets[d] + excl;
     }

@@ -32,7 +32,7 @@ namespace rr
 namespace
 {
 using namespace stream_detail;
-template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream>
+template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream, bool kPrecise>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, uint32_t gcap)
 {
     __shared__ uint32_t s_stack[kPBlock * kPShort];
@@ -110,6 +110,9 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         const NodeView nd = load_binary_node(nodes, s.caddr);
                         if (kBox)
                             write_box_hit<kFull>(a.hits, gid, 0u, nd.child1, nd.child1);
+                        else if (kPrecise)
+                            write_hit_precise<kFull>(a.hits, gid, s.ray, nd.l0, nd.h0, nd.l1, 0u, nd.child1,
+                                                     nd.child1);
                         else
                             write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1,
                                              nd.child1);
@@ -138,7 +141,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         {
                             active = true;
                             nf     = 0;
-                            p_start(s, load_ray_cg(a.rays, gid));
+                            p_start<kPrecise>(s, load_ray_cg(a.rays, gid));
                         }
                         else
                         {
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                     {
                         active = true;
                         nf     = 0;
-                        p_start(s, a.rays, gid);
+                        p_start<kPrecise>(s, a.rays, gid);
                     }
                 }
             }
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        if (active && p_step<kAny, false, kBox>(s, nodes, a.node_limit, st, a.words, nf))
+        if (active && p_step<kAny, false, kBox, kPrecise>(s, nodes, a.node_limit, st, a.words, nf))
         {
             active  = false;
             pending = true;
@@ -173,10 +176,10 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
     }
 }
 
-template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream>
+template <bool kAny, bool kFull, bool kStats, bool kBox, bool kStream, bool kPrecise = false>
 cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 {
-    auto kern   = k_trace_persistent<kAny, kFull, kStats, kBox, kStream>;
+    auto kern   = k_trace_persistent<kAny, kFull, kStats, kBox, kStream, kPrecise>;
     int  per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {
@@ -190,16 +193,26 @@ cudaError_t go2(const TraceArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// Triangle leaves: the reference's test, or the precise one; box leaves have
+// no precise variant (their hit is the slab entry distance).
+template <bool kAny, bool kFull, bool kStats, bool kStream>
+cudaError_t go_tri(const TraceArgs& a, cudaStream_t s)
+{
+    if (a.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT)
+        return go2<kAny, kFull, kStats, false, kStream, true>(a, s);
+    return go2<kAny, kFull, kStats, false, kStream>(a, s);
+}
+
 template <bool kAny, bool kFull, bool kStats>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
-    return a.box_leaves ? go2<kAny, kFull, kStats, true, false>(a, s) : go2<kAny, kFull, kStats, false, false>(a, s);
+    return a.box_leaves ? go2<kAny, kFull, kStats, true, false>(a, s) : go_tri<kAny, kFull, kStats, false>(a, s);
 }
 
 template <bool kAny, bool kFull>
 cudaError_t go_stream(const TraceArgs& a, cudaStream_t s)
 {
-    return a.box_leaves ? go2<kAny, kFull, false, true, true>(a, s) : go2<kAny, kFull, false, false, true>(a, s);
+    return a.box_leaves ? go2<kAny, kFull, false, true, true>(a, s) : go_tri<kAny, kFull, false, true>(a, s);
 }
 }  // namespace
 

@@ -11,6 +11,7 @@
 #pragma once
 #include "rr_internal.h"
 #include "trace_common.cuh"
+#include "trace_precise.cuh"
 
 namespace rr
 {
@@ -42,10 +43,13 @@ struct PStack
     __device__ __forceinline__ uint32_t& at(int k) const { return s[k * kPBlock]; }
 };
 
+// kPrecise: the precise triangle test's traversal (trace_precise.cuh): the
+// exact reciprocal of the direction and slab distances (p - o) * inv.
+template <bool kPrecise = false>
 __device__ __forceinline__ void p_start(PRay& s, const Ray& r)
 {
     s.ray   = r;
-    s.inv   = safe_invdir(s.ray.d);
+    s.inv   = kPrecise ? exact_invdir(s.ray.d) : safe_invdir(s.ray.d);
     s.oxi   = f3(-s.ray.o.x * s.inv.x, -s.ray.o.y * s.inv.y, -s.ray.o.z * s.inv.z);
     s.ct    = s.ray.tmax;
     s.caddr = kInvalid;
@@ -53,13 +57,19 @@ __device__ __forceinline__ void p_start(PRay& s, const Ray& r)
     s.gsp = s.steps = 0;
     s.sp            = 0;
 }
-__device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i) { p_start(s, load_ray(rays, i)); }
+template <bool kPrecise = false>
+__device__ __forceinline__ void p_start(PRay& s, const uint8_t* rays, uint32_t i)
+{
+    p_start<kPrecise>(s, load_ray(rays, i));
+}
 
 // One iteration of the reference's traversal loop.  Returns true when the ray
 // is finished (stack empty, or a hit accepted by an any-hit query).  The
 // query is kAny, or `any` when kRuntime (requests of both kinds mixed); the
 // leaves are boxes (AABB-list geometry) when kBox, or `box` when kRuntime.
-template <bool kAny, bool kRuntime = false, bool kBox = false>
+// kPrecise: the conservative box test and the precise triangle test
+// (trace_precise.cuh) in the same visit order.
+template <bool kAny, bool kRuntime = false, bool kBox = false, bool kPrecise = false>
 __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ nodes, uint32_t node_limit,
                                        const PStack& st, DeviceWords* words, uint32_t& nf, bool any = false,
                                        bool box = false)
@@ -77,8 +87,16 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
     if (nd.child0 != kInvalid)
     {
         float a0, a1, b0, b1;
-        isect_box(nd.l0, nd.h0, s.inv, s.oxi, s.ct, s.ray.tmin, a0, a1);
-        isect_box(nd.l1, nd.h1, s.inv, s.oxi, s.ct, s.ray.tmin, b0, b1);
+        if (kPrecise)
+        {
+            isect_box_robust(nd.l0, nd.h0, s.inv, s.ray.o, s.ct, s.ray.tmin, a0, a1);
+            isect_box_robust(nd.l1, nd.h1, s.inv, s.ray.o, s.ct, s.ray.tmin, b0, b1);
+        }
+        else
+        {
+            isect_box(nd.l0, nd.h0, s.inv, s.oxi, s.ct, s.ray.tmin, a0, a1);
+            isect_box(nd.l1, nd.h1, s.inv, s.oxi, s.ct, s.ray.tmin, b0, b1);
+        }
         const bool tc0 = a0 <= a1, tc1 = b0 <= b1;
         const bool c1f = tc1 && (a0 > b0);
         if (tc0 || tc1)
@@ -111,6 +129,7 @@ __device__ __forceinline__ bool p_step(PRay& s, const BvhNode* __restrict__ node
     else
     {
         const float t = (kBox || (kRuntime && box)) ? isect_leaf_box(s.ray, s.inv, s.oxi, nd.l0, nd.h0, s.ct)
+                        : kPrecise                  ? isect_tri_precise(s.ray, nd.l0, nd.h0, nd.l1, s.ct)
                                                     : isect_tri(s.ray, nd.l0, nd.h0, nd.l1, s.ct);
         if (t < s.ct)
         {

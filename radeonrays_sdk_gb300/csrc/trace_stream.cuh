@@ -9,7 +9,8 @@ namespace rr
 {
 namespace stream_detail
 {
-// Bounded wait for a chunk's arrival flag: about 2^21 polls of ~1 us.  After
+// Bounded wait for a chunk's arrival flag: about 2^21 polls of ~1 us (the
+// context's wait limits can shorten it: rrCudaSetWaitLimits).  After
 // one lane has given up (the copy never landed), every later wait fails at
 // once, so a stuck copy costs one timeout, not one per ray.
 //
@@ -32,7 +33,8 @@ __device__ __noinline__ static int wait_arrival(const TraceArgs& a, uint32_t hi)
     const uint32_t  g       = hi & ~3u;
     const uint4*    quad    = reinterpret_cast<const uint4*>(a.stream_words + g);
     const uint32_t* gave_up = a.stream_words + a.stream_chunks + a.stream_parts;
-    for (uint32_t k = 0; k < kArrivalPolls; ++k)
+    const uint32_t  polls   = a.stream_polls ? a.stream_polls : kArrivalPolls;
+    for (uint32_t k = 0; k < polls; ++k)
     {
         uint4 f;
         asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"

@@ -118,6 +118,11 @@ class RRCudaTraversalOptions(C.Structure):
                 ("short_stack", C.c_uint32), ("reserved", C.c_uint32 * 1)]
 
 
+class RRCudaWaitLimits(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("lookback_polls", C.c_uint32), ("arrival_polls", C.c_uint32),
+                ("test_hold_sort_tile", C.c_uint32), ("test_drop_arrival_chunk", C.c_uint32)]
+
+
 class RRCudaTraversalStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("node_fetches", C.c_uint64), ("triangle_fetches", C.c_uint64),
                 ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64)]
@@ -173,6 +178,7 @@ PROTOTYPES = {
     "rrCudaGetDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaGetTraversalStats": [_P, C.POINTER(RRCudaTraversalStats)],
     "rrCudaSetWaitTimeout": [_P, C.c_uint32],
+    "rrCudaSetWaitLimits": [_P, C.POINTER(RRCudaWaitLimits)],
     "rrCudaIntersectNoAlloc": [_P, C.c_uint32, C.c_int, _P, C.c_uint32, C.c_int, _P, _P],
     "rrCudaGetNoAllocDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaAutotuneTraversal": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P,
@@ -566,6 +572,14 @@ class Context:
               "rrCudaAutotuneTraversal")
         return {"traversal": o.traversal, "ray_order": o.ray_order, "blocks_per_sm": o.blocks_per_sm,
                 "short_stack": o.short_stack}
+
+    def set_wait_limits(self, lookback_polls=0, arrival_polls=0, hold_sort_tile=RR_INVALID,
+                        drop_arrival_chunk=RR_INVALID):
+        """Limits of the bounded device waits, and the test hooks that make
+        them run out (rrCudaSetWaitLimits); no arguments restore the defaults."""
+        w = RRCudaWaitLimits(C.sizeof(RRCudaWaitLimits), lookback_polls, arrival_polls, hold_sort_tile,
+                             drop_arrival_chunk)
+        check(self.L.rrCudaSetWaitLimits(self.ctx, C.byref(w)), "rrCudaSetWaitLimits")
 
     def device_errors(self) -> int:
         v = C.c_uint32()

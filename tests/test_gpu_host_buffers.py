@@ -44,8 +44,12 @@ def test_streamed_host_trace_equals_device_trace(ctx, n, chunk, q, o):
     if q == 1:
         rays[:, 7] = np.float32(0.05)
     bvh = ctx.build_geometry(to_dev(v), to_dev(i), quality=True)
-    want = hits_np(ctx.intersect(bvh, to_dev(rays), query=q, output=o))
-    got = ctx.intersect_host(bvh, torch.from_numpy(rays).pin_memory(), query=q, output=o, chunk_rays=chunk)
+    ctx.set_traversal(3)  # the persistent binary kernel's streamed variant (the 4-wide one: test below)
+    try:
+        want = hits_np(ctx.intersect(bvh, to_dev(rays), query=q, output=o))
+        got = ctx.intersect_host(bvh, torch.from_numpy(rays).pin_memory(), query=q, output=o, chunk_rays=chunk)
+    finally:
+        ctx.set_traversal(0)
     assert np.array_equal(got.numpy().view(np.uint32), want)
     assert ctx.device_errors() == 0
 

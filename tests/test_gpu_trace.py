@@ -161,14 +161,14 @@ def test_wait_event_timeout_is_bounded(ctx):
     hits = torch.empty((R, 4), dtype=torch.int32, device="cuda")
     scratch = torch.empty(ctx.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda")
     cs = ctx.command_stream()
-    for _ in range(8):
+    for _ in range(16):  # tens of milliseconds of queued work against a 0 ms limit
         ctx.cmd_intersect(res, rays_d, R, hits, scratch, cs)
     ev = ctx.submit(cs, wait=False)
     assert ctx.L.rrCudaSetWaitTimeout(ctx.ctx, 0) == rr.RR_SUCCESS
     first = ctx.L.rrWaitEvent(ctx.ctx, ev)
     assert ctx.L.rrCudaSetWaitTimeout(ctx.ctx, 600000) == rr.RR_SUCCESS
     assert ctx.L.rrWaitEvent(ctx.ctx, ev) == rr.RR_SUCCESS
-    assert first in (rr.RR_ERROR_INTERNAL, rr.RR_SUCCESS)
+    assert first == rr.RR_ERROR_INTERNAL
     ctx.L.rrReleaseEvent(ctx.ctx, ev)
     ctx.release_stream(cs)
 
