@@ -28,6 +28,10 @@ Reported (one JSON line on rank 0):
                every ray, and its own fp64 t / uv error
   fp64_t_error t / uv error of the chosen hits against an fp64 evaluation of
                the same ray-triangle pairs on the first 1,048,576 rays
+  precise      the opt-in precise triangle test (watertight decision, accurate
+               t and uv in fp32): Mrays/s of its autotuned kernel, its hit
+               differences from the plain kernel classified, and its own fp64
+               t / uv error
   cpu_baseline the oracle's C++ restatement of the reference traversal on the
                host cores, on a bounded sample of the same rays
 With --gpus N under torchrun every rank traces its own 16,777,216 rays against
@@ -80,6 +84,8 @@ def parse():
     ap.add_argument("--no-anyhit", action="store_true", help="skip the any-hit (occlusion) measurement")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the 8-wide 8-bit-bounds run (hit identity and fp64 error of that format)")
+    ap.add_argument("--no-precise", action="store_true",
+                    help="skip the precise triangle test run (watertight, accurate t; opt-in mode)")
     ap.add_argument("--e2e-chunk", type=int, default=0,
                     help="rays per copy-in chunk of the e2e run (0: the library's default, 2^17)")
     ap.add_argument("--quality", type=int, default=1,
@@ -231,16 +237,20 @@ def cpu_baseline(v, i, rays, seconds, threads=None):
             "sample": f"first {target:,} rays of the workload, closest hit, binary nodes built by the oracle"}, nodes
 
 
-def precision_report(v, i, rays, hits, nodes, n=1 << 20):
+def precision_report(v, i, rays, hits, nodes, n=1 << 20, precise=False):
     """t and uv error of the fp32 closest hits against the exact (fp64)
     intersection of the same ray with the same triangle, on the first n rays.
     `hits` are the chosen path's RRHit records (uint32 view); t32 is the
-    oracle's fp32 distance, which equals the kernels' (same arithmetic)."""
+    oracle's fp32 distance, which equals the kernels' (same arithmetic: the
+    reference's test, or with `precise` the precise triangle test)."""
     import oracle
     sub = rays[:n]
     h = hits[:n]
     hit = h[:, 2] != 0xFFFFFFFF
-    t32 = oracle.trace_t(nodes, sub, threads=os.cpu_count() or 1)
+    if precise:
+        t32 = oracle.trace_precise(nodes, sub, threads=os.cpu_count() or 1)[1]
+    else:
+        t32 = oracle.trace_t(nodes, sub, threads=os.cpu_count() or 1)
     idx = i.astype(np.int64)
     tri9 = np.zeros((n, 9), np.float32)
     tri9[hit] = v[idx[h[hit, 3]]].reshape(-1, 9)
@@ -253,6 +263,27 @@ def precision_report(v, i, rays, hits, nodes, n=1 << 20):
             "t_ulp_p999": float(np.percentile(ulp, 99.9)), "t_within_2ulp": float(np.mean(ulp <= 2.0)),
             "uv_abs_err_max": float(uv_err.max()), "uv_abs_err_mean": float(uv_err.mean()),
             "reference": "fp64 Moller-Trumbore + barycentrics of the same ray and triangle (oracle rro_fp64_hit)"}
+
+
+def precise_vs_plain(v, i, rays, hp, ph):
+    """Hit-ID differences of the precise triangle test from the plain kernel
+    (the reference's test) on every ray, classified: hit flags that differ
+    either way, and for rays where both hit different triangles the gap
+    between the two triangles' precise distances."""
+    import oracle
+    mp, mr = hp[:, 2] != 0xFFFFFFFF, ph[:, 2] != 0xFFFFFFFF
+    diff = np.where(mp & mr & (hp[:, 3] != ph[:, 3]))[0]
+    rep = {"rays": int(rays.shape[0]), "hit_only_with_precise": int(np.sum(mp & ~mr)),
+           "hit_only_with_reference_test": int(np.sum(mr & ~mp)), "different_triangle": int(diff.size)}
+    if diff.size and diff.size < 200000:
+        idx = i.astype(np.int64)
+        ta = oracle.tri_test_precise(rays[diff], v[idx[hp[diff, 3]]].reshape(-1, 9))[:, 0].astype(np.float64)
+        tb = oracle.tri_test_precise(rays[diff], v[idx[ph[diff, 3]]].reshape(-1, 9))[:, 0].astype(np.float64)
+        gap = np.abs(ta - tb) / np.spacing(np.abs(ta).astype(np.float32)).astype(np.float64)
+        gap[~np.isfinite(tb)] = np.inf  # the plain path's triangle is no hit for the precise test
+        rep.update({"equal_t": int(np.sum(gap == 0)), "within_2ulp": int(np.sum((gap > 0) & (gap <= 2))),
+                    "farther": int(np.sum(gap > 2)), "precise_t_never_larger": bool(np.all(ta <= tb))})
+    return rep
 
 
 def run_reference(args):
@@ -488,6 +519,26 @@ def run_ours(args):
         ctx.set_traversal(chosen_trav, args.block, chosen_per_sm, ray_order=chosen_order, short_stack=chosen_stack)
         assert ctx.device_errors() == 0, "device error word set during the any-hit run"
 
+    # ---- the precise triangle test (opt-in RR_CUDA_TRIANGLE_TEST_WATERTIGHT):
+    # the same rays and chosen tree, kernel autotuned for the mode; its
+    # hits against the plain kernel's, classified, and its fp64 error below.
+    precise = None
+    if not args.no_precise and "plain" in out and not args.only:
+        ctx.set_traversal(0, triangle_test=rr.RR_CUDA_TRIANGLE_TEST_WATERTIGHT)
+        tuned_p = ctx.autotune(bvh_c, rays_d, hits=hits_d, scratch=scratch_t)
+        cur["bvh"] = hcb
+        kp = max(3, args.steps // 3)
+        per_p, total_p = time_steps(trace_step, kp, args.warmup, ws, stream)
+        hp = hits_d.cpu().numpy().view(np.uint32).copy()
+        precise = {"triangle_test": "watertight decision (Woop et al. 2013, exact edge signs), t and uv from "
+                                    "exact differences and compensated products, robust box test (Ize 2013); fp32",
+                   "kernel": KERNELS.get(tuned_p["traversal"], "?"), "tree": "the chosen path's",
+                   "value": R * ws * kp / (total_p / 1e3) / 1e6, "unit": "Mrays/s",
+                   "p50_ms": statistics.median(per_p), "p99_ms": float(np.percentile(per_p, 99)),
+                   "vs_plain_hits": precise_vs_plain(v, i, rays, hp, out["plain"]["hits"]), "hits": hp}
+        ctx.set_traversal(chosen_trav, args.block, chosen_per_sm, ray_order=chosen_order, short_stack=chosen_stack)
+        assert ctx.device_errors() == 0, "device error word set during the precise run"
+
     # ---- end to end through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and not args.only:
@@ -586,6 +637,11 @@ def run_ours(args):
         line["fp64_t_error"] = precision_report(v, i, rays, c["hits"], nodes)
     if anyhit:
         line["any_hit"] = anyhit
+    if precise:
+        hp = precise.pop("hits")
+        if not args.no_cpu:
+            precise["fp64_t_error"] = precision_report(v, i, rays, hp, nodes, precise=True)
+        line["precise"] = precise
     if wide8:
         h8 = wide8.pop("hits")
         if not args.no_cpu:

@@ -66,6 +66,26 @@ typedef enum
     RR_CUDA_TRAVERSAL_BVH4 = 4
 } RRCudaTraversal;
 
+/* Ray-triangle test of the traversal kernels. */
+typedef enum
+{
+    /* The reference's test (vlk/kernels/common.h:103-137, Moller-Trumbore,
+     * with the reference's slab test and barycentrics): hits bit-identical to
+     * the reference's traversal.  The default. */
+    RR_CUDA_TRIANGLE_TEST_REFERENCE = 0,
+    /* Watertight and accurate, in fp32 (no counterpart in the reference): the
+     * watertight hit decision of Woop, Benthin and Wald (JCGT 2013) with the
+     * edge functions' signs computed exactly, t and the barycentrics from
+     * exact differences and compensated ("double-float") products (t within
+     * about 1 ulp of the exact intersection of the fp32 ray and triangle),
+     * and a conservative box test (Ize, JCGT 2013) that never culls a box the
+     * ray touches.  Supported by RR_CUDA_TRAVERSAL_AUTO,
+     * RR_CUDA_TRAVERSAL_BINARY_PERSISTENT and RR_CUDA_TRAVERSAL_BVH4 on
+     * triangle geometries (not on scene buffers, AABB lists or the
+     * multi-request launch). */
+    RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 1
+} RRCudaTriangleTest;
+
 typedef struct
 {
     uint32_t struct_size;     /* sizeof(RRCudaTraversalOptions) */
@@ -77,7 +97,7 @@ typedef struct
                                  direction octant and origin first (batches of 2^20 rays or more) */
     uint32_t short_stack;     /* RR_CUDA_TRAVERSAL_BVH4 single-level kernel: shared-memory stack entries
                                  per ray, 0 = default (16), else 12..32 (deeper entries spill to scratch) */
-    uint32_t reserved[1];
+    uint32_t triangle_test;   /* RRCudaTriangleTest, 0 = the reference's */
 } RRCudaTraversalOptions;
 
 /* Fetch counters accumulated while collect_stats is 1. */

@@ -50,7 +50,8 @@ def lib() -> C.CDLL:
         _lib = C.CDLL(str(LIB))
         for name in ("rro_mesh_aabb", "rro_morton", "rro_sort32", "rro_sort64", "rro_emit", "rro_fit",
                      "rro_build_mesh", "rro_trace", "rro_build_scene", "rro_trace_scene", "rro_fp64_hit",
-                     "rro_trace_t", "rro_tri_test", "rro_trace_leaves"):
+                     "rro_trace_t", "rro_tri_test", "rro_trace_leaves", "rro_trace_precise",
+                     "rro_tri_test_precise"):
             getattr(_lib, name).restype = None
     return _lib
 
@@ -147,6 +148,27 @@ def trace(nodes, rays, query=0, output=0, threads=8, hits=None, fetches=False, b
     lib().rro_trace_leaves(_p(nodes), C.c_uint32(nodes.size), _p(r), C.c_uint32(R), C.c_int(query),
                            C.c_int(output), _p(hits), _p(f), C.c_int(threads), C.c_int(1 if box_leaves else 0))
     return (hits, f) if fetches else hits
+
+
+def trace_precise(nodes, rays, query=0, output=0, threads=8):
+    """The precise triangle test's traversal (watertight decision, accurate t
+    and uv, robust box test) in the reference's visit order: the twin of the
+    kernels' RR_CUDA_TRIANGLE_TEST_WATERTIGHT mode.  Returns (hits, t) with t
+    the fp32 distance of each closest (any: first) hit, +inf on a miss."""
+    R = rays.shape[0]
+    hits = np.full((R, 4) if output == 0 else (R,), INVALID, dtype=np.uint32)
+    t = np.full(R, np.inf, dtype=np.float32)
+    lib().rro_trace_precise(_p(nodes), C.c_uint32(nodes.size), _p(np.ascontiguousarray(rays, np.float32)),
+                            C.c_uint32(R), C.c_int(query), C.c_int(output), _p(hits), _p(t), C.c_int(threads))
+    return hits, t
+
+
+def tri_test_precise(rays, tri9):
+    R = rays.shape[0]
+    out = np.zeros((R, 3), dtype=np.float32)
+    lib().rro_tri_test_precise(_p(np.ascontiguousarray(rays, np.float32)), _p(np.ascontiguousarray(tri9, np.float32)),
+                               C.c_uint32(R), _p(out))
+    return out
 
 
 def aabb_vertices(boxes):

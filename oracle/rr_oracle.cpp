@@ -426,11 +426,169 @@ static inline float isect_leaf_box(const RayF& r, F3 inv, F3 oxi, const float* l
     return t0 <= t1 ? t0 : t_max;
 }
 
+// ---- the precise triangle test (this build's opt-in mode, no reference
+// counterpart): the FP32 twin of csrc/trace_precise.cuh, operation for
+// operation, so that the kernels' hits can be checked bit for bit.
+//   decision: Woop, Benthin, Wald, "Watertight Ray/Triangle Intersection",
+//     JCGT 2013 (shear to the ray, 2-D edge functions with exact signs);
+//   t, u, v: exact input differences and compensated products (error-free
+//     transformations: TwoSum, TwoProduct with fma), quotient corrected by
+//     its exact remainder;
+//   box test: Ize, "Robust BVH Ray Traversal", JCGT 2013 ((p - o) * (1 / d),
+//     far distance moved outward by 2 gamma_3).
+namespace precise
+{
+const float kRobustFar = 1.00000036f;
+struct DF
+{
+    float h, l;
+};
+static inline DF two_sum(float a, float b)
+{
+    const float s = a + b, bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+static inline DF two_diff(float a, float b)
+{
+    const float s = a - b, bb = s - a;
+    return DF{s, (a - (s - bb)) - (b + bb)};
+}
+static inline DF fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+static inline DF two_prod(float a, float b)
+{
+    const float p = a * b;
+    return DF{p, fmaf(a, b, -p)};
+}
+static inline float exact_sign_dop(float a, float b, float c, float d)
+{
+    const float p1 = a * b, p2 = c * d, r = p1 - p2;
+    if (r != 0.0f) return r;
+    return fmaf(a, b, -p1) - fmaf(c, d, -p2);
+}
+static inline DF df_dop(DF a, DF b, DF c, DF d)
+{
+    const DF    p = two_prod(a.h, b.h), q = two_prod(c.h, d.h), s = two_diff(p.h, q.h);
+    const float lo = s.l + (p.l - q.l) + ((a.h * b.l + a.l * b.h) - (c.h * d.l + c.l * d.h));
+    return fast_two_sum(s.h, lo);
+}
+static inline DF df_dot3(DF ax, DF ay, DF az, DF bx, DF by, DF bz)
+{
+    const DF    px = two_prod(ax.h, bx.h), py = two_prod(ay.h, by.h), pz = two_prod(az.h, bz.h);
+    const DF    s1 = two_sum(px.h, py.h), s2 = two_sum(s1.h, pz.h);
+    const float lx = px.l + (ax.h * bx.l + ax.l * bx.h);
+    const float ly = py.l + (ay.h * by.l + ay.l * by.h);
+    const float lz = pz.l + (az.h * bz.l + az.l * bz.h);
+    return fast_two_sum(s2.h, ((s1.l + s2.l) + lx) + (ly + lz));
+}
+static inline DF df_div(DF n, DF d)
+{
+    const float q = n.h / d.h;
+    const float r = fmaf(-q, d.h, n.h) + (n.l - q * d.l);
+    return fast_two_sum(q, r / d.h);
+}
+struct Tri
+{
+    DF w[3], e1[3], e2[3], n[3];
+};
+static inline Tri setup(const RayF& r, F3 v0, F3 v1, F3 v2)
+{
+    Tri         p;
+    const float o[3] = {r.o.x, r.o.y, r.o.z}, a[3] = {v0.x, v0.y, v0.z}, b[3] = {v1.x, v1.y, v1.z},
+                c[3] = {v2.x, v2.y, v2.z};
+    for (int k = 0; k < 3; ++k)
+    {
+        p.w[k]  = two_diff(a[k], o[k]);
+        p.e1[k] = two_diff(b[k], a[k]);
+        p.e2[k] = two_diff(c[k], a[k]);
+    }
+    p.n[0] = df_dop(p.e1[1], p.e2[2], p.e1[2], p.e2[1]);
+    p.n[1] = df_dop(p.e1[2], p.e2[0], p.e1[0], p.e2[2]);
+    p.n[2] = df_dop(p.e1[0], p.e2[1], p.e1[1], p.e2[0]);
+    return p;
+}
+static inline DF t_of(const Tri& p, const RayF& r, bool& ok)
+{
+    const DF N = df_dot3(p.n[0], p.n[1], p.n[2], p.w[0], p.w[1], p.w[2]);
+    const DF D = df_dot3(p.n[0], p.n[1], p.n[2], DF{r.d.x, 0.f}, DF{r.d.y, 0.f}, DF{r.d.z, 0.f});
+    ok         = D.h != 0.0f;
+    return ok ? df_div(N, D) : DF{0.f, 0.f};
+}
+// Watertight decision, then the accurate t; t_max on a miss.
+static inline float isect_tri(const RayF& r, F3 v0, F3 v1, F3 v2, float t_max)
+{
+    const float adx = fabsf(r.d.x), ady = fabsf(r.d.y), adz = fabsf(r.d.z);
+    const int   kz  = (adx >= ady && adx >= adz) ? 0 : (ady >= adz ? 1 : 2);
+    int         kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+    const float d[3] = {r.d.x, r.d.y, r.d.z};
+    if (d[kz] < 0.0f) std::swap(kx, ky);
+    const float sx = d[kx] / d[kz], sy = d[ky] / d[kz];
+    const float o[3] = {r.o.x, r.o.y, r.o.z};
+    const float a[3] = {v0.x - o[0], v0.y - o[1], v0.z - o[2]};
+    const float b[3] = {v1.x - o[0], v1.y - o[1], v1.z - o[2]};
+    const float c[3] = {v2.x - o[0], v2.y - o[1], v2.z - o[2]};
+    const float ax = a[kx] - sx * a[kz], ay = a[ky] - sy * a[kz];
+    const float bx = b[kx] - sx * b[kz], by = b[ky] - sy * b[kz];
+    const float cx = c[kx] - sx * c[kz], cy = c[ky] - sy * c[kz];
+    const float U = exact_sign_dop(cx, by, cy, bx), V = exact_sign_dop(ax, cy, ay, cx), W = exact_sign_dop(bx, ay, by, ax);
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return t_max;
+    if (U + V + W == 0.0f) return t_max;
+    bool      ok;
+    const Tri p = setup(r, v0, v1, v2);
+    const DF  t = t_of(p, r, ok);
+    if (!ok || !(t.h >= r.tmin) || t.h > t_max) return t_max;
+    return t.h;
+}
+static inline void barycentrics(const RayF& r, F3 v0, F3 v1, F3 v2, float& u_out, float& v_out)
+{
+    u_out = v_out = 0.f;
+    bool      ok;
+    const Tri p = setup(r, v0, v1, v2);
+    const DF  t = t_of(p, r, ok);
+    if (!ok) return;
+    const float dd[3] = {r.d.x, r.d.y, r.d.z};
+    DF          q[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        const DF    pr = two_prod(t.h, dd[k]);
+        const DF    s  = two_diff(pr.h, p.w[k].h);
+        q[k]           = fast_two_sum(s.h, s.l + ((pr.l + t.l * dd[k]) - p.w[k].l));
+    }
+    const float an[3] = {fabsf(p.n[0].h), fabsf(p.n[1].h), fabsf(p.n[2].h)};
+    int         ia, ib, in;
+    if (an[2] >= an[0] && an[2] >= an[1])
+        ia = 0, ib = 1, in = 2;
+    else if (an[0] >= an[1])
+        ia = 1, ib = 2, in = 0;
+    else
+        ia = 2, ib = 0, in = 1;
+    const DF det = p.n[in];
+    if (det.h == 0.0f) return;
+    u_out = df_div(df_dop(q[ia], p.e2[ib], q[ib], p.e2[ia]), det).h;
+    v_out = df_div(df_dop(p.e1[ia], q[ib], p.e1[ib], q[ia]), det).h;
+}
+static inline float robust_far(float t1) { return t1 * (t1 >= 0.0f ? kRobustFar : 2.0f - kRobustFar); }
+static inline void isect_box(const float* lo, const float* hi, F3 inv, F3 o, float tmax_, float tmin_, float& t0,
+                             float& t1)
+{
+    const float fx = (hi[0] - o.x) * inv.x, fy = (hi[1] - o.y) * inv.y, fz = (hi[2] - o.z) * inv.z;
+    const float nx = (lo[0] - o.x) * inv.x, ny = (lo[1] - o.y) * inv.y, nz = (lo[2] - o.z) * inv.z;
+    t1 = robust_far(fminf(fminf(fmaxf(fz, nz), fminf(fmaxf(fx, nx), fmaxf(fy, ny))), tmax_));
+    t0 = fmaxf(fmaxf(fminf(fz, nz), fmaxf(fminf(fx, nx), fminf(fy, ny))), tmin_);
+}
+}  // namespace precise
+
+// precise: the precise triangle test's traversal (same visit order, robust
+// box test, precise triangle test and barycentrics); out_t (optional)
+// receives the fp32 distance of the closest hit (+inf on a miss).
 static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int full, void* hits, uint64_t gi,
-                      uint64_t* fetches, int box_leaves = 0)
+                      uint64_t* fetches, int box_leaves = 0, int precise_test = 0, float* out_t = nullptr)
 {
     RayF     r      = load_ray(rr);
-    F3       inv    = safe_invdir(r.d);
+    F3       inv    = precise_test ? f3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z) : safe_invdir(r.d);
     F3       oxi    = f3(-r.o.x * inv.x, -r.o.y * inv.y, -r.o.z * inv.z);
     float    ct     = r.tmax;
     uint32_t caddr  = kInvalid;
@@ -446,8 +604,16 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
         if (nd.child0 != kInvalid)
         {
             float a0, a1, b0, b1;
-            isect_box(nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, inv, oxi, ct, r.tmin, a0, a1);
-            isect_box(nd.aabb1_min_or_v2, nd.aabb1_max_or_v3, inv, oxi, ct, r.tmin, b0, b1);
+            if (precise_test)
+            {
+                precise::isect_box(nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, inv, r.o, ct, r.tmin, a0, a1);
+                precise::isect_box(nd.aabb1_min_or_v2, nd.aabb1_max_or_v3, inv, r.o, ct, r.tmin, b0, b1);
+            }
+            else
+            {
+                isect_box(nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, inv, oxi, ct, r.tmin, a0, a1);
+                isect_box(nd.aabb1_min_or_v2, nd.aabb1_max_or_v3, inv, oxi, ct, r.tmin, b0, b1);
+            }
             bool tc0 = a0 <= a1, tc1 = b0 <= b1;
             bool c1f = tc1 && (a0 > b0);
             if (tc0 || tc1)
@@ -469,9 +635,11 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
         }
         else
         {
-            float t = box_leaves ? isect_leaf_box(r, inv, oxi, nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, ct)
-                                 : isect_tri(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
-                                             ld3(nd.aabb1_min_or_v2), ct);
+            float t = box_leaves     ? isect_leaf_box(r, inv, oxi, nd.aabb0_min_or_v0, nd.aabb0_max_or_v1, ct)
+                      : precise_test ? precise::isect_tri(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                                                          ld3(nd.aabb1_min_or_v2), ct)
+                                     : isect_tri(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                                                 ld3(nd.aabb1_min_or_v2), ct);
             if (t < ct)
             {
                 if (!any)
@@ -486,6 +654,9 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
                         rro_hit& h = ((rro_hit*)hits)[gi];
                         if (box_leaves)
                             h.uv[0] = h.uv[1] = 0.f;
+                        else if (precise_test)
+                            precise::barycentrics(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
+                                                  ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
                         else
                             barycentrics(hit_point(r, t), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
                                          ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
@@ -495,12 +666,14 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
                     else
                         ((uint32_t*)hits)[gi] = nd.child1;
                     if (fetches) fetches[gi] = nfetch;
+                    if (out_t) out_t[gi] = t;
                     return;
                 }
             }
         }
         addr = stack[--sp];
     }
+    if (out_t) out_t[gi] = caddr != kInvalid ? ct : INFINITY;
     if (caddr != kInvalid)
     {
         const rro_node& nd = nodes[caddr];
@@ -509,6 +682,9 @@ static void trace_one(const rro_node* nodes, const rro_ray& rr, int any, int ful
             rro_hit& h = ((rro_hit*)hits)[gi];
             if (box_leaves)
                 h.uv[0] = h.uv[1] = 0.f;
+            else if (precise_test)
+                precise::barycentrics(r, ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1), ld3(nd.aabb1_min_or_v2),
+                                      h.uv[0], h.uv[1]);
             else
                 barycentrics(hit_point(r, ct), ld3(nd.aabb0_min_or_v0), ld3(nd.aabb0_max_or_v1),
                              ld3(nd.aabb1_min_or_v2), h.uv[0], h.uv[1]);
@@ -1251,6 +1427,34 @@ void rro_trace_t(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, u
         }
         if (hit) out_t[gi] = ct;
     });
+}
+
+// The precise triangle test's traversal (csrc/trace_precise.cuh twin): hits
+// as rro_trace, and (optional) the fp32 distance of each closest / first hit.
+void rro_trace_precise(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, int query,
+                       int output, void* hits, float* out_t, int threads)
+{
+    parallel_for(nrays, threads, [&](uint64_t gi) {
+        if (out_t) out_t[gi] = INFINITY;
+        if (n_nodes == 0) return;
+        trace_one(nodes, rays[gi], query == 1, output == 0, hits, gi, nullptr, 0, 1, out_t);
+    });
+}
+
+// The precise test of ray i against triangle tri9[i]: t (or +inf) and uv.
+void rro_tri_test_precise(const rro_ray* rays, const float* tri9, uint32_t nrays, float* out_tuv)
+{
+    for (uint32_t i = 0; i < nrays; ++i)
+    {
+        RayF         r = load_ray(rays[i]);
+        const float* v = tri9 + 9ull * i;
+        const float  t = precise::isect_tri(r, ld3(v), ld3(v + 3), ld3(v + 6), r.tmax);
+        float        u = 0.f, w = 0.f;
+        if (t < r.tmax) precise::barycentrics(r, ld3(v), ld3(v + 3), ld3(v + 6), u, w);
+        out_tuv[3ull * i + 0] = t < r.tmax ? t : INFINITY;
+        out_tuv[3ull * i + 1] = u;
+        out_tuv[3ull * i + 2] = w;
+    }
 }
 
 // Per-triangle FP32 test (isect_tri + barycentrics) of ray i against the

@@ -63,6 +63,11 @@ void rro_fp64_hit(const rro_ray* rays, const float* tri9, const uint32_t* valid,
 void rro_trace_t(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, float* out_t,
                  int threads);
 void rro_tri_test(const rro_ray* rays, const float* tri9, uint32_t nrays, float* out_tuv);
+/* The precise triangle test (watertight decision, accurate t and uv, robust
+ * box test): traversal in the reference's visit order, and the test alone. */
+void rro_trace_precise(const rro_node* nodes, uint32_t n_nodes, const rro_ray* rays, uint32_t nrays, int query,
+                       int output, void* hits, float* out_t, int threads);
+void rro_tri_test_precise(const rro_ray* rays, const float* tri9, uint32_t nrays, float* out_tuv);
 
 #ifdef __cplusplus
 }

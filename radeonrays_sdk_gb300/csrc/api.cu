@@ -648,6 +648,16 @@ struct StreamPlan
     size_t    scratch_bytes = 0;  // scratch left to the kernel
 };
 
+// The precise triangle test runs on triangle geometries only (the two-level,
+// AABB-list and multi-request kernels keep the reference's test).
+bool precise_unsupported(Context* ctx, const uint8_t* bvh)
+{
+    if (ctx->topts.triangle_test != RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return false;
+    auto it = ctx->registry.find((uintptr_t)bvh);
+    if (it == ctx->registry.end()) return false;  // traversed as binary triangle nodes
+    return it->second.kind != kKindGeom || it->second.prim_kind != kPrimTriangles;
+}
+
 // The launch of one rrCmdIntersect: arguments from the buffers and the
 // traversal options, kernel chosen by the buffer kind and options.  With a
 // stream plan, returns an empty Op unless the persistent binary or the
@@ -674,6 +684,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     a.ray_order     = (int)o.ray_order;
     a.sm_count      = ctx->sm_count;
     a.stream_polls  = ctx->arrival_polls;
+    a.triangle_test = (int)o.triangle_test;
     auto    it      = ctx->registry.find((uintptr_t)bvh);
     BufInfo bi;
     if (it != ctx->registry.end()) bi = it->second;
@@ -1179,6 +1190,7 @@ RR_API RRError rrCmdIntersect(RRContext              context,
     RR_TRY({
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
+        if (precise_unsupported(ctx, P(scene_buffer)->addr())) return RR_ERROR_NOT_IMPLEMENTED;
         const uint32_t* ind =
             indirect_ray_count ? reinterpret_cast<const uint32_t*>(P(indirect_ray_count)->addr()) : nullptr;
         record(S(command_stream), trace_op(ctx, P(scene_buffer)->addr(), P(rays)->addr(), ray_count, ind,
@@ -1210,6 +1222,7 @@ RR_API RRError rrCudaCmdIntersectHostBuffers(RRContext              context,
     RR_TRY({
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
+        if (precise_unsupported(ctx, P(scene_buffer)->addr())) return RR_ERROR_NOT_IMPLEMENTED;
         ctx->ensure_pipe();
         // Chunks go round-robin to the side streams; each stream owns an equal
         // share of the scratch (rrGetTraceMemoryRequirements(ray_count) bytes).
@@ -1689,6 +1702,11 @@ RR_API RRError rrCudaSetTraversalOptions(RRContext context, const RRCudaTraversa
         return RR_ERROR_INVALID_PARAMETER;
     if (options->block_size && (options->block_size % 32 || options->block_size > 1024)) return RR_ERROR_INVALID_PARAMETER;
     if (options->short_stack && (options->short_stack < 12 || options->short_stack > 32)) return RR_ERROR_INVALID_PARAMETER;
+    if (options->triangle_test > RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return RR_ERROR_INVALID_PARAMETER;
+    // The precise test runs in the persistent kernels (binary and 4-wide).
+    if (options->triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT && options->traversal != RR_CUDA_TRAVERSAL_AUTO &&
+        options->traversal != RR_CUDA_TRAVERSAL_BINARY_PERSISTENT && options->traversal != RR_CUDA_TRAVERSAL_BVH4)
+        return RR_ERROR_INVALID_PARAMETER;
     C(context)->topts = *options;
     return RR_SUCCESS;
 }
@@ -1786,9 +1804,12 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
         // output, ray-count octave (the format decides the candidates).
         uint32_t octave = 0;
         while ((1ull << (octave + 1)) <= ray_count) ++octave;
+        const uint32_t tt = ctx->topts.triangle_test;
+        if (precise_unsupported(ctx, bvh)) return RR_ERROR_NOT_IMPLEMENTED;
         const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.format) +
                                 "|" + std::to_string(bi.n) + "|" + std::to_string((int)query) + "|" +
-                                std::to_string((int)query_output) + "|" + std::to_string(octave);
+                                std::to_string((int)query_output) + "|" + std::to_string(octave) +
+                                (tt ? "|t" + std::to_string(tt) : std::string());
         auto hit = ctx->tuned.find(key);
         const char* cache_path = std::getenv("RR_CUDA_TUNE_CACHE");
         if (hit == ctx->tuned.end() && cache_path)
@@ -1810,6 +1831,7 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
                         o.ray_order     = ro;
                         o.blocks_per_sm = bps;
                         o.short_stack   = depth;
+                        o.triangle_test = tt;
                         ctx->tuned[key] = o;
                     }
                 }
@@ -1820,11 +1842,14 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
         if (hit == ctx->tuned.end())
         {
             std::vector<RRCudaTraversalOptions> cand;
+            // The precise test runs in the persistent kernels only.
             auto add = [&](uint32_t trav, uint32_t order) {
+                if (tt && trav != RR_CUDA_TRAVERSAL_BINARY_PERSISTENT && trav != RR_CUDA_TRAVERSAL_BVH4) return;
                 RRCudaTraversalOptions o{};
-                o.struct_size = sizeof(o);
-                o.traversal   = trav;
-                o.ray_order   = order;
+                o.struct_size   = sizeof(o);
+                o.traversal     = trav;
+                o.ray_order     = order;
+                o.triangle_test = tt;
                 cand.push_back(o);
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);

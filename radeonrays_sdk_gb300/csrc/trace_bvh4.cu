@@ -38,11 +38,14 @@ struct B4Ray
     int      sp;     // entries in the short stack
 };
 
+// kPrecise: `inv` is the exact reciprocal and `oxi` the origin (the robust
+// box test of trace_precise.cuh).
+template <bool kPrecise>
 __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
 {
     s.ray  = r;
-    s.inv  = safe_invdir(r.d);
-    s.oxi  = f3(-r.o.x * s.inv.x, -r.o.y * s.inv.y, -r.o.z * s.inv.z);
+    s.inv  = kPrecise ? exact_invdir(r.d) : safe_invdir(r.d);
+    s.oxi  = kPrecise ? r.o : f3(-r.o.x * s.inv.x, -r.o.y * s.inv.y, -r.o.z * s.inv.z);
     s.ct   = r.tmax;
     s.best = kInvalid;
     s.ref  = 0;  // the root 4-wide node
@@ -52,7 +55,7 @@ __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
 
 // One step; returns true when the ray is finished (stack empty, or a hit
 // accepted by an any-hit query).  nf / tf count node and leaf fetches.
-template <bool kAny>
+template <bool kAny, bool kPrecise>
 __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ wn, const BvhNode* __restrict__ nodes,
                                         uint32_t wlim, uint32_t first_leaf, uint32_t node_limit, const PStack& st,
                                         DeviceWords* words, uint32_t& nf, uint32_t& tf)
@@ -72,7 +75,8 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
         const float4* p = reinterpret_cast<const float4*>(nodes + idx);
         const float4  a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
         ++tf;
-        const float t = isect_tri(s.ray, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), s.ct);
+        const F3    v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
+        const float t  = kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct) : isect_tri(s.ray, v0, v1, v2, s.ct);
         if (t < s.ct)
         {
             s.ct   = t;
@@ -82,7 +86,7 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        const B4Hits h = b4_children(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
+        const B4Hits h = b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
         if (h.n)
         {
@@ -99,7 +103,7 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
 // kernel's streamed variant.
 // The short stack is dynamic shared memory of kPBlock x depth entries; the
 // depth (12..32, default kPShort) is a launch parameter the autotuner picks.
-template <bool kAny, bool kFull, bool kStats, bool kStream>
+template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t gcap, int depth)
 {
     extern __shared__ uint32_t s_stack[];
@@ -172,7 +176,12 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
                     if (s.best != kInvalid)
                     {
                         const NodeView nd = load_binary_node(nodes, s.best);
-                        write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                        if (kPrecise)
+                            write_hit_precise<kFull>(a.hits, gid, s.ray, nd.l0, nd.h0, nd.l1, 0u, nd.child1,
+                                                     nd.child1);
+                        else
+                            write_hit<kFull>(a.hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1,
+                                             nd.child1);
                     }
                     else
                         write_miss<kFull>(a.hits, gid);
@@ -199,7 +208,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
                         {
                             active = true;
                             nf = tf = 0;
-                            b4_start(s, load_ray_cg(a.rays, gid));
+                            b4_start<kPrecise>(s, load_ray_cg(a.rays, gid));
                         }
                         else
                         {
@@ -213,7 +222,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
                     {
                         active = true;
                         nf = tf = 0;
-                        b4_start(s, load_ray(a.rays, gid));
+                        b4_start<kPrecise>(s, load_ray(a.rays, gid));
                     }
                 }
             }
@@ -221,7 +230,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        if (active && b4_step<kAny>(s, wn, nodes, a.wide_limit, first_leaf, a.node_limit, st, a.words, nf, tf))
+        if (active &&
+            b4_step<kAny, kPrecise>(s, wn, nodes, a.wide_limit, first_leaf, a.node_limit, st, a.words, nf, tf))
         {
             active  = false;
             pending = true;
@@ -234,10 +244,10 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
     }
 }
 
-template <bool kAny, bool kFull, bool kStats, bool kStream>
-cudaError_t go(const TraceArgs& a, cudaStream_t s)
+template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise>
+cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 {
-    auto         kern   = k_trace_bvh4<kAny, kFull, kStats, kStream>;
+    auto         kern   = k_trace_bvh4<kAny, kFull, kStats, kStream, kPrecise>;
     const int    depth  = a.short_stack > 0 ? a.short_stack : kPShort;
     const size_t smem   = (size_t)kPBlock * depth * sizeof(uint32_t);
     int          per_sm = a.blocks_per_sm;
@@ -251,6 +261,13 @@ cudaError_t go(const TraceArgs& a, cudaStream_t s)
     if (e != cudaSuccess) return e;
     kern<<<g.blocks, kPBlock, smem, s>>>(a, g.gcap, depth);
     return cudaGetLastError();
+}
+
+template <bool kAny, bool kFull, bool kStats, bool kStream>
+cudaError_t go(const TraceArgs& a, cudaStream_t s)
+{
+    if (a.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return go2<kAny, kFull, kStats, kStream, true>(a, s);
+    return go2<kAny, kFull, kStats, kStream, false>(a, s);
 }
 }  // namespace
 

@@ -4,6 +4,7 @@
 // that spills and refills in full blocks.
 #pragma once
 #include "trace_persistent.cuh"
+#include "trace_precise.cuh"
 
 namespace rr
 {
@@ -85,6 +86,10 @@ struct B4Hits
 // fma(hi, inv, oxi) >= fma(lo, inv, oxi), so the reference's min / max of
 // the two are exactly these.  The boxes are stored lo[3][4] then hi[3][4],
 // so the choice is a load offset.
+// kRobust (the precise triangle test's traversal, trace_precise.cuh): `inv`
+// is the exact reciprocal, `oxi` the ray origin, the distances are
+// (p - o) * inv and the far one is moved outward by 2 gamma_3.
+template <bool kRobust = false>
 __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 oxi, float tmin, float ct)
 {
     const float4* p  = reinterpret_cast<const float4*>(node);
@@ -93,8 +98,17 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
     const float4  fx = __ldg(p + 3 - ox), fy = __ldg(p + 4 - oy), fz = __ldg(p + 5 - oz);
     const uint4   cr = __ldg(reinterpret_cast<const uint4*>(p + 6));
     auto          key = [&](float ax, float ay, float az, float bx, float by, float bz, uint32_t r) {
-        const float t0 = fmaxf(b4_max3(fmaf(ax, inv.x, oxi.x), fmaf(ay, inv.y, oxi.y), fmaf(az, inv.z, oxi.z)), tmin);
-        const float t1 = fminf(b4_min3(fmaf(bx, inv.x, oxi.x), fmaf(by, inv.y, oxi.y), fmaf(bz, inv.z, oxi.z)), ct);
+        float t0, t1;
+        if (kRobust)
+        {
+            t0 = fmaxf(b4_max3((ax - oxi.x) * inv.x, (ay - oxi.y) * inv.y, (az - oxi.z) * inv.z), tmin);
+            t1 = robust_far(fminf(b4_min3((bx - oxi.x) * inv.x, (by - oxi.y) * inv.y, (bz - oxi.z) * inv.z), ct));
+        }
+        else
+        {
+            t0 = fmaxf(b4_max3(fmaf(ax, inv.x, oxi.x), fmaf(ay, inv.y, oxi.y), fmaf(az, inv.z, oxi.z)), tmin);
+            t1 = fminf(b4_min3(fmaf(bx, inv.x, oxi.x), fmaf(by, inv.y, oxi.y), fmaf(bz, inv.z, oxi.z)), ct);
+        }
         return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
     };
     float  k0 = key(nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, cr.x);

@@ -44,6 +44,7 @@ RR_LOG_LEVEL_DEBUG, RR_LOG_LEVEL_INFO, RR_LOG_LEVEL_WARN, RR_LOG_LEVEL_ERROR, RR
 RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8, RR_CUDA_NODE_FORMAT_BVH4 = 0, 1, 2
 RR_CUDA_TRAVERSAL_AUTO, RR_CUDA_TRAVERSAL_BINARY, RR_CUDA_TRAVERSAL_WIDE = 0, 1, 2
 RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, RR_CUDA_TRAVERSAL_BVH4 = 3, 4
+RR_CUDA_TRIANGLE_TEST_REFERENCE, RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 0, 1
 RR_CUDA_DEVICE_ERROR_STACK_OVERFLOW = 1
 RR_CUDA_DEVICE_ERROR_BAD_BUFFER = 2
 RR_CUDA_DEVICE_ERROR_COLLAPSE_DEPTH = 4
@@ -115,7 +116,7 @@ class RRSceneBuildInput(C.Structure):
 class RRCudaTraversalOptions(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("traversal", C.c_uint32), ("block_size", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("collect_stats", C.c_uint32), ("ray_order", C.c_uint32),
-                ("short_stack", C.c_uint32), ("reserved", C.c_uint32 * 1)]
+                ("short_stack", C.c_uint32), ("triangle_test", C.c_uint32)]
 
 
 class RRCudaWaitLimits(C.Structure):
@@ -550,9 +551,9 @@ class Context:
 
     # -- options and diagnostics
     def set_traversal(self, traversal=RR_CUDA_TRAVERSAL_AUTO, block_size=0, blocks_per_sm=0, collect_stats=0,
-                      ray_order=0, short_stack=0):
+                      ray_order=0, short_stack=0, triangle_test=RR_CUDA_TRIANGLE_TEST_REFERENCE):
         o = RRCudaTraversalOptions(C.sizeof(RRCudaTraversalOptions), traversal, block_size, blocks_per_sm,
-                                   collect_stats, ray_order, short_stack)
+                                   collect_stats, ray_order, short_stack, triangle_test)
         check(self.L.rrCudaSetTraversalOptions(self.ctx, C.byref(o)), "rrCudaSetTraversalOptions")
 
     def autotune(self, bvh, rays, query=RR_INTERSECT_QUERY_CLOSEST, output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT,

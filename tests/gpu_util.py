@@ -42,15 +42,17 @@ def trace(ctx, bvh, rays, query=0, output=0, traversal=0):
     return hits_np(h)
 
 
-def tie_only_mismatch(orc, rays, a, b, vertices, indices):
+def tie_only_mismatch(orc, rays, a, b, vertices, indices, precise=False):
     """Rays where closest-hit primitives a and b differ must be exact equal-t
-    ties: both triangles hit at the same fp32 distance."""
+    ties: both triangles hit at the same fp32 distance (by the reference's
+    triangle test, or the precise one)."""
     diff = np.where(a[:, 3] != b[:, 3])[0]
     if diff.size == 0:
         return 0
     assert np.all(a[diff, 2] != INVALID) and np.all(b[diff, 2] != INVALID)
     idx = indices.astype(np.int64).reshape(-1, 3)
-    ta = orc.tri_test(rays[diff], vertices[idx[a[diff, 3]]].reshape(-1, 9))[:, 0]
-    tb = orc.tri_test(rays[diff], vertices[idx[b[diff, 3]]].reshape(-1, 9))[:, 0]
+    test = orc.tri_test_precise if precise else orc.tri_test
+    ta = test(rays[diff], vertices[idx[a[diff, 3]]].reshape(-1, 9))[:, 0]
+    tb = test(rays[diff], vertices[idx[b[diff, 3]]].reshape(-1, 9))[:, 0]
     assert np.array_equal(ta, tb), (diff[:8], ta[:8], tb[:8])
     return diff.size

@@ -1,0 +1,158 @@
+"""Parity at the full sizes of the benchmark configurations, against the
+oracle (the CPU restatement of isect.comp:88-246 and isect_2l.comp:136-323).
+
+  * heightfield, 1449 x 1449 vertices (4,193,408 triangles), 16,777,216
+    incoherent rays: the build bit-identical to the oracle's; the plain and
+    persistent kernels bit-identical to the oracle for closest hit and for
+    any hit (occlusion rays, tmax ~ U[0.01, 0.5]); the 4-wide kernel (fast
+    and quality trees) with identical hit flags and primitive ids that differ
+    only at exact equal-t ties;
+  * the same heightfield with 8-wide 8-bit-bounded nodes: identical hit flags
+    and only equal-t ties against the plain path, on every ray;
+  * 2,048 BLASes (68.6 M triangles) built in one fused build and a TLAS of
+    2,048 instances: sampled BLASes bit-identical to the oracle's builds, the
+    TLAS nodes and transforms bit-identical, and the plain and persistent
+    two-level kernels bit-identical to the oracle on 1,048,576 rays.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gpu_util import INVALID, hits_np, tie_only_mismatch, to_dev, trailer_of
+
+pytestmark = pytest.mark.gpu
+THREADS = os.cpu_count() or 8
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 2 ** 20
+    except OSError:
+        pass
+    return 0.0
+
+
+def _trace(ctx, bvh, rays_d, traversal, q=0):
+    ctx.set_traversal(traversal)
+    try:
+        return hits_np(ctx.intersect(bvh, rays_d, query=q))
+    finally:
+        ctx.set_traversal(0)
+
+
+@pytest.fixture(scope="module")
+def c1(orc):
+    from radeonrays_sdk_gb300 import scenes
+    v, i, rays = scenes.config1()
+    assert i.shape[0] == 4_193_408 and rays.shape[0] == 16_777_216
+    occl = rays.copy()
+    occl[:, 7] = np.random.default_rng(0x52520001).uniform(0.01, 0.5, rays.shape[0]).astype(np.float32)
+    nodes, _, _ = orc.build_mesh(v, i, threads=THREADS)
+    want = orc.trace(nodes, rays, threads=THREADS)
+    want_any = orc.trace(nodes, occl, query=1, threads=THREADS)
+    return v, i, rays, occl, nodes, want, want_any
+
+
+def test_config1_full_build_and_plain_traversal(ctx, orc, c1):
+    import torch
+    v, i, rays, occl, nodes, want, want_any = c1
+    n = i.shape[0]
+    bvh = ctx.build_geometry(to_dev(v), to_dev(i))
+    got_nodes = bvh[: nodes.size * 64].cpu().numpy().view(np.uint32).reshape(-1, 16)
+    assert np.array_equal(got_nodes, nodes.view(np.uint32).reshape(-1, 16))
+    assert trailer_of(bvh, n)["leaf_count"] == n
+    rays_d, occl_d = to_dev(rays), to_dev(occl)
+    for trav in (1, 3):
+        assert np.array_equal(_trace(ctx, bvh, rays_d, trav), want), trav
+        assert np.array_equal(_trace(ctx, bvh, occl_d, trav, q=1), want_any), trav
+    assert ctx.device_errors() == 0
+    del bvh
+    torch.cuda.empty_cache()
+
+
+def test_config1_full_chosen_ties_only(ctx, orc, c1):
+    import torch
+    from radeonrays_sdk_gb300 import rr
+    v, i, rays, occl, nodes, want, want_any = c1
+    rays_d, occl_d = to_dev(rays), to_dev(occl)
+    for quality in (False, True):
+        bvh = ctx.build_geometry(to_dev(v), to_dev(i), quality=quality)
+        if quality:  # the reference's visit order on the restructured tree
+            qn = bvh[: nodes.size * 64].cpu().numpy().view(rr.NODE_DTYPE)
+            ref = orc.trace(qn, rays, threads=THREADS)
+            ref_any = orc.trace(qn, occl, query=1, threads=THREADS)
+        else:
+            ref, ref_any = want, want_any
+        got = _trace(ctx, bvh, rays_d, 4)
+        hit = ref[:, 2] != INVALID
+        assert np.array_equal(got[:, 2] != INVALID, hit)
+        ties = tie_only_mismatch(orc, rays, got, ref, v, i)
+        assert ties < 100, ties
+        same = got[:, 3] == ref[:, 3]
+        assert np.array_equal(got[same & hit], ref[same & hit])
+        ga = _trace(ctx, bvh, occl_d, 4, q=1)
+        assert np.array_equal(ga[:, 2] != INVALID, ref_any[:, 2] != INVALID)
+        del bvh
+        torch.cuda.empty_cache()
+    assert ctx.device_errors() == 0
+
+
+def test_config3_full_wide8_ties_only(ctx, orc, c1):
+    """8-wide nodes with 8-bit conservative bounds: every hit exact, except
+    where two triangles are hit at exactly the same fp32 t."""
+    import torch
+    v, i, rays, occl, nodes, want, want_any = c1
+    bvh = ctx.build_geometry(to_dev(v), to_dev(i), node_format=1)
+    got = _trace(ctx, bvh, to_dev(rays), 2)
+    assert np.array_equal(got[:, 2] != INVALID, want[:, 2] != INVALID)
+    ties = tie_only_mismatch(orc, rays, got, want, v, i)
+    assert ties < 100, ties
+    hit = want[:, 2] != INVALID
+    same = got[:, 3] == want[:, 3]
+    assert np.array_equal(got[same & hit], want[same & hit])
+    ga = _trace(ctx, bvh, to_dev(occl), 2, q=1)
+    assert np.array_equal(ga[:, 2] != INVALID, want_any[:, 2] != INVALID)
+    assert ctx.device_errors() == 0
+    del bvh
+    torch.cuda.empty_cache()
+
+
+def test_config2_full_fused_build_tlas_and_two_level(ctx, orc):
+    import torch
+    from radeonrays_sdk_gb300 import rr, scenes
+    if _mem_available_gb() < 48:
+        pytest.skip("needs about 24 GB of host memory for 2,048 BLAS node arrays")
+    blas, M, rays = scenes.config2(n_blas=2048, nrays=1 << 20)
+    counts = np.array([ix.shape[0] for _, ix in blas])
+    assert counts.size == 2048 and counts.sum() > 60_000_000
+    fused = ctx.build_geometries([(to_dev(vx), to_dev(ix)) for vx, ix in blas], node_format=0)
+    # Sampled BLASes (and the largest) bit-identical to the oracle's builds.
+    pick = sorted(set(np.random.default_rng(7).choice(2048, 48, replace=False).tolist()) | {int(counts.argmax())})
+    for k in pick:
+        want, _, _ = orc.build_mesh(*blas[k], threads=THREADS)
+        got = fused[k][: want.size * 64].cpu().numpy().view(np.uint32).reshape(-1, 16)
+        assert np.array_equal(got, want.view(np.uint32).reshape(-1, 16)), k
+    gpu_nodes = [fused[k][: (2 * int(c) - 1) * 64].cpu().numpy().view(rr.NODE_DTYPE) for k, c in enumerate(counts)]
+    del blas
+    scene = ctx.build_scene(fused, M)
+    tlas, xf = orc.build_scene(gpu_nodes, counts, M)
+    buf = scene.cpu().numpy()
+    assert np.array_equal(buf[: tlas.size * 64].view(np.uint32), tlas.view(np.uint32).reshape(-1))
+    xoff = tlas.size * 64  # [inverse, forward] transforms follow the nodes
+    assert np.array_equal(buf[xoff: xoff + xf.size * 4].view(np.float32).reshape(xf.shape), xf)
+    want = orc.trace_scene(tlas, xf, gpu_nodes, rays, threads=THREADS)
+    assert np.mean(want[:, 2] != INVALID) > 0.05
+    rays_d = to_dev(rays)
+    for trav in (1, 3):
+        assert np.array_equal(_trace(ctx, scene, rays_d, trav), want), trav
+    occl = rays.copy()
+    occl[:, 7] = np.float32(20.0)
+    want_any = orc.trace_scene(tlas, xf, gpu_nodes, occl, query=1, threads=THREADS)
+    assert np.array_equal(_trace(ctx, scene, to_dev(occl), 3, q=1), want_any)
+    assert ctx.device_errors() == 0
+    del fused, scene, gpu_nodes
+    torch.cuda.empty_cache()

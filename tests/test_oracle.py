@@ -281,3 +281,49 @@ def test_oracle_restructure_is_a_valid_cheaper_tree(orc):
     if orc.ref_lib() is not None:
         ok, _ = orc.ref_validate(r1)
         assert ok
+
+
+def test_precise_oracle_is_watertight(orc):
+    """Rays aimed exactly at shared vertices and edges of a grid mesh: the
+    reference's Moller-Trumbore test (common.h:103-137) lets some through
+    the cracks between triangles; the precise mode's watertight test (exact
+    edge-function signs on the sheared vertices) hits every one."""
+    from edge_rays import bumpy_grid, edge_rays
+    v, i = bumpy_grid()
+    rays = edge_rays(v)
+    nodes, _, _ = orc.build_mesh(v, i)
+    ref = orc.trace(nodes, rays)
+    hp, tp = orc.trace_precise(nodes, rays)
+    assert (ref[:, 2] == 0xFFFFFFFF).sum() > 1000
+    assert (hp[:, 2] == 0xFFFFFFFF).sum() == 0
+    assert np.all(np.isfinite(tp))
+
+
+def test_precise_oracle_t_and_uv_accuracy(orc):
+    """Precise mode: t within 1 ulp and uv within 1e-6 of the fp64
+    intersection of the same ray and triangle, on every hit; the reference's
+    arithmetic is far outside that bound on the same rays."""
+    from radeonrays_sdk_gb300 import scenes
+    v, i, rays = scenes.config1(grid=129, nrays=1 << 16)
+    nodes, _, _ = orc.build_mesh(v, i)
+    hp, tp = orc.trace_precise(nodes, rays)
+    hit = hp[:, 2] != 0xFFFFFFFF
+    assert hit.sum() > 10000
+    idx = i.astype(np.int64)
+    tri9 = np.zeros((rays.shape[0], 9), np.float32)
+    tri9[hit] = v[idx[hp[hit, 3]]].reshape(-1, 9)
+    e = orc.fp64_hit(rays, tri9, hit.astype(np.uint32))
+    ulp = np.abs(tp[hit].astype(np.float64) - e[hit, 0]) / np.spacing(np.abs(tp[hit])).astype(np.float64)
+    assert ulp.max() <= 1.0, ulp.max()
+    uv = hp[hit, :2].view(np.float32).astype(np.float64)
+    assert np.abs(uv - e[hit, 1:3]).max() <= 1e-6
+    # The same rays with the reference's test: hit flags agree except at cracks.
+    ref = orc.trace(nodes, rays)
+    assert np.mean((ref[:, 2] != 0xFFFFFFFF) == hit) > 0.999
+    tr = orc.trace_t(nodes, rays)
+    rh = ref[:, 2] != 0xFFFFFFFF
+    tri9r = np.zeros((rays.shape[0], 9), np.float32)
+    tri9r[rh] = v[idx[ref[rh, 3]]].reshape(-1, 9)
+    er = orc.fp64_hit(rays, tri9r, rh.astype(np.uint32))
+    ulp_r = np.abs(tr[rh].astype(np.float64) - er[rh, 0]) / np.spacing(np.abs(tr[rh])).astype(np.float64)
+    assert ulp_r.max() > 10.0
