@@ -1346,6 +1346,23 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
     uint32_t*              pf    = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(stage->p) + gap);
     std::memset(stage->p, 0, gap + pre);
     uint64_t total = 0;
+    // The 4-wide kernel when the traversal option allows it and every request
+    // with rays has a triangle geometry with 4-wide nodes (or none at all).
+    const uint32_t trav = ctx->topts.traversal;
+    bool           use4 = trav == RR_CUDA_TRAVERSAL_AUTO || trav == RR_CUDA_TRAVERSAL_BVH4;
+    for (uint32_t k = 0; k < count && use4; ++k)
+    {
+        auto it = ctx->registry.find((uintptr_t)dq[k].bvh);
+        if (it == ctx->registry.end())
+        {
+            use4 = dq[k].ray_count == 0;
+            continue;
+        }
+        const BufInfo& b = it->second;
+        use4 = b.kind == kKindGeom && (b.n == 0 || dq[k].ray_count == 0 ||
+                                       (b.format == RR_CUDA_NODE_FORMAT_BVH4 && b.prim_kind == kPrimTriangles &&
+                                        b.wide_off % 256 == 0 && b.wide_off / 256 <= 0xffffffffull));
+    }
     for (uint32_t k = 0; k < count; ++k)
     {
         const DevRequest& q = dq[k];
@@ -1367,6 +1384,12 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
                   (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
                   (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u) |
                   (bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs ? kReqBoxes : 0u);
+        if (use4 && bi.kind == kKindGeom && bi.n > 0 && bi.format == RR_CUDA_NODE_FORMAT_BVH4)
+        {
+            r.flags |= kReqBvh4;
+            r.wide_off256 = (uint32_t)(bi.wide_off / 256);
+            r.wide_limit  = (uint32_t)bi.wide_capacity;
+        }
         rq[k] = r;
         pf[k] = (uint32_t)total;
         total += q.ray_count;
@@ -1386,6 +1409,7 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
     a.sm_count         = ctx->sm_count;
     a.blocks_per_sm    = (int)ctx->topts.blocks_per_sm;
     a.collect_stats    = ctx->topts.collect_stats ? 1 : 0;
+    a.use_bvh4         = use4 ? 1 : 0;
     const size_t bytes = gap + pre;
     *out               = [=](cudaStream_t s) -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(sc + L.req_off, stage->p, bytes, cudaMemcpyHostToDevice, s);

@@ -334,6 +334,7 @@ constexpr uint32_t kReqAny   = 1;  // any-hit query (else closest)
 constexpr uint32_t kReqFull  = 2;  // full RRHit output (else instance id)
 constexpr uint32_t kReqEmpty = 4;  // geometry without triangles: every ray misses
 constexpr uint32_t kReqBoxes = 8;  // AABB-list geometry: leaves are boxes
+constexpr uint32_t kReqBvh4  = 16; // traced over the geometry's 4-wide nodes
 struct __align__(16) BatchTraceReq
 {
     const uint8_t* bvh;   // geometry result buffer (binary nodes at offset 0)
@@ -342,6 +343,8 @@ struct __align__(16) BatchTraceReq
     uint32_t       ray_count;
     uint32_t       node_limit;  // binary nodes in the buffer (kInvalid: unknown)
     uint32_t       flags;
+    uint32_t       wide_off256; // kReqBvh4: byte offset of the 4-wide nodes / 256
+    uint32_t       wide_limit;  // kReqBvh4: 4-wide node capacity
     uint32_t       pad;
 };
 static_assert(sizeof(BatchTraceReq) == 48, "request layout");
@@ -367,10 +370,12 @@ struct BatchTraceArgs
     int                  sm_count;
     int                  blocks_per_sm;
     int                  collect_stats;
+    int                  use_bvh4;  // every request kReqBvh4 or empty: the 4-wide kernel
 };
-// Every request's rays in one persistent launch (reference visit order per
-// ray, so each hit equals the single-request result).  The request table and
-// prefix must already be in the scratch.
+// Every request's rays in one persistent launch (per ray the visit order of
+// the single-request kernel it stands for -- the reference's binary order, or
+// the 4-wide kernel's with use_bvh4 -- so each hit equals the single-request
+// result).  The request table and prefix must already be in the scratch.
 cudaError_t launch_trace_batch(const BatchTraceArgs& a, cudaStream_t s);
 
 cudaError_t launch_trace_binary(const TraceArgs& a, cudaStream_t s);

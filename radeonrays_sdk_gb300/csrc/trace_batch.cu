@@ -9,6 +9,12 @@
 // per-ray state machine as the single-request persistent kernel
 // (trace_persistent.cuh): the reference's visit order and arithmetic, so every
 // hit is bit-identical to tracing that request alone with rrCmdIntersect.
+//
+// With 4-wide geometries (use_bvh4: every request's buffer carries 4-wide
+// nodes) the lanes run the 4-wide kernel's state machine (trace_bvh4.cuh)
+// instead, so each hit equals that request traced alone with
+// RR_CUDA_TRAVERSAL_BVH4.
+#include "trace_bvh4.cuh"
 #include "trace_persistent.cuh"
 
 namespace rr
@@ -119,10 +125,114 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
     }
 }
 
+// The 4-wide variant: the same refill loop around b4_step; a request's
+// 4-wide nodes sit wide_off256 * 256 bytes into its buffer, its binary leaves
+// (the triangles) at [n - 1, 2n - 2].
+template <bool kStats>
+__global__ void __launch_bounds__(kPBlock, 8) k_trace_batch_bvh4(BatchTraceArgs a, uint32_t gcap)
+{
+    __shared__ uint32_t s_stack[kPBlock * kPShort];
+    const uint32_t      tglob = blockIdx.x * blockDim.x + threadIdx.x;
+    PStack              st;
+    st.s     = s_stack + threadIdx.x;
+    st.g     = reinterpret_cast<uint32_t*>(a.scratch + a.spill_off) + (uint64_t)tglob * gcap;
+    st.gcap  = gcap;
+    st.depth = kPShort;
+    uint32_t*      ray_ctr = reinterpret_cast<uint32_t*>(a.scratch);
+    const uint32_t lane    = threadIdx.x & 31;
+    const uint32_t lt      = (1u << lane) - 1u;
+    const uint32_t count   = a.total;
+
+    B4Ray           s;
+    const BvhNode*  nodes = nullptr;
+    const Bvh4Node* wn    = nullptr;
+    uint32_t        gid = kInvalid, r = 0, nlim = 0, wlim = 0, first_leaf = 0, nf = 0, tf = 0;
+    bool            any = false, active = false, pending = false, exhausted = false;
+    for (;;)
+    {
+        __syncwarp();
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
+        {
+            const uint32_t n    = exhausted ? 0u : __popc(idle);
+            uint32_t       base = 0;
+            if (n)
+            {
+                const int leader = __ffs(idle) - 1;
+                if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+                base      = __shfl_sync(0xffffffffu, base, leader);
+                exhausted = base + n >= count;
+            }
+            if (!active)
+            {
+                if (pending)
+                {
+                    void*      hits = a.req[r].hits;
+                    const bool full = (a.req[r].flags & kReqFull) != 0;
+                    if (s.best != kInvalid)
+                    {
+                        const NodeView nd = load_binary_node(nodes, s.best);
+                        if (full)
+                            write_hit<true>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                        else
+                            write_hit<false>(hits, gid, s.ray, s.ct, nd.l0, nd.h0, nd.l1, 0u, nd.child1, nd.child1);
+                    }
+                    else if (full)
+                        write_miss<true>(hits, gid);
+                    else
+                        write_miss<false>(hits, gid);
+                    if (kStats)
+                    {
+                        atomicAdd(&a.words->rays, 1ull);
+                        atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
+                        atomicAdd(&a.words->tri_fetches, (unsigned long long)tf);
+                    }
+                    pending = false;
+                }
+                const uint32_t my = base + __popc(idle & lt);
+                if (n && my < count)
+                {
+                    r                      = batch_find(a.prefix, a.count, my);
+                    gid                    = my - __ldg(a.prefix + r);
+                    const BatchTraceReq& q  = a.req[r];
+                    const uint32_t       fl = q.flags;
+                    if (fl & kReqEmpty)
+                    {
+                        if (fl & kReqFull)
+                            write_miss<true>(q.hits, gid);
+                        else
+                            write_miss<false>(q.hits, gid);
+                    }
+                    else
+                    {
+                        active     = true;
+                        nf = tf    = 0;
+                        nodes      = reinterpret_cast<const BvhNode*>(q.bvh);
+                        wn         = reinterpret_cast<const Bvh4Node*>(q.bvh + (size_t)q.wide_off256 * 256);
+                        nlim       = q.node_limit;
+                        first_leaf = (nlim + 1u) / 2u - 1u;
+                        wlim       = q.wide_limit;
+                        any        = (fl & kReqAny) != 0;
+                        b4_start<false>(s, load_ray(q.rays, gid));
+                    }
+                }
+            }
+        }
+        const uint32_t amask = __ballot_sync(0xffffffffu, active);
+        if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
+        if (active &&
+            b4_step<false, false, true>(s, wn, nodes, wlim, first_leaf, nlim, st, a.words, nf, tf, any))
+        {
+            active  = false;
+            pending = true;
+        }
+    }
+}
+
 template <bool kStats>
 cudaError_t go(const BatchTraceArgs& a, cudaStream_t s)
 {
-    auto kern   = k_trace_batch<kStats>;
+    auto kern   = a.use_bvh4 ? k_trace_batch_bvh4<kStats> : k_trace_batch<kStats>;
     int  per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {

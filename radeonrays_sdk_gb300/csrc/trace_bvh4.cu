@@ -26,78 +26,6 @@ namespace rr
 namespace
 {
 using namespace stream_detail;
-struct B4Ray
-{
-    Ray      ray;
-    F3       inv, oxi;
-    float    ct;
-    uint32_t best;   // binary leaf node of the closest hit (kInvalid: none)
-    uint32_t ref;    // reference to fetch next
-    uint32_t gsp;    // entries spilled to global
-    uint32_t steps;
-    int      sp;     // entries in the short stack
-};
-
-// kPrecise: `inv` is the exact reciprocal and `oxi` the origin (the robust
-// box test of trace_precise.cuh).
-template <bool kPrecise>
-__device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
-{
-    s.ray  = r;
-    s.inv  = kPrecise ? exact_invdir(r.d) : safe_invdir(r.d);
-    s.oxi  = kPrecise ? r.o : f3(-r.o.x * s.inv.x, -r.o.y * s.inv.y, -r.o.z * s.inv.z);
-    s.ct   = r.tmax;
-    s.best = kInvalid;
-    s.ref  = 0;  // the root 4-wide node
-    s.gsp = s.steps = 0;
-    s.sp            = 0;
-}
-
-// One step; returns true when the ray is finished (stack empty, or a hit
-// accepted by an any-hit query).  nf / tf count node and leaf fetches.
-template <bool kAny, bool kPrecise>
-__device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ wn, const BvhNode* __restrict__ nodes,
-                                        uint32_t wlim, uint32_t first_leaf, uint32_t node_limit, const PStack& st,
-                                        DeviceWords* words, uint32_t& nf, uint32_t& tf)
-{
-    const uint32_t ref = s.ref;
-    const bool     leaf = (ref & kBvh4Leaf) != 0;
-    const uint32_t idx  = ref & ~kBvh4Leaf;
-    if (++s.steps > kFetchCap || (leaf ? (idx < first_leaf || idx >= node_limit) : idx >= wlim))
-    {
-        raise_error(words, RR_CUDA_DEVICE_ERROR_NODE_RANGE);
-        s.best = kInvalid;
-        return true;
-    }
-    bool pop = true, done = false;
-    if (leaf)
-    {
-        const float4* p = reinterpret_cast<const float4*>(nodes + idx);
-        const float4  a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-        ++tf;
-        const F3    v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
-        const float t  = kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct) : isect_tri(s.ray, v0, v1, v2, s.ct);
-        if (t < s.ct)
-        {
-            s.ct   = t;
-            s.best = idx;
-            if (kAny) done = true;
-        }
-    }
-    else
-    {
-        const B4Hits h = b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
-        ++nf;
-        if (h.n)
-        {
-            s.ref = b4_descend(h, s.sp, s.gsp, st, words);
-            pop   = false;
-        }
-    }
-    if (pop && !done && !b4_pop(s.sp, s.gsp, st, s.ref)) done = true;
-    return done;
-}
-
 // kStream: the streamed variant for host-buffer tracing (trace_stream.cuh),
 // with the same arrival waits and done counts as the persistent binary
 // kernel's streamed variant.

@@ -6,13 +6,19 @@ oracle (the CPU restatement of isect.comp:88-246 and isect_2l.comp:136-323).
     persistent kernels bit-identical to the oracle for closest hit and for
     any hit (occlusion rays, tmax ~ U[0.01, 0.5]); the 4-wide kernel (fast
     and quality trees) with identical hit flags and primitive ids that differ
-    only at exact equal-t ties;
+    only where the two triangles' distances are equal or within 2 ulp;
   * the same heightfield with 8-wide 8-bit-bounded nodes: identical hit flags
-    and only equal-t ties against the plain path, on every ray;
+    and the same tie rule against the plain path, on every ray;
   * 2,048 BLASes (68.6 M triangles) built in one fused build and a TLAS of
     2,048 instances: sampled BLASes bit-identical to the oracle's builds, the
     TLAS nodes and transforms bit-identical, and the plain and persistent
     two-level kernels bit-identical to the oracle on 1,048,576 rays.
+
+A visit order other than the reference's can keep a triangle 1-2 ulp
+farther than the reference's on a handful of the 16.8 M rays: the reference's
+fp32 slab test (common.h:150-164) culls a box whose entry distance rounds past
+the closest t found so far, so which of two nearly equidistant triangles
+survives depends on the order in which they are found.
 """
 import os
 
@@ -90,7 +96,7 @@ def test_config1_full_chosen_ties_only(ctx, orc, c1):
         got = _trace(ctx, bvh, rays_d, 4)
         hit = ref[:, 2] != INVALID
         assert np.array_equal(got[:, 2] != INVALID, hit)
-        ties = tie_only_mismatch(orc, rays, got, ref, v, i)
+        ties = tie_only_mismatch(orc, rays, got, ref, v, i, near_ulp=2)
         assert ties < 100, ties
         same = got[:, 3] == ref[:, 3]
         assert np.array_equal(got[same & hit], ref[same & hit])
@@ -109,7 +115,7 @@ def test_config3_full_wide8_ties_only(ctx, orc, c1):
     bvh = ctx.build_geometry(to_dev(v), to_dev(i), node_format=1)
     got = _trace(ctx, bvh, to_dev(rays), 2)
     assert np.array_equal(got[:, 2] != INVALID, want[:, 2] != INVALID)
-    ties = tie_only_mismatch(orc, rays, got, want, v, i)
+    ties = tie_only_mismatch(orc, rays, got, want, v, i, near_ulp=2)
     assert ties < 100, ties
     hit = want[:, 2] != INVALID
     same = got[:, 3] == want[:, 3]

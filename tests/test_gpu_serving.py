@@ -15,9 +15,10 @@ def _scenes():
             scenes.soup(40000, scenes.rng(50, 2))]
 
 
-def _alone(ctx, bvh, rays, q, o):
-    """The request traced alone by rrCmdIntersect with the plain kernel."""
-    ctx.set_traversal(1)
+def _alone(ctx, bvh, rays, q, o, traversal=1):
+    """The request traced alone by rrCmdIntersect (the plain kernel, or the
+    4-wide kernel for the 4-wide launches)."""
+    ctx.set_traversal(traversal)
     h = hits_np(ctx.intersect(bvh, to_dev(rays), query=q, output=o))
     ctx.set_traversal(0)
     return h
@@ -69,6 +70,51 @@ def test_server_results_equal_alone_under_eviction(ctx):
     assert stats["latency_ms"]["p99"] >= stats["latency_ms"]["p50"] > 0
     assert ctx.device_errors() == 0
     bvhs = {k: pool.build(k) for k in range(len(ms))}
-    for r in reqs:
-        want = _alone(ctx, bvhs[r.scene], r.rays, r.query, r.output)
+    for r in reqs:  # the pool's scenes have 4-wide nodes: the launches ran the 4-wide kernel
+        want = _alone(ctx, bvhs[r.scene], r.rays, r.query, r.output, traversal=4)
         assert np.array_equal(r.hits, want), r.rid
+
+
+def test_batch_bvh4_equals_alone_and_oracle(ctx, orc):
+    """Requests whose geometries all carry 4-wide nodes run the 4-wide
+    multi-request kernel: each request's hits equal the 4-wide kernel's on
+    that request alone, bit for bit, and the oracle's up to equal-t ties."""
+    from radeonrays_sdk_gb300 import scenes
+    from gpu_util import tie_only_mismatch
+    ms = _scenes()
+    bvhs = [ctx.build_geometry(to_dev(v), to_dev(i)) for v, i in ms]
+    empty = ctx.build_geometry(to_dev(np.zeros((0, 3), np.float32)), to_dev(np.zeros((0, 3), np.uint32)))
+    spec = [(0, 5000, 0, 0), (1, 1, 1, 0), (2, 77777, 0, 1), (0, 0, 0, 0), (1, 20000, 1, 1), (-1, 300, 0, 0),
+            (2, 4096, 1, 0), (1, 30000, 0, 0)]
+    reqs, host = [], []
+    for k, (s, n, q, o) in enumerate(spec):
+        v = ms[max(s, 0)][0]
+        rays = scenes.incoherent_rays(n, v.min(axis=0), v.max(axis=0), scenes.rng(53, k))
+        if q == 1 and n:
+            rays[:, 7] = np.float32(0.2)
+        reqs.append((empty if s < 0 else bvhs[s], to_dev(rays), q, o))
+        host.append((s, rays, q, o))
+    ctx.set_traversal(0)
+    got = [hits_np(h) for h in ctx.intersect_batch(reqs)]
+    ctx.set_traversal(1)  # a binary traversal option keeps the reference-order kernel
+    plain = [hits_np(h) for h in ctx.intersect_batch(reqs)]
+    ctx.set_traversal(0)
+    assert ctx.device_errors() == 0
+    for (s, rays, q, o), (bvh, _, _, _), g, p in zip(host, reqs, got, plain):
+        if rays.shape[0] == 0:
+            continue
+        assert np.array_equal(g, _alone(ctx, bvh, rays, q, o, traversal=4)), (s, q, o)
+        assert np.array_equal(p, _alone(ctx, bvh, rays, q, o, traversal=1)), (s, q, o)
+        if s < 0:
+            miss = g[:, 2] if o == 0 else g
+            assert np.all(miss == INVALID)
+            continue
+        v, i = ms[s]
+        want = orc.trace(orc.build_mesh(v, i)[0], rays, query=q, output=0)
+        gf = g if o == 0 else None
+        if o == 0:
+            assert np.array_equal(gf[:, 2] != INVALID, want[:, 2] != INVALID)
+            if q == 0:
+                tie_only_mismatch(orc, rays, gf, want, v, i)
+        else:
+            assert np.array_equal(g != INVALID, want[:, 2] != INVALID)
