@@ -37,9 +37,15 @@ Reported (one JSON line on rank 0):
 With --gpus N under torchrun every rank traces its own 16,777,216 rays against
 its own replica of the BVH (replicas only: the path has no exchange step).
 
-Other workloads (not the headline line): --workload blas2048 (fused build of
-2,048 BLASes + two-level traversal) and --workload serving (resident scenes,
-continuous batching, p50/p99 request latency).
+  blas2048     the batching configuration: fused build of 2,048 BLASes and
+               two-level traversal, chosen vs plain (summary of
+               --workload blas2048, without its one-by-one build baseline)
+  serving      the serving configuration: resident scenes, continuous
+               batching, throughput and p50/p99 request latency at 50/80/95%
+               of saturation, 10,000 requests per load point, and a checked
+               sample (summary of --workload serving)
+Other workloads (their own JSON line): --workload blas2048 and
+--workload serving.
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port of isect.comp; the reference's own bvh_analyzer cannot be built
@@ -84,6 +90,8 @@ def parse():
     ap.add_argument("--no-anyhit", action="store_true", help="skip the any-hit (occlusion) measurement")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the 8-wide 8-bit-bounds run (hit identity and fp64 error of that format)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batching (2,048 BLASes) and serving summaries of the default line")
     ap.add_argument("--no-precise", action="store_true",
                     help="skip the precise triangle test run (watertight, accurate t; opt-in mode)")
     ap.add_argument("--e2e-chunk", type=int, default=0,
@@ -102,8 +110,10 @@ def parse():
     ap.add_argument("--no-separate", action="store_true",
                     help="blas2048: skip the one-by-one build baseline (about 160,000 launches)")
     ap.add_argument("--scenes", type=int, default=64)
-    ap.add_argument("--requests", type=int, default=300)
+    ap.add_argument("--requests", type=int, default=10000, help="serving: requests per load point")
     ap.add_argument("--slots", type=int, default=3)
+    ap.add_argument("--scene-format", default="bvh4", choices=["bvh4", "binary"],
+                    help="serving: node format of the resident scenes (bvh4 runs the 4-wide multi-request kernel)")
     ap.add_argument("--slot-rays", type=int, default=1 << 22)
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0)
     ap.add_argument("--chosen-format", default="bvh4", choices=["wide8", "bvh4"],
@@ -391,6 +401,22 @@ def run_ours(args):
     b_per, b_total = time_steps(build_step, 5, 2, 1, stream)
     build = {"ms": statistics.median(b_per), "mtris_s": ntri / statistics.median(b_per) / 1e3,
              "format": "binary + bvh4", "triangles": ntri, "flags": "PREFER_FAST_BUILD (reference LBVH)"}
+    # RR_BUILD_OPERATION_UPDATE (refit of the same topology, then the 4-wide
+    # collapse again) with the vertices moved up by 1 %; then back, so that
+    # the tree traced below is the built one.
+    v_up = (v_d * 1.01).contiguous()
+    u_scratch = torch.empty(max(1, s_bytes), dtype=torch.uint8, device="cuda")
+
+    def update_step(vv=v_up):
+        ctx.update_geometry(vv, i_d, bvh, stream=ext, scratch=u_scratch)
+        ctx.release_ptrs()
+    u_per, _ = time_steps(update_step, 5, 2, 1, stream)
+    update_step(v_d)
+    torch.cuda.synchronize()
+    build["update"] = {"ms": statistics.median(u_per), "mtris_s": ntri / statistics.median(u_per) / 1e3,
+                       "operation": "RR_BUILD_OPERATION_UPDATE: leaves take the new vertices, atomic refit, "
+                                    "4-wide collapse again"}
+    del v_up
     # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
     # LBVH + treelet restructure); the plain path the reference's fast LBVH.
     bvh_c = bvh
@@ -653,18 +679,45 @@ def run_ours(args):
         if not args.no_cpu:
             wide8["fp64_t_error"] = precision_report(v, i, rays, h8, nodes)
         line["precision_wide8"] = wide8
-    print(json.dumps(line), flush=True)
     ctx.close()
+    if ws == 1 and not args.no_extras and not args.only:
+        # The batching and serving configurations, summarised in the same line.
+        del rays_d, hits_d, scratch_t, bvh, bvh_c, v_d, i_d
+        torch.cuda.empty_cache()
+        b = batch_summary(args, separate=False)
+        line["blas2048"] = {"workload": b["workload"], "fused_build_ms": b["build"]["fused_ms"],
+                            "fused_build_mtris_s": b["build"]["fused_mtris_s"], "tlas_ms": b["build"]["tlas_ms"],
+                            "chosen": b["trace"]["chosen"], "plain": b["trace"]["plain"],
+                            "chosen_kernel": b["chosen_traversal"]["kernel"],
+                            "speedup_vs_plain": b["speedup_vs_plain"], "hit_flags_identical": b["hit_flags_identical"],
+                            "hit_mismatches_vs_plain": b["hit_mismatches_vs_plain"], "device_errors": b["device_errors"]}
+        torch.cuda.empty_cache()
+        sv = serving_summary(args)
+        line["serving"] = {"workload": sv["workload"], "requests_per_point": args.requests,
+                           "saturation_mrays_s": sv["saturation"]["throughput_mrays_s"],
+                           "load_sweep": [{"offered_load": r["offered_load"], "throughput_mrays_s":
+                                           r["throughput_mrays_s"], "p50_ms": r["latency_ms"]["p50"],
+                                           "p99_ms": r["latency_ms"]["p99"], "makespan_s": r["makespan_s"],
+                                           "launches": r["launches"]} for r in sv["load_sweep"]],
+                           "hits_checked": sv["hits_checked"], "device_errors": sv["device_errors"]}
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args):
-    """--workload blas2048: 2,048 soups with log-uniform 64..262,144 triangles
-    built in one fused build (rrCudaCmdBuildGeometries, replayed as a CUDA
-    graph) against one rrCmdBuildGeometry per BLAS; then the instance tree
-    and incoherent two-level closest-hit traversal, chosen vs plain."""
+    """--workload blas2048: the summary below as its own JSON line."""
     import torch
     ws, rank, local = dist()
     torch.cuda.set_device(local)
+    print(json.dumps(batch_summary(args, separate=not args.no_separate)), flush=True)
+
+
+def batch_summary(args, separate=True):
+    """2,048 soups with log-uniform 64..262,144 triangles built in one fused
+    build (rrCudaCmdBuildGeometries, replayed as a CUDA graph) against one
+    rrCmdBuildGeometry per BLAS (`separate`); then the instance tree and
+    incoherent two-level closest-hit traversal, chosen (autotuned) vs plain,
+    with the hits of the two classified."""
+    import torch
     from radeonrays_sdk_gb300 import rr, scenes
     blas, M, rays = scenes.config2(n_blas=args.blas, nrays=args.batch_rays)
     counts = np.array([i.shape[0] for _, i in blas])
@@ -696,7 +749,7 @@ def run_batch(args):
     keep = ctx._keep
     f_t = timed(lambda: ctx.submit(cs), max(3, args.steps // 10), 2)
     # One rrCmdBuildGeometry per BLAS, each enqueued at once on a CUDA stream.
-    s_t = [float("nan")] if args.no_separate else \
+    s_t = [float("nan")] if not separate else \
         timed(lambda: ctx.build_geometries(meshes, node_format=fmt, api="separate"), 2, 1)
     errors = ctx.device_errors()
     scene = ctx.build_scene(fused, M)
@@ -748,27 +801,35 @@ def run_batch(args):
                                                "selected_by": "rrCudaAutotuneTraversal"},
             "speedup_vs_plain": out["plain"]["ms"] / out["chosen"]["ms"],
             "hit_flags_identical": flags_equal, "hit_mismatches_vs_plain": mism, "device_errors": int(errors)}
-    print(json.dumps(line), flush=True)
     del keep
     ctx.release_stream(cs)
     ctx.close()
+    return line
 
 
 def run_serving(args):
-    """--workload serving: 64 resident scenes (log-uniform 10^4..2x10^6
-    triangles, soup or heightfield), Poisson arrivals of log-uniform 1,024..
-    1,048,576-ray requests (70% closest, 30% any-hit), continuous batching
-    into rrCudaCmdIntersectBatch launches.  Saturation throughput first (all
-    requests at t = 0), then offered loads of 50/80/95% of it: throughput and
-    p50/p99 request latency (arrival to hits in host memory)."""
+    """--workload serving: the summary below as its own JSON line."""
     import torch
     ws, rank, local = dist()
     torch.cuda.set_device(local)
+    print(json.dumps(serving_summary(args)), flush=True)
+
+
+def serving_summary(args):
+    """64 resident scenes (log-uniform 10^4..2x10^6 triangles, soup or
+    heightfield), Poisson arrivals of log-uniform 1,024..1,048,576-ray
+    requests (70% closest, 30% any-hit), continuous batching into
+    rrCudaCmdIntersectBatchHost launches.  Saturation throughput first (all
+    requests at t = 0), then offered loads of 50/80/95% of it: throughput and
+    p50/p99 request latency (arrival to hits in host memory)."""
+    import torch
     from radeonrays_sdk_gb300 import rr, serving
     meshes = serving.config4(args.scenes)
     ntri = sum(i.shape[0] for _, i in meshes)
     ctx = rr.Context()
-    pool = serving.ScenePool(ctx, int(args.hbm_budget_gb * (1 << 30)))
+    pool = serving.ScenePool(ctx, int(args.hbm_budget_gb * (1 << 30)),
+                             node_format=rr.RR_CUDA_NODE_FORMAT_BINARY if args.scene_format == "binary" else
+                             rr.RR_CUDA_NODE_FORMAT_BVH4)
     for k, (v, i) in enumerate(meshes):
         pool.register(k, v, i)
     torch.cuda.synchronize()
@@ -779,15 +840,30 @@ def run_serving(args):
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     server = serving.Server(ctx, pool, slot_rays=args.slot_rays, slots=args.slots, max_requests=256)
-    warm = serving.make_requests(meshes, 16, rate_per_s=1e9, seed=40)
+    # Checked first: requests with their own buffers, each against the same
+    # request traced alone by rrCmdIntersect with the kernel the launches run.
+    check = serving.make_requests(meshes, 48, rate_per_s=1e9, hi_rays=1 << 16, seed=39)
+    server.run(check)
+    alone_trav = rr.RR_CUDA_TRAVERSAL_BINARY if args.scene_format == "binary" else rr.RR_CUDA_TRAVERSAL_BVH4
+    ctx.set_traversal(alone_trav)
+    same = 0
+    for r in check:
+        alone = ctx.intersect(pool.build(r.scene), torch.from_numpy(r.rays).cuda(), query=r.query,
+                              output=r.output).cpu().numpy().view(np.uint32)
+        same += int(np.array_equal(r.hits, alone))
+    ctx.set_traversal(0)
+    # Timed runs: rays are slices of pinned per-scene pools, hits go to a
+    # pinned ring, so that thousands of requests need no per-request buffers.
+    pools = serving.RayPools(meshes)
+    warm = serving.make_requests(meshes, 64, rate_per_s=1e9, seed=40, pools=pools)
     server.run(warm)
-    sat_reqs = serving.make_requests(meshes, args.requests, rate_per_s=1e9, seed=41)
+    sat_reqs = serving.make_requests(meshes, args.requests, rate_per_s=1e9, seed=41, pools=pools)
     sat = server.run(sat_reqs)
     mean_rays = sat["rays"] / sat["requests"]
     cap = sat["throughput_mrays_s"] * 1e6 / mean_rays  # requests per second at saturation
     sweep = []
     for k, frac in enumerate((0.5, 0.8, 0.95)):
-        reqs = serving.make_requests(meshes, args.requests, rate_per_s=frac * cap, seed=42 + k)
+        reqs = serving.make_requests(meshes, args.requests, rate_per_s=frac * cap, seed=42 + k, pools=pools)
         res = server.run(reqs)
         res["offered_load"] = frac
         res["rate_req_s"] = frac * cap
@@ -799,9 +875,16 @@ def run_serving(args):
             "slots": args.slots, "slot_rays": args.slot_rays, "hbm_budget_gb": args.hbm_budget_gb,
             "scene_build_s": build_s, "resident_bytes": pool.bytes, "saturation": sat, "load_sweep": sweep,
             "latency_definition": "arrival to hits copied to the request's pinned host buffer",
+            "scene_format": "binary nodes only (launches run the reference-order multi-request kernel)"
+                            if args.scene_format == "binary" else
+                            "binary + 4-wide nodes (launches run the 4-wide multi-request kernel)",
+            "hits_checked": {"requests": len(check), "identical_to_alone": same,
+                             "against": "each request traced alone by rrCmdIntersect with "
+                                        + ("RR_CUDA_TRAVERSAL_BINARY" if args.scene_format == "binary" else
+                                           "RR_CUDA_TRAVERSAL_BVH4")},
             "device_errors": ctx.device_errors()}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
 def main():

@@ -21,8 +21,10 @@ Model:
     different slots overlap on the device: continuous batching at launch
     granularity, with no device-side wait of any kind.
   * Each request's hits are bit-identical to tracing it alone (the batched
-    kernel runs the reference's per-ray visit order), whatever it is packed
-    with; the tests check this.
+    kernel runs, per ray, the visit order of the single-request kernel it
+    stands for: the 4-wide kernel on the pool's default 4-wide scenes, the
+    reference's binary order otherwise), whatever it is packed with; the
+    tests check this.
 """
 from __future__ import annotations
 
@@ -43,6 +45,9 @@ class Request:
     rays: np.ndarray        # (R, 8) float32, host
     query: int = rr.RR_INTERSECT_QUERY_CLOSEST
     output: int = rr.RR_INTERSECT_QUERY_OUTPUT_FULL_HIT
+    # pinned host views (ray pools, make_requests(pools=...)): the server
+    # uses them instead of pinning a copy of `rays`
+    pinned_rays: object = None
     # filled by the server
     admitted: float = -1.0
     done: float = -1.0
@@ -226,12 +231,28 @@ class Server:
         return done
 
     def _pin(self, requests) -> None:
-        """Page-locked host copies of every request's rays and hit records (a
-        client of the loop hands over pinned buffers; done before the clock starts)."""
+        """Page-locked host buffers of every request's rays and hit records (a
+        client of the loop hands over pinned buffers; done before the clock
+        starts).  Requests with pinned views of a ray pool use those, and take
+        their hit records from a pinned ring in arrival order: admission is
+        oldest first, so requests in flight together never share ring memory
+        while the ring holds twice the rays all slots can hold.  A ring
+        request's `hits` stay valid until the ring comes round again."""
         import torch
         self._pinned = {}
-        for r in requests:
+        ring_req = [r for r in requests if r.pinned_rays is not None]
+        ring_rays = 2 * len(self.slots) * self.slot_rays
+        if ring_req and (getattr(self, "_ring", None) is None or self._ring.shape[0] < ring_rays):
+            self._ring = torch.empty((ring_rays, 4), dtype=torch.int32).pin_memory()
+        cur = 0
+        for r in sorted(requests, key=lambda q: q.arrival):
             n = r.rays.shape[0]
+            if r.pinned_rays is not None:
+                if cur + n > self._ring.shape[0]:
+                    cur = 0
+                self._pinned[r.rid] = (r.pinned_rays, self._ring[cur:cur + n])
+                cur += n
+                continue
             rays = torch.from_numpy(np.ascontiguousarray(r.rays, np.float32)).pin_memory()
             hits = torch.empty((n, 4), dtype=torch.int32).pin_memory()
             self._pinned[r.rid] = (rays, hits)
@@ -295,11 +316,36 @@ def config4(n_scenes: int = 64, lo_tris: float = 1e4, hi_tris: float = 2e6, seed
     return out
 
 
+class RayPools:
+    """Pinned host pools of incoherent rays, one closest-hit and one any-hit
+    pool (tmax ~ U[0.01, 0.5]) of `pool_rays` rays per scene, so that long
+    runs of requests need no per-request host buffers.  One unit pool
+    (origins in [0, 1]^3, directions uniform on the sphere) is mapped into
+    each scene's bounding box."""
+
+    def __init__(self, meshes, pool_rays: int = 1 << 20, seed: int = 4):
+        import torch
+        from . import scenes
+        self.pool_rays = int(pool_rays)
+        g = scenes.rng(seed, 9)
+        unit = scenes.incoherent_rays(self.pool_rays, (0, 0, 0), (1, 1, 1), g)
+        tmax_any = g.uniform(0.01, 0.5, size=self.pool_rays).astype(np.float32)
+        self.closest, self.any = [], []
+        for v, _ in meshes:
+            lo, hi = v.min(axis=0).astype(np.float64), v.max(axis=0).astype(np.float64)
+            r = unit.copy()
+            r[:, 0:3] = (lo + unit[:, 0:3].astype(np.float64) * (hi - lo)).astype(np.float32)
+            self.closest.append(torch.from_numpy(r).pin_memory())
+            r[:, 7] = tmax_any
+            self.any.append(torch.from_numpy(r).pin_memory())
+
+
 def make_requests(meshes, n_requests: int, rate_per_s: float, lo_rays: int = 1024, hi_rays: int = 1 << 20,
-                  any_fraction: float = 0.3, seed: int = 4) -> list[Request]:
+                  any_fraction: float = 0.3, seed: int = 4, pools: RayPools | None = None) -> list[Request]:
     """Poisson arrivals at `rate_per_s`; request sizes log-uniform in
     [lo_rays, hi_rays]; 30% any-hit (tmax ~ U[0.01, 0.5]) and 70% closest-hit
-    incoherent rays inside the scene's box."""
+    incoherent rays inside the scene's box.  With `pools`, a request's rays
+    are a random slice of its scene's pinned pool (no copy)."""
     import math
     from . import scenes
     g = scenes.rng(seed, 7)
@@ -311,8 +357,16 @@ def make_requests(meshes, n_requests: int, rate_per_s: float, lo_rays: int = 102
         n = int(round(math.exp(g.uniform(math.log(lo_rays), math.log(hi_rays)))))
         v = meshes[sid][0]
         any_hit = g.random() < any_fraction
+        q = rr.RR_INTERSECT_QUERY_ANY if any_hit else rr.RR_INTERSECT_QUERY_CLOSEST
+        if pools is not None:
+            n = min(n, pools.pool_rays)
+            off = int(g.integers(0, pools.pool_rays - n + 1))
+            pool = (pools.any if any_hit else pools.closest)[sid]
+            view = pool[off:off + n]
+            reqs.append(Request(k, t, sid, view.numpy(), q, pinned_rays=view))
+            continue
         rays = scenes.incoherent_rays(n, v.min(axis=0), v.max(axis=0), scenes.rng(seed, 1000 + k))
         if any_hit:
             rays[:, 7] = g.uniform(0.01, 0.5, size=n).astype(np.float32)
-        reqs.append(Request(k, t, sid, rays, rr.RR_INTERSECT_QUERY_ANY if any_hit else rr.RR_INTERSECT_QUERY_CLOSEST))
+        reqs.append(Request(k, t, sid, rays, q))
     return reqs

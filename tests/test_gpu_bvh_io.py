@@ -72,8 +72,8 @@ def test_pool_checkpoint_and_resume(ctx, tmp_path):
     reqs = serving.make_requests(ms, 12, rate_per_s=1e6, lo_rays=100, hi_rays=3000, seed=95)
     serving.Server(ctx, fresh, slot_rays=1 << 15, slots=2, max_requests=8).run(reqs)
     assert fresh.builds == 0
-    for r in reqs:
-        ctx.set_traversal(1)
+    for r in reqs:  # the pool's default scenes have 4-wide nodes: the launches ran the 4-wide kernel
+        ctx.set_traversal(4)
         want = hits_np(ctx.intersect(pool.resident[r.scene], to_dev(r.rays), query=r.query, output=r.output))
         ctx.set_traversal(0)
         assert np.array_equal(r.hits, want), r.rid
