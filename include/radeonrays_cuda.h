@@ -31,7 +31,13 @@ typedef enum
     RR_CUDA_NODE_FORMAT_WIDE8 = 1,
     /* Binary nodes plus 4-wide 128-byte nodes with exact fp32 child boxes
      * whose leaf children are the binary leaf nodes (the default). */
-    RR_CUDA_NODE_FORMAT_BVH4 = 2
+    RR_CUDA_NODE_FORMAT_BVH4 = 2,
+    /* The node width rrCudaAutotuneNodeFormat picked for meshes of the same
+     * size class (triangle-count octave) on this GPU, from this context or
+     * the RR_CUDA_TUNE_CACHE file; BVH4 when none was picked.  Memory
+     * requirements with AUTO are sized for either width.  A fused build
+     * (rrCudaCmdBuildGeometries) takes its largest mesh's width. */
+    RR_CUDA_NODE_FORMAT_AUTO = 3
 } RRCudaNodeFormat;
 
 /* Passed through RRBuildOptions::backend_specific_info.  A null
@@ -211,6 +217,30 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext               context,
                                        RRDevicePtr             hits,
                                        RRDevicePtr             scratch,
                                        RRCudaTraversalOptions* chosen);
+
+/* Pick the node width for a mesh and a ray workload (no reference
+ * counterpart: the reference has one binary node format).  Builds the mesh
+ * (build_input, with build_options' quality flag) into temporary buffers in
+ * the 4-wide (BVH4) and the 8-wide quantised (WIDE8) formats -- the only
+ * call of this library that allocates device memory for itself -- runs the
+ * traversal autotuner on each with the caller's rays (timed afresh), and
+ * keeps the faster.  The choice is remembered for the mesh's size class
+ * (triangle-count octave) on this GPU, in the context and in the
+ * RR_CUDA_TUNE_CACHE file when set, and later builds with
+ * RR_CUDA_NODE_FORMAT_AUTO use it; the context's traversal option becomes
+ * the winner's.  Synchronous; `hits` and `scratch` as for
+ * rrCudaAutotuneTraversal.  Triangle meshes with the reference's triangle
+ * test only. */
+RR_API RRError rrCudaAutotuneNodeFormat(RRContext                   context,
+                                        const RRGeometryBuildInput* build_input,
+                                        const RRBuildOptions*       build_options,
+                                        RRIntersectQuery            query,
+                                        RRDevicePtr                 rays,
+                                        uint32_t                    ray_count,
+                                        RRIntersectQueryOutput      query_output,
+                                        RRDevicePtr                 hits,
+                                        RRDevicePtr                 scratch,
+                                        uint32_t*                   node_format);
 
 /* Make a geometry result buffer that was not built on this context -- read
  * back from a file, copied from another process or context -- known to it, so

@@ -181,6 +181,7 @@ struct Context
     bool                   graphs   = true;
     bool                   fuse_builds = true;  // fuse consecutive geometry builds of a command stream
     std::string            gpu_name;
+    std::map<std::string, uint32_t> fmt_choice;  // node-format tuner results by mesh-size key
     std::map<std::string, RRCudaTraversalOptions> tuned;  // autotuner results by workload key
     std::map<uintptr_t, BufInfo> registry;
     // Ops run at once on external streams, kept (with the memory they own)
@@ -400,7 +401,7 @@ bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
     const RRCudaBuildOptions* c = reinterpret_cast<const RRCudaBuildOptions*>(o->backend_specific_info);
     if (c->struct_size < sizeof(RRCudaBuildOptions)) return false;
     if (c->node_format != RR_CUDA_NODE_FORMAT_BINARY && c->node_format != RR_CUDA_NODE_FORMAT_WIDE8 &&
-        c->node_format != RR_CUDA_NODE_FORMAT_BVH4)
+        c->node_format != RR_CUDA_NODE_FORMAT_BVH4 && c->node_format != RR_CUDA_NODE_FORMAT_AUTO)
         return false;
     if (c->morton_bits != 0 && c->morton_bits != 30 && c->morton_bits != 63) return false;
     bp.format = c->node_format;
@@ -459,13 +460,52 @@ inline uint32_t build_format(const MeshArgs& ma, uint32_t requested)
 
 // Validate one geometry build (reference radeonrays.cpp:242-299) and resolve
 // its buffers.
-RRError prepare_geometry(const RRGeometryBuildInput* in, const BuildParams& bp, RRDevicePtr temporary_buffer,
-                         RRDevicePtr geometry_buffer, PendingGeom* pg)
+// RR_CUDA_NODE_FORMAT_AUTO: the node width rrCudaAutotuneNodeFormat chose
+// for meshes of this size (triangle-count octave) on this GPU -- from the
+// context, else from the RR_CUDA_TUNE_CACHE file -- or BVH4 when none was.
+std::string fmt_key(const Context* ctx, uint32_t n)
+{
+    uint32_t octave = 0;
+    while ((1ull << (octave + 1)) <= n) ++octave;
+    return "fmt|" + ctx->gpu_name + "|" + std::to_string(octave);
+}
+uint32_t resolve_format(Context* ctx, uint32_t requested, uint32_t n)
+{
+    if (requested != RR_CUDA_NODE_FORMAT_AUTO) return requested;
+    const std::string key = fmt_key(ctx, n);
+    auto              hit = ctx->fmt_choice.find(key);
+    if (hit == ctx->fmt_choice.end())
+    {
+        uint32_t fmt = RR_CUDA_NODE_FORMAT_BVH4;
+        if (const char* path = std::getenv("RR_CUDA_TUNE_CACHE"))
+            if (FILE* f = std::fopen(path, "r"))
+            {
+                char line[512];
+                while (std::fgets(line, sizeof(line), f))
+                {
+                    char*    tab = std::strchr(line, '\t');
+                    unsigned v   = 0;
+                    if (!tab) continue;
+                    *tab = 0;
+                    if (key == line && std::sscanf(tab + 1, "%u", &v) == 1 &&
+                        (v == RR_CUDA_NODE_FORMAT_BVH4 || v == RR_CUDA_NODE_FORMAT_WIDE8))
+                        fmt = v;
+                }
+                std::fclose(f);
+            }
+        hit = ctx->fmt_choice.emplace(key, fmt).first;
+    }
+    return hit->second;
+}
+
+RRError prepare_geometry(Context* ctx, const RRGeometryBuildInput* in, const BuildParams& bp,
+                         RRDevicePtr temporary_buffer, RRDevicePtr geometry_buffer, PendingGeom* pg)
 {
     RRError e = geometry_source(in, true, &pg->ma);
     if (e != RR_SUCCESS) return e;
     if (!geometry_buffer || (!temporary_buffer && pg->ma.n > 0)) return RR_ERROR_INVALID_PARAMETER;
-    pg->L                    = geom_layout(pg->ma.n, build_format(pg->ma, bp.format), bp.bits);
+    const uint32_t fmt       = resolve_format(ctx, bp.format, pg->ma.n);
+    pg->L                    = geom_layout(pg->ma.n, build_format(pg->ma, fmt), bp.bits);
     pg->L.restructure_min    = bp.restructure ? kRestructureMinPrims : 0u;
     pg->L.restructure_passes = bp.restructure ? kRestructurePasses : 0u;
     pg->scratch          = temporary_buffer ? P(temporary_buffer)->addr() : nullptr;
@@ -842,6 +882,152 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
 }
 }  // namespace
 
+namespace
+{
+// The traversal autotuner (rrCudaAutotuneTraversal) on a device buffer.
+// With use_cache false the cached decision is ignored and every candidate is
+// timed again; *best_ms (optional) receives the winner's time per launch
+// (negative when the decision came from the cache).  Throws CudaFail.
+RRError autotune_traversal(Context* ctx, uint8_t* bvh, RRIntersectQuery query, uint8_t* rays_p, uint32_t ray_count,
+                           RRIntersectQueryOutput query_output, uint8_t* hits_p, uint8_t* scratch_p, bool use_cache,
+                           RRCudaTraversalOptions* chosen, float* best_ms_out)
+{
+    if (best_ms_out) *best_ms_out = -1.f;
+    {
+        auto        it  = ctx->registry.find((uintptr_t)bvh);
+        BufInfo     bi;
+        if (it != ctx->registry.end()) bi = it->second;
+        const bool has_wide = (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0) ||
+                              (bi.kind == kKindScene && bi.scene_wide);
+        // Workload key: device, buffer kind, node format and size, query,
+        // output, ray-count octave (the format decides the candidates).
+        uint32_t octave = 0;
+        while ((1ull << (octave + 1)) <= ray_count) ++octave;
+        const uint32_t tt = ctx->topts.triangle_test;
+        if (precise_unsupported(ctx, bvh)) return RR_ERROR_NOT_IMPLEMENTED;
+        const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.format) +
+                                "|" + std::to_string(bi.n) + "|" + std::to_string((int)query) + "|" +
+                                std::to_string((int)query_output) + "|" + std::to_string(octave) +
+                                (tt ? "|t" + std::to_string(tt) : std::string());
+        auto hit = use_cache ? ctx->tuned.find(key) : ctx->tuned.end();
+        const char* cache_path = std::getenv("RR_CUDA_TUNE_CACHE");
+        if (use_cache && hit == ctx->tuned.end() && cache_path)
+        {
+            if (FILE* f = std::fopen(cache_path, "r"))
+            {
+                char     line[512];
+                while (std::fgets(line, sizeof(line), f))
+                {
+                    char*    tab = std::strchr(line, '\t');
+                    unsigned t = 0, ro = 0, bps = 0, depth = 0;
+                    if (!tab) continue;
+                    *tab = 0;
+                    if (key == line && std::sscanf(tab + 1, "%u %u %u %u", &t, &ro, &bps, &depth) >= 3)
+                    {
+                        RRCudaTraversalOptions o{};
+                        o.struct_size   = sizeof(o);
+                        o.traversal     = t;
+                        o.ray_order     = ro;
+                        o.blocks_per_sm = bps;
+                        o.short_stack   = depth;
+                        o.triangle_test = tt;
+                        ctx->tuned[key] = o;
+                    }
+                }
+                std::fclose(f);
+            }
+            hit = ctx->tuned.find(key);
+        }
+        if (hit == ctx->tuned.end())
+        {
+            std::vector<RRCudaTraversalOptions> cand;
+            // The precise test runs in the persistent kernels only.
+            auto add = [&](uint32_t trav, uint32_t order) {
+                if (tt && trav != RR_CUDA_TRAVERSAL_BINARY_PERSISTENT && trav != RR_CUDA_TRAVERSAL_BVH4) return;
+                RRCudaTraversalOptions o{};
+                o.struct_size   = sizeof(o);
+                o.traversal     = trav;
+                o.ray_order     = order;
+                o.triangle_test = tt;
+                cand.push_back(o);
+            };
+            add(RR_CUDA_TRAVERSAL_BINARY, 0);
+            add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
+            if ((bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+                 bi.prim_kind == kPrimTriangles) ||
+                (bi.kind == kKindScene && bi.scene_bvh4))
+                add(RR_CUDA_TRAVERSAL_BVH4, 0);
+            if (has_wide)
+            {
+                add(RR_CUDA_TRAVERSAL_WIDE, 1);
+                if (bi.kind == kKindGeom && ray_count >= (1u << 20)) add(RR_CUDA_TRAVERSAL_WIDE, 2);
+            }
+            cudaEvent_t e0, e1;
+            check(cudaEventCreate(&e0), "event");
+            check(cudaEventCreate(&e1), "event");
+            float best_ms = 1e30f;
+            RRCudaTraversalOptions best = cand[0];
+            auto try_cand = [&](const RRCudaTraversalOptions& o, float margin) {
+                Op op = trace_op(ctx, bvh, rays_p, ray_count, nullptr, hits_p, scratch_p, query, query_output, o);
+                check(op(ctx->stream), "tune warm-up");
+                check(cudaEventRecord(e0, ctx->stream), "event");
+                for (int r = 0; r < 3; ++r) check(op(ctx->stream), "tune run");
+                check(cudaEventRecord(e1, ctx->stream), "event");
+                check(cudaEventSynchronize(e1), "event");
+                float ms = 0.f;
+                check(cudaEventElapsedTime(&ms, e0, e1), "event");
+                RR_LOG_INFO("autotune %s: traversal %u order %u blocks/SM %u stack %u -> %.3f ms", key.c_str(),
+                            o.traversal, o.ray_order, o.blocks_per_sm, o.short_stack, ms / 3.f);
+                if (ms < best_ms * margin)
+                {
+                    best_ms = ms;
+                    best    = o;
+                }
+            };
+            // Stage 1: kernel and node width.  Stage 2: the winner's launch
+            // shape (resident blocks per SM, against the occupancy maximum)
+            // and, for the 4-wide kernel, its shared-stack depth; a stage-2
+            // variant must be 1 % faster to replace the default shape, so
+            // run-to-run noise does not move it.
+            for (const auto& o : cand) try_cand(o, 1.0f);
+            const RRCudaTraversalOptions w = best;
+            if (w.traversal != RR_CUDA_TRAVERSAL_BINARY)
+                for (uint32_t bps : {4u, 6u})
+                {
+                    RRCudaTraversalOptions o = w;
+                    o.blocks_per_sm          = bps;
+                    try_cand(o, 0.99f);
+                }
+            if (w.traversal == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom)
+                for (uint32_t depth : {12u, 24u})
+                {
+                    RRCudaTraversalOptions o = w;
+                    o.short_stack            = depth;
+                    try_cand(o, 0.99f);
+                }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (best_ms_out) *best_ms_out = best_ms / 3.f;
+            ctx->tuned[key] = best;
+            if (cache_path)
+                if (FILE* f = std::fopen(cache_path, "a"))
+                {
+                    std::fprintf(f, "%s\t%u %u %u %u\n", key.c_str(), best.traversal, best.ray_order,
+                                 best.blocks_per_sm, best.short_stack);
+                    std::fclose(f);
+                }
+            hit = ctx->tuned.find(key);
+        }
+        RRCudaTraversalOptions o = hit->second;
+        o.collect_stats          = 0;
+        ctx->topts               = o;
+        if (chosen) *chosen = o;
+        return RR_SUCCESS;
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 RR_API RRError rrSetLogLevel(RRLogLevel log_level)
@@ -922,6 +1108,16 @@ RR_API RRError rrGetGeometryBuildMemoryRequirements(RRContext                   
         if (e != RR_SUCCESS) return e;
         BuildParams bp;
         if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
+        if (bp.format == RR_CUDA_NODE_FORMAT_AUTO)
+        {
+            // Sized for either node width the tuner may pick.
+            const GeomLayout a = geom_layout(ma.n, build_format(ma, RR_CUDA_NODE_FORMAT_BVH4), bp.bits);
+            const GeomLayout b = geom_layout(ma.n, build_format(ma, RR_CUDA_NODE_FORMAT_WIDE8), bp.bits);
+            memory_requirements->result_buffer_size           = std::max(a.total, b.total);
+            memory_requirements->temporary_build_buffer_size  = std::max(a.s_total, b.s_total);
+            memory_requirements->temporary_update_buffer_size = std::max(a.u_total, b.u_total);
+            return RR_SUCCESS;
+        }
         GeomLayout L                                      = geom_layout(ma.n, build_format(ma, bp.format), bp.bits);
         memory_requirements->result_buffer_size           = L.total;
         memory_requirements->temporary_build_buffer_size  = L.s_total;
@@ -984,7 +1180,7 @@ RR_API RRError rrCmdBuildGeometry(RRContext                   context,
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
         PendingGeom pg;
-        RRError     e = prepare_geometry(build_input, bp, temporary_buffer, geometry_buffer, &pg);
+        RRError     e = prepare_geometry(ctx, build_input, bp, temporary_buffer, geometry_buffer, &pg);
         if (e != RR_SUCCESS) return e;
         record_build(S(command_stream), pg);
         register_geometry(ctx, pg);
@@ -1041,9 +1237,23 @@ RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
         DeviceGuard              g(ctx->device);
         std::vector<PendingGeom> geoms(count);
         RangeSet                 used;
+        if (bp.format == RR_CUDA_NODE_FORMAT_AUTO)
+        {
+            // One node width for the whole fused build: the largest mesh's.
+            uint32_t nmax = 0;
+            for (uint32_t i = 0; i < count; ++i)
+            {
+                MeshArgs ma;
+                RRError  e = geometry_source(build_inputs + i, false, &ma);
+                if (e != RR_SUCCESS) return e;
+                nmax = std::max(nmax, ma.n);
+            }
+            bp.format = resolve_format(ctx, RR_CUDA_NODE_FORMAT_AUTO, nmax);
+        }
         for (uint32_t i = 0; i < count; ++i)
         {
-            RRError e = prepare_geometry(build_inputs + i, bp, temporary_buffers[i], geometry_buffers[i], &geoms[i]);
+            RRError e =
+                prepare_geometry(ctx, build_inputs + i, bp, temporary_buffers[i], geometry_buffers[i], &geoms[i]);
             if (e != RR_SUCCESS) return e;
             if (!claim_build_ranges(used, geoms[i])) return RR_ERROR_INVALID_PARAMETER;
         }
@@ -1818,135 +2028,102 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext              context,
     RR_TRY({
         Context*    ctx = C(context);
         DeviceGuard g(ctx->device);
-        uint8_t*    bvh = P(scene_buffer)->addr();
-        auto        it  = ctx->registry.find((uintptr_t)bvh);
-        BufInfo     bi;
-        if (it != ctx->registry.end()) bi = it->second;
-        const bool has_wide = (bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_WIDE8 && bi.n > 0) ||
-                              (bi.kind == kKindScene && bi.scene_wide);
-        // Workload key: device, buffer kind, node format and size, query,
-        // output, ray-count octave (the format decides the candidates).
-        uint32_t octave = 0;
-        while ((1ull << (octave + 1)) <= ray_count) ++octave;
-        const uint32_t tt = ctx->topts.triangle_test;
-        if (precise_unsupported(ctx, bvh)) return RR_ERROR_NOT_IMPLEMENTED;
-        const std::string key = ctx->gpu_name + "|" + std::to_string(bi.kind) + "|" + std::to_string(bi.format) +
-                                "|" + std::to_string(bi.n) + "|" + std::to_string((int)query) + "|" +
-                                std::to_string((int)query_output) + "|" + std::to_string(octave) +
-                                (tt ? "|t" + std::to_string(tt) : std::string());
-        auto hit = ctx->tuned.find(key);
-        const char* cache_path = std::getenv("RR_CUDA_TUNE_CACHE");
-        if (hit == ctx->tuned.end() && cache_path)
+        return autotune_traversal(ctx, P(scene_buffer)->addr(), query, P(rays)->addr(), ray_count, query_output,
+                                  P(hits)->addr(), P(scratch)->addr(), true, chosen, nullptr);
+    })
+}
+
+RR_API RRError rrCudaAutotuneNodeFormat(RRContext                   context,
+                                        const RRGeometryBuildInput* build_input,
+                                        const RRBuildOptions*       build_options,
+                                        RRIntersectQuery            query,
+                                        RRDevicePtr                 rays,
+                                        uint32_t                    ray_count,
+                                        RRIntersectQueryOutput      query_output,
+                                        RRDevicePtr                 hits,
+                                        RRDevicePtr                 scratch,
+                                        uint32_t*                   node_format)
+{
+    if (!context || !build_input || !rays || !hits || !scratch || !ray_count) return RR_ERROR_INVALID_PARAMETER;
+    if (query != RR_INTERSECT_QUERY_CLOSEST && query != RR_INTERSECT_QUERY_ANY) return RR_ERROR_INVALID_PARAMETER;
+    if (query_output != RR_INTERSECT_QUERY_OUTPUT_FULL_HIT && query_output != RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID)
+        return RR_ERROR_INVALID_PARAMETER;
+    RR_TRY({
+        BuildParams bp;
+        if (!parse_build_options(build_options, bp)) return RR_ERROR_INVALID_PARAMETER;
+        Context*    ctx = C(context);
+        DeviceGuard g(ctx->device);
+        MeshArgs    ma;
+        RRError     e = geometry_source(build_input, true, &ma);
+        if (e != RR_SUCCESS) return e;
+        if (ma.n == 0 || ma.prim_kind != kPrimTriangles) return RR_ERROR_INVALID_PARAMETER;
+        if (ctx->topts.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return RR_ERROR_NOT_IMPLEMENTED;
+        uint32_t               best_fmt = RR_CUDA_NODE_FORMAT_BVH4;
+        float                  best_ms  = 1e30f;
+        RRCudaTraversalOptions best_opt{};
+        // Each width: a temporary build on the context's stream (the tuner
+        // allocates; a build call never does), then the traversal tuner on
+        // the caller's rays, timed afresh.
+        for (uint32_t fmt : {(uint32_t)RR_CUDA_NODE_FORMAT_BVH4, (uint32_t)RR_CUDA_NODE_FORMAT_WIDE8})
         {
-            if (FILE* f = std::fopen(cache_path, "r"))
+            PendingGeom pg;
+            pg.ma                    = ma;
+            pg.L                     = geom_layout(ma.n, fmt, bp.bits);
+            pg.L.restructure_min     = bp.restructure ? kRestructureMinPrims : 0u;
+            pg.L.restructure_passes  = bp.restructure ? kRestructurePasses : 0u;
+            uint8_t *sc = nullptr, *res = nullptr;
+            check(cudaMalloc(&sc, pg.L.s_total), "cudaMalloc tuner scratch");
+            if (cudaMalloc(&res, pg.L.total) != cudaSuccess)
             {
-                char     line[512];
-                while (std::fgets(line, sizeof(line), f))
-                {
-                    char*    tab = std::strchr(line, '\t');
-                    unsigned t = 0, ro = 0, bps = 0, depth = 0;
-                    if (!tab) continue;
-                    *tab = 0;
-                    if (key == line && std::sscanf(tab + 1, "%u %u %u %u", &t, &ro, &bps, &depth) >= 3)
-                    {
-                        RRCudaTraversalOptions o{};
-                        o.struct_size   = sizeof(o);
-                        o.traversal     = t;
-                        o.ray_order     = ro;
-                        o.blocks_per_sm = bps;
-                        o.short_stack   = depth;
-                        o.triangle_test = tt;
-                        ctx->tuned[key] = o;
-                    }
-                }
+                cudaFree(sc);
+                throw CudaFail(cudaErrorMemoryAllocation, "cudaMalloc tuner result");
+            }
+            pg.scratch = sc;
+            pg.result  = res;
+            float                  ms = -1.f;
+            RRCudaTraversalOptions o{};
+            RRError                r  = RR_SUCCESS;
+            try
+            {
+                bool many = false;
+                Op   op   = build_batch_op(ctx, {pg}, &many);
+                check(op(ctx->stream), "tuner build");
+                check(cudaStreamSynchronize(ctx->stream), "tuner build");
+                register_geometry(ctx, pg);
+                r = autotune_traversal(ctx, res, query, P(rays)->addr(), ray_count, query_output, P(hits)->addr(),
+                                       P(scratch)->addr(), false, &o, &ms);
+            }
+            catch (...)
+            {
+                ctx->registry.erase((uintptr_t)res);
+                cudaStreamSynchronize(ctx->stream);
+                cudaFree(sc);
+                cudaFree(res);
+                throw;
+            }
+            ctx->registry.erase((uintptr_t)res);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(sc);
+            cudaFree(res);
+            if (r != RR_SUCCESS) return r;
+            RR_LOG_INFO("node-format tune: format %u -> traversal %u, %.3f ms", fmt, o.traversal, ms);
+            if (ms >= 0.f && ms < best_ms)
+            {
+                best_ms  = ms;
+                best_fmt = fmt;
+                best_opt = o;
+            }
+        }
+        const std::string key = fmt_key(ctx, ma.n);
+        ctx->fmt_choice[key]  = best_fmt;
+        if (const char* path = std::getenv("RR_CUDA_TUNE_CACHE"))
+            if (FILE* f = std::fopen(path, "a"))
+            {
+                std::fprintf(f, "%s\t%u\n", key.c_str(), best_fmt);
                 std::fclose(f);
             }
-            hit = ctx->tuned.find(key);
-        }
-        if (hit == ctx->tuned.end())
-        {
-            std::vector<RRCudaTraversalOptions> cand;
-            // The precise test runs in the persistent kernels only.
-            auto add = [&](uint32_t trav, uint32_t order) {
-                if (tt && trav != RR_CUDA_TRAVERSAL_BINARY_PERSISTENT && trav != RR_CUDA_TRAVERSAL_BVH4) return;
-                RRCudaTraversalOptions o{};
-                o.struct_size   = sizeof(o);
-                o.traversal     = trav;
-                o.ray_order     = order;
-                o.triangle_test = tt;
-                cand.push_back(o);
-            };
-            add(RR_CUDA_TRAVERSAL_BINARY, 0);
-            add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
-            if ((bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
-                 bi.prim_kind == kPrimTriangles) ||
-                (bi.kind == kKindScene && bi.scene_bvh4))
-                add(RR_CUDA_TRAVERSAL_BVH4, 0);
-            if (has_wide)
-            {
-                add(RR_CUDA_TRAVERSAL_WIDE, 1);
-                if (bi.kind == kKindGeom && ray_count >= (1u << 20)) add(RR_CUDA_TRAVERSAL_WIDE, 2);
-            }
-            cudaEvent_t e0, e1;
-            check(cudaEventCreate(&e0), "event");
-            check(cudaEventCreate(&e1), "event");
-            float best_ms = 1e30f;
-            RRCudaTraversalOptions best = cand[0];
-            auto try_cand = [&](const RRCudaTraversalOptions& o, float margin) {
-                Op op = trace_op(ctx, bvh, P(rays)->addr(), ray_count, nullptr, P(hits)->addr(), P(scratch)->addr(),
-                                 query, query_output, o);
-                check(op(ctx->stream), "tune warm-up");
-                check(cudaEventRecord(e0, ctx->stream), "event");
-                for (int r = 0; r < 3; ++r) check(op(ctx->stream), "tune run");
-                check(cudaEventRecord(e1, ctx->stream), "event");
-                check(cudaEventSynchronize(e1), "event");
-                float ms = 0.f;
-                check(cudaEventElapsedTime(&ms, e0, e1), "event");
-                RR_LOG_INFO("autotune %s: traversal %u order %u blocks/SM %u stack %u -> %.3f ms", key.c_str(),
-                            o.traversal, o.ray_order, o.blocks_per_sm, o.short_stack, ms / 3.f);
-                if (ms < best_ms * margin)
-                {
-                    best_ms = ms;
-                    best    = o;
-                }
-            };
-            // Stage 1: kernel and node width.  Stage 2: the winner's launch
-            // shape (resident blocks per SM, against the occupancy maximum)
-            // and, for the 4-wide kernel, its shared-stack depth; a stage-2
-            // variant must be 1 % faster to replace the default shape, so
-            // run-to-run noise does not move it.
-            for (const auto& o : cand) try_cand(o, 1.0f);
-            const RRCudaTraversalOptions w = best;
-            if (w.traversal != RR_CUDA_TRAVERSAL_BINARY)
-                for (uint32_t bps : {4u, 6u})
-                {
-                    RRCudaTraversalOptions o = w;
-                    o.blocks_per_sm          = bps;
-                    try_cand(o, 0.99f);
-                }
-            if (w.traversal == RR_CUDA_TRAVERSAL_BVH4 && bi.kind == kKindGeom)
-                for (uint32_t depth : {12u, 24u})
-                {
-                    RRCudaTraversalOptions o = w;
-                    o.short_stack            = depth;
-                    try_cand(o, 0.99f);
-                }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            ctx->tuned[key] = best;
-            if (cache_path)
-                if (FILE* f = std::fopen(cache_path, "a"))
-                {
-                    std::fprintf(f, "%s\t%u %u %u %u\n", key.c_str(), best.traversal, best.ray_order,
-                                 best.blocks_per_sm, best.short_stack);
-                    std::fclose(f);
-                }
-            hit = ctx->tuned.find(key);
-        }
-        RRCudaTraversalOptions o = hit->second;
-        o.collect_stats          = 0;
-        ctx->topts               = o;
-        if (chosen) *chosen = o;
+        ctx->topts = best_opt;
+        if (node_format) *node_format = best_fmt;
         return RR_SUCCESS;
     })
 }

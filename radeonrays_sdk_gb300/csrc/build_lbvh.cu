@@ -182,6 +182,75 @@ __device__ __forceinline__ void emit_node(const void* __restrict__ codes, uint32
     if (i == 0) nodes[0].parent = kInvalid;
 }
 
+// Compact topology of a geometry build, in its scratch: the emit writes it
+// and the refit reads it, then writes every node whole.  Children as one
+// 8-byte word per internal node, parents as one 4-byte word per node, and the
+// climb flags.  The emit's words are thus dense stores into arrays of 4 and
+// 8-byte words instead of scattered 4-byte stores into 64-byte nodes (each
+// of which made L2 fetch the node's sector before merging the word).
+struct Topo
+{
+    uint2*    child;   // n - 1
+    uint32_t* parent;  // 2n - 1
+    uint32_t* flag;    // n - 1
+};
+__host__ __device__ __forceinline__ size_t topo_align(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+__host__ __device__ __forceinline__ size_t topo_bytes(uint32_t n)
+{
+    if (n < 2) return 0;
+    return topo_align(8ull * (n - 1)) + topo_align(4ull * (2ull * n - 1)) + topo_align(4ull * (n - 1));
+}
+__device__ __forceinline__ Topo topo_of(const BuildItem& it)
+{
+    uint8_t* base = it.scratch + it.s_topo;
+    Topo     t;
+    t.child  = reinterpret_cast<uint2*>(base);
+    t.parent = reinterpret_cast<uint32_t*>(base + topo_align(8ull * (it.n - 1)));
+    t.flag   = t.parent + topo_align(4ull * (2ull * it.n - 1)) / 4;
+    return t;
+}
+
+// emit_node into the compact topology (flag cleared for the refit's climb).
+template <int kBits>
+__device__ __forceinline__ void emit_node_topo(const void* __restrict__ codes, uint32_t n, uint32_t i, const Topo& t)
+{
+    Delta<kBits> delta{codes, (int64_t)n};
+    const int64_t ii = i;
+    const int     dd   = delta(ii, ii + 1) - delta(ii, ii - 1);
+    const int64_t d    = dd > 0 ? 1 : (dd < 0 ? -1 : 0);
+    const int     dmin = delta(ii, ii - d);
+    int64_t       lmax = 2;
+    while (delta(ii, ii + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0, tt = lmax;
+    do
+    {
+        tt /= 2;
+        if (delta(ii, ii + (l + tt) * d) > dmin) l += tt;
+    } while (tt > 1);
+    const int64_t e    = ii + l * d;
+    const int64_t lo_e = ii < e ? ii : e, hi_e = ii < e ? e : ii;
+    const int64_t sx   = lo_e > 0 ? lo_e : 0;
+    const int64_t sy   = hi_e < (int64_t)n - 1 ? hi_e : (int64_t)n - 1;
+    int64_t       left = sx, right = sy;
+    const int     nid  = delta(left, right);
+    do
+    {
+        int64_t ns = (right + left) / 2;
+        if (delta(left, ns) > nid)
+            left = ns;
+        else
+            right = ns;
+    } while (right > left + 1);
+    const int64_t  s  = left;
+    const uint32_t al = (s == sx) ? (uint32_t)(n - 1 + s) : (uint32_t)s;
+    const uint32_t ar = (s + 1 == sy) ? (uint32_t)(n - 1 + s + 1) : (uint32_t)(s + 1);
+    t.child[i]   = make_uint2(al, ar);
+    t.flag[i]    = 0;
+    t.parent[al] = i;
+    t.parent[ar] = i;
+    if (i == 0) t.parent[0] = kInvalid;
+}
+
 // One sorted array (the instance tree of a scene build).
 template <int kBits>
 __global__ void __launch_bounds__(256) k_emit(const void* __restrict__ codes, uint32_t n, BvhNode* nodes)
@@ -407,7 +476,7 @@ __global__ void __launch_bounds__(kBlk) k_batch_emit(BatchArgs b)
     const BuildItem& it  = b.items[r.g];
     const uint64_t   i64 = ((uint64_t)r.tile * Cfg::kChunks + blockIdx.x % Cfg::kChunks) * kChunk + threadIdx.x;
     if (i64 + 1 >= it.n) return;
-    emit_node<kBits>(it.scratch + it.s_codes, it.n, (uint32_t)i64, reinterpret_cast<BvhNode*>(it.result));
+    emit_node_topo<kBits>(it.scratch + it.s_codes, it.n, (uint32_t)i64, topo_of(it));
 }
 
 // ---- treelet restructure (quality build) -----------------------------------
@@ -735,13 +804,19 @@ __device__ __forceinline__ void node_box(const BvhNode* nodes, uint32_t s, uint3
 // emit, unchanged by the climb) are read before the flag, so those loads
 // overlap the atomic.  The boxes are the reference's: a node's box is the
 // union of its two child boxes, slot 0 first.
+// kTopo: a build -- the topology comes from the compact arrays (topo_of)
+// and every node is written whole; otherwise an update of a built tree,
+// whose nodes hold the topology and the climb flags.
+template <bool kTopo>
 __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, uint32_t n, uint32_t k, uint32_t prim,
                                          DeviceWords* words)
 {
     const uint32_t leaf = n - 1 + k;
     F3             a, bb, c;
     tri_verts(it, prim, a, bb, c);
-    uint32_t parent = (n == 1) ? kInvalid : __ldcg(&nodes[leaf].parent);
+    Topo topo{};
+    if (kTopo && n > 1) topo = topo_of(it);
+    uint32_t parent = (n == 1) ? kInvalid : (kTopo ? __ldcg(&topo.parent[leaf]) : __ldcg(&nodes[leaf].parent));
     float4*  dst    = reinterpret_cast<float4*>(nodes + leaf);
     __stcg(dst + 0, make_float4(a.x, a.y, a.z, __uint_as_float(kInvalid)));
     __stcg(dst + 1, make_float4(bb.x, bb.y, bb.z, __uint_as_float(prim)));
@@ -759,9 +834,22 @@ __device__ __forceinline__ void fit_leaf(const BuildItem& it, BvhNode* nodes, ui
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
             return;
         }
-        BvhNode*       nd = nodes + addr;
-        const uint32_t c0 = __ldcg(&nd->child0), c1 = __ldcg(&nd->child1), up = __ldcg(&nd->parent);
-        if (climb_exch(&nd->update) == 0u) return;
+        BvhNode* nd = nodes + addr;
+        uint32_t c0, c1, up;
+        if (kTopo)
+        {
+            const uint2 ch = __ldcg(&topo.child[addr]);
+            c0             = ch.x;
+            c1             = ch.y;
+            up             = __ldcg(&topo.parent[addr]);
+        }
+        else
+        {
+            c0 = __ldcg(&nd->child0);
+            c1 = __ldcg(&nd->child1);
+            up = __ldcg(&nd->parent);
+        }
+        if (climb_exch(kTopo ? &topo.flag[addr] : &nd->update) == 0u) return;
         if (c0 >= 2 * n - 1 || c1 >= 2 * n - 1 || (c0 != x && c1 != x))
         {
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
@@ -794,7 +882,7 @@ __global__ void __launch_bounds__(kBlk) k_batch_refit(BatchArgs b, DeviceWords* 
     const uint32_t  k          = (uint32_t)k64;
     BvhNode*        nodes      = reinterpret_cast<BvhNode*>(it.result);
     const uint32_t* sorted_idx = reinterpret_cast<const uint32_t*>(it.scratch + it.s_idx);
-    fit_leaf(it, nodes, n, k, sorted_idx[k], words);
+    fit_leaf<true>(it, nodes, n, k, sorted_idx[k], words);
 }
 
 // RR_BUILD_OPERATION_UPDATE (lbvh_reset_update_flags.comp:58-80): every
@@ -814,7 +902,7 @@ __global__ void __launch_bounds__(kBlk) k_update_fit(BuildItem it, DeviceWords* 
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= it.n) return;
     BvhNode* nodes = reinterpret_cast<BvhNode*>(it.result);
-    fit_leaf(it, nodes, it.n, k, __ldcg(&nodes[it.n - 1 + k].child1), words);
+    fit_leaf<false>(it, nodes, it.n, k, __ldcg(&nodes[it.n - 1 + k].child1), words);
 }
 
 __global__ void k_put_single(BuildItem* items, BuildItem it, uint32_t* tile_prefix, uint32_t tiles)
@@ -927,7 +1015,8 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
     L.s_queue       = align_up(L.s_sort + L.s_sort_bytes, kAlign);
     L.s_queue_bytes =
         ((format == RR_CUDA_NODE_FORMAT_WIDE8 || format == RR_CUDA_NODE_FORMAT_BVH4) && n > 0) ? 2 * kAlign + 2ull * 8ull * n : 0;
-    L.s_total       = align_up(L.s_queue + L.s_queue_bytes, kAlign);
+    L.s_topo        = align_up(L.s_queue + L.s_queue_bytes, kAlign);
+    L.s_total       = align_up(L.s_topo + topo_bytes(n), kAlign);
     // An update re-collapses the wide nodes: descriptor of one + queues.
     L.u_queue = align_up(batch_desc_bytes(1), kAlign);
     L.u_total = L.s_queue_bytes ? align_up(L.u_queue + L.s_queue_bytes, kAlign) : 0;
@@ -950,6 +1039,7 @@ BuildItem make_build_item(const GeomLayout& L, const float* vertices, uint64_t s
     it.s_idx_alt     = L.s_idx_alt;
     it.s_sort        = L.s_sort;
     it.s_queue       = L.s_queue;
+    it.s_topo        = L.s_topo;
     it.trailer_off   = L.trailer_off;
     it.wide_off      = L.wide_off;
     it.tris_off      = L.tris_off;

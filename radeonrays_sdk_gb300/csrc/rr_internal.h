@@ -138,7 +138,7 @@ struct GeomLayout
     size_t   total;
     // scratch
     size_t   s_desc, s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_sort_bytes, s_queue, s_queue_bytes,
-        s_total;
+        s_topo, s_total;
     // update scratch (RR_BUILD_OPERATION_UPDATE): descriptor | collapse queues
     size_t   u_queue, u_total;
     uint32_t sort_tiles, sort_passes;
@@ -162,6 +162,7 @@ struct __align__(16) BuildItem
     uint8_t*     result;
     uint64_t     stride_floats;
     uint64_t     s_bounds, s_codes, s_codes_alt, s_idx, s_idx_alt, s_sort, s_queue;
+    uint64_t     s_topo;    // compact topology of the build (emit -> refit): children, parents, climb flags
     uint64_t     trailer_off, wide_off, tris_off;
     uint32_t     wide_capacity, tri_capacity;
     uint32_t     n;

@@ -41,7 +41,7 @@ RR_INDEX_TYPE_UINT32, RR_INDEX_TYPE_UINT16 = 0, 1
 RR_INTERSECT_QUERY_CLOSEST, RR_INTERSECT_QUERY_ANY = 0, 1
 RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID = 0, 1
 RR_LOG_LEVEL_DEBUG, RR_LOG_LEVEL_INFO, RR_LOG_LEVEL_WARN, RR_LOG_LEVEL_ERROR, RR_LOG_LEVEL_OFF = 1, 2, 3, 4, 5
-RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8, RR_CUDA_NODE_FORMAT_BVH4 = 0, 1, 2
+RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8, RR_CUDA_NODE_FORMAT_BVH4, RR_CUDA_NODE_FORMAT_AUTO = 0, 1, 2, 3
 RR_CUDA_TRAVERSAL_AUTO, RR_CUDA_TRAVERSAL_BINARY, RR_CUDA_TRAVERSAL_WIDE = 0, 1, 2
 RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, RR_CUDA_TRAVERSAL_BVH4 = 3, 4
 RR_CUDA_TRIANGLE_TEST_REFERENCE, RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 0, 1
@@ -184,6 +184,8 @@ PROTOTYPES = {
     "rrCudaGetNoAllocDeviceErrors": [_P, C.POINTER(C.c_uint32)],
     "rrCudaAutotuneTraversal": [_P, _P, C.c_int, _P, C.c_uint32, C.c_int, _P, _P,
                                 C.POINTER(RRCudaTraversalOptions)],
+    "rrCudaAutotuneNodeFormat": [_P, C.POINTER(RRGeometryBuildInput), C.POINTER(RRBuildOptions), C.c_int, _P,
+                                 C.c_uint32, C.c_int, _P, _P, C.POINTER(C.c_uint32)],
     "rrCudaCmdBuildGeometries": [_P, C.c_uint32, C.POINTER(RRGeometryBuildInput), C.POINTER(RRBuildOptions), _PP,
                                  _PP, _P],
     "rrCudaGetIntersectBatchMemoryRequirements": [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_size_t)],
@@ -573,6 +575,27 @@ class Context:
               "rrCudaAutotuneTraversal")
         return {"traversal": o.traversal, "ray_order": o.ray_order, "blocks_per_sm": o.blocks_per_sm,
                 "short_stack": o.short_stack}
+
+    def autotune_node_format(self, vertices, indices, rays, query=RR_INTERSECT_QUERY_CLOSEST,
+                             output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, quality=False) -> int:
+        """rrCudaAutotuneNodeFormat: build the mesh in the 4-wide and the 8-wide
+        format, tune the traversal of each on `rays`, remember the faster width
+        for meshes of this size (RR_CUDA_NODE_FORMAT_AUTO builds use it) and
+        return it."""
+        torch = _torch()
+        ntri = indices.numel() // 3
+        bi, mesh = self._build_input(self.ptr(vertices), vertices.numel() // 3, 12, self.ptr(indices), ntri,
+                                     indices.dtype == torch.int16)
+        opts, keep = self._options(RR_CUDA_NODE_FORMAT_AUTO, 30, quality)
+        R = rays.shape[0]
+        hits = torch.empty((R, 4) if output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT else (R,), dtype=torch.int32,
+                           device=rays.device)
+        scratch = torch.empty(self.trace_scratch_bytes(R), dtype=torch.uint8, device=rays.device)
+        fmt = C.c_uint32()
+        check(self.L.rrCudaAutotuneNodeFormat(self.ctx, C.byref(bi), C.byref(opts), query, self.ptr(rays), R, output,
+                                              self.ptr(hits), self.ptr(scratch), C.byref(fmt)),
+              "rrCudaAutotuneNodeFormat")
+        return fmt.value
 
     def set_wait_limits(self, lookback_polls=0, arrival_polls=0, hold_sort_tile=RR_INVALID,
                         drop_arrival_chunk=RR_INVALID):

@@ -85,8 +85,16 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     req_8 = rr.RRMemoryRequirements()
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts8), C.byref(req_8)) == 0
     assert req_8.result_buffer_size > req.result_buffer_size > req_b.result_buffer_size
+    # AUTO (the node-format tuner's choice) is sized for either width.
+    auto_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_AUTO, 30, 0)
+    optsa = rr.RRBuildOptions(1, C.cast(C.pointer(auto_opts), C.c_void_p))
+    req_a = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsa), C.byref(req_a)) == 0
+    assert req_a.result_buffer_size == max(req.result_buffer_size, req_8.result_buffer_size)
+    assert req_a.temporary_build_buffer_size == max(req.temporary_build_buffer_size,
+                                                    req_8.temporary_build_buffer_size)
     # An unknown node format is rejected.
-    bad_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), 3, 30, 0)
+    bad_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), 4, 30, 0)
     optsx = rr.RRBuildOptions(1, C.cast(C.pointer(bad_opts), C.c_void_p))
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsx), C.byref(req_8)) == \
         rr.RR_ERROR_INVALID_PARAMETER

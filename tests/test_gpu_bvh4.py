@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import MESH_FIXTURES, golden
-from gpu_util import INVALID, build, nodes_of, tie_only_mismatch, trace, trailer_of
+from gpu_util import INVALID, build, hits_np, nodes_of, tie_only_mismatch, to_dev, trace, trailer_of
 
 pytestmark = pytest.mark.gpu
 
@@ -165,3 +165,27 @@ def test_bvh4_stack_depth_and_launch_shape_keep_hits(ctx, orc):
             ctx.set_traversal(BVH4, short_stack=bad)
     ctx.set_traversal(0)
     assert ctx.device_errors() == 0
+
+
+def test_node_format_autotuner_and_auto_builds(ctx, orc, tmp_path, monkeypatch):
+    """rrCudaAutotuneNodeFormat builds the mesh in both wide formats, tunes the
+    traversal of each, and remembers the faster width for the mesh's size
+    class; builds with RR_CUDA_NODE_FORMAT_AUTO then use it, from the context
+    and, through RR_CUDA_TUNE_CACHE, in a fresh one."""
+    from radeonrays_sdk_gb300 import rr, scenes
+    monkeypatch.setenv("RR_CUDA_TUNE_CACHE", str(tmp_path / "tune.tsv"))
+    v, i, rays = scenes.config1(grid=257, nrays=1 << 18)
+    with rr.Context() as c:
+        fmt = c.autotune_node_format(to_dev(v), to_dev(i), to_dev(rays))
+        assert fmt in (rr.RR_CUDA_NODE_FORMAT_BVH4, rr.RR_CUDA_NODE_FORMAT_WIDE8)
+        res = c.build_geometry(to_dev(v), to_dev(i), node_format=rr.RR_CUDA_NODE_FORMAT_AUTO)
+        assert trailer_of(res, i.shape[0])["node_format"] == fmt
+        nodes, _, _ = orc.build_mesh(v, i)
+        want = orc.trace(nodes, rays, threads=16)
+        got = hits_np(c.intersect(res, to_dev(rays)))
+        assert np.array_equal(got[:, 2] != INVALID, want[:, 2] != INVALID)
+        assert c.device_errors() == 0
+    assert "fmt|" in (tmp_path / "tune.tsv").read_text()
+    with rr.Context() as c2:  # a fresh context reads the choice from the cache file
+        res2 = c2.build_geometry(to_dev(v), to_dev(i), node_format=rr.RR_CUDA_NODE_FORMAT_AUTO)
+        assert trailer_of(res2, i.shape[0])["node_format"] == fmt
