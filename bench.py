@@ -116,8 +116,9 @@ def parse():
                     help="serving: node format of the resident scenes (bvh4 runs the 4-wide multi-request kernel)")
     ap.add_argument("--slot-rays", type=int, default=1 << 22)
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0)
-    ap.add_argument("--chosen-format", default="bvh4", choices=["wide8", "bvh4"],
-                    help="node format of the chosen path's tree (the binary nodes are always there)")
+    ap.add_argument("--chosen-format", default="auto", choices=["auto", "wide8", "bvh4", "bvh4q8"],
+                    help="node format of the chosen path's tree (the binary nodes are always there); auto: the "
+                         "node-format autotuner's pick (rrCudaAutotuneNodeFormat) on the workload's rays")
     ap.add_argument("--chosen", type=int, default=0,
                     help="chosen traversal: 0 autotuned (rrCudaAutotuneTraversal), 2 wide (8-wide nodes, "
                          "--chosen-format wide8), 3 binary persistent, 4 4-wide fp32 nodes (--chosen-format bvh4)")
@@ -219,11 +220,11 @@ def describe(args, ntri):
                         "rays per GPU (origins uniform in the mesh box, directions uniform on the sphere), "
                         "closest hit, full RRHit output",
             "triangles": ntri, "rays_per_gpu": args.rays, "query": "closest", "output": "full_hit",
-            "chosen": "autotuned (rrCudaAutotuneTraversal) among the kernels the chosen tree's format allows: "
-                      "plain binary, persistent lane-refill binary (reference visit order), and persistent 4-wide "
-                      f"fp32 nodes (format bvh4) or 8-wide 8-bit nodes (format wide8), then the winner's resident "
-                      "blocks per SM and (4-wide) shared-stack depth; format here: "
-                      f"{args.chosen_format}",
+            "chosen": "autotuned: the node format (rrCudaAutotuneNodeFormat: 4-wide nodes with fp32 bounds "
+                      "(bvh4) or 8-bit bounds (bvh4q8), or 8-wide 8-bit nodes (wide8)), then the kernel "
+                      "(rrCudaAutotuneTraversal among plain binary, persistent lane-refill binary and the format's "
+                      "wide kernel), the winner's resident blocks per SM and (4-wide) shared-stack depth; format "
+                      f"here: {args.chosen_format}",
             "plain": "64-byte binary nodes, one thread per ray, reference visit order",
             "l2": "inputs larger than L2 (rays 32 B x rays, BVH > 129 MB); no flush needed",
             "parallelism": "replicas (rays sharded per GPU, BVH replicated)"}
@@ -424,7 +425,20 @@ def run_ours(args):
     # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
     # LBVH + treelet restructure); the plain path the reference's fast LBVH.
     bvh_c = bvh
-    cfmt = rr.RR_CUDA_NODE_FORMAT_BVH4 if args.chosen_format == "bvh4" else rr.RR_CUDA_NODE_FORMAT_WIDE8
+    format_tuned = None
+    if args.chosen_format == "auto":
+        # The node-format autotuner: builds the chosen tree in each wide
+        # format, tunes the traversal of each on the workload's rays (untimed)
+        # and keeps the fastest.
+        rays_tune = torch.from_numpy(rays).cuda()
+        cfmt = ctx.autotune_node_format(v_d, i_d, rays_tune, quality=bool(args.quality))
+        format_tuned = {rr.RR_CUDA_NODE_FORMAT_BVH4: "bvh4", rr.RR_CUDA_NODE_FORMAT_BVH4Q8: "bvh4q8",
+                        rr.RR_CUDA_NODE_FORMAT_WIDE8: "wide8"}[cfmt]
+        del rays_tune
+        torch.cuda.empty_cache()
+    else:
+        cfmt = {"bvh4": rr.RR_CUDA_NODE_FORMAT_BVH4, "bvh4q8": rr.RR_CUDA_NODE_FORMAT_BVH4Q8,
+                "wide8": rr.RR_CUDA_NODE_FORMAT_WIDE8}[args.chosen_format]
     if args.quality or cfmt != rr.RR_CUDA_NODE_FORMAT_BVH4:
         cs_bytes, cr_bytes = ctx.geometry_requirements(ntri, cfmt, 30, v.shape[0], 12)
         bvh_c = torch.empty(cr_bytes, dtype=torch.uint8, device="cuda")
@@ -478,7 +492,10 @@ def run_ours(args):
         ctx.set_traversal(trav, *shape, ray_order=order, short_stack=depth)
         # Bytes per fetch: binary node 64; 8-wide node 80 (+ 48-byte triangles);
         # 4-wide node 128 (+ the 48 bytes of a binary leaf's three vertices).
-        node_b = {rr.RR_CUDA_TRAVERSAL_WIDE: 80, rr.RR_CUDA_TRAVERSAL_BVH4: 128}.get(trav, 64)
+        node_b = {rr.RR_CUDA_TRAVERSAL_WIDE: 80,
+                  rr.RR_CUDA_TRAVERSAL_BVH4: 64 if cfmt == rr.RR_CUDA_NODE_FORMAT_BVH4Q8 else 128}.get(trav, 64)
+        if name == "plain":
+            node_b = 64
         alg = R * (32 + 16) + st["node_fetches"] * node_b + st["triangle_fetches"] * 48
         clocks = Clocks(local)
         with clocks:
@@ -627,9 +644,11 @@ def run_ours(args):
     achieved = c["alg_bytes"] / mean_launch_s / 1e9
     traffic = None
     kernel = KERNELS.get(c["trav"], "k_trace_binary")
+    traffic_key = kernel + ("_q8" if key == "chosen" and c["trav"] == rr.RR_CUDA_TRAVERSAL_BVH4 and
+                            cfmt == rr.RR_CUDA_NODE_FORMAT_BVH4Q8 else "")
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        t = json.loads(tf.read_text()).get(kernel)
+        t = json.loads(tf.read_text()).get(traffic_key)
         if t and t.get("dram_bytes_per_ray"):
             traffic = t["dram_bytes_per_ray"] * R
     line = {
@@ -646,6 +665,8 @@ def run_ours(args):
                      "node_fetches_per_ray": c["stats"]["node_fetches"] / R,
                      "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R},
         "clocks": c["clocks"], "gpu_launches": args.steps, "build": build, "traversal": key,
+        "chosen_format": {"format": format_tuned or args.chosen_format,
+                          "selected_by": "rrCudaAutotuneNodeFormat" if format_tuned else "command line"},
         "chosen_kernel": {"kernel": kernel, "traversal": c["trav"], "ray_order": c["order"],
                           "blocks_per_sm": chosen_per_sm or "occupancy maximum",
                           "short_stack": chosen_stack or 16,

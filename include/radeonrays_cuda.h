@@ -35,9 +35,16 @@ typedef enum
     /* The node width rrCudaAutotuneNodeFormat picked for meshes of the same
      * size class (triangle-count octave) on this GPU, from this context or
      * the RR_CUDA_TUNE_CACHE file; BVH4 when none was picked.  Memory
-     * requirements with AUTO are sized for either width.  A fused build
+     * requirements with AUTO are sized for any of the wide formats.  A fused build
      * (rrCudaCmdBuildGeometries) takes its largest mesh's width. */
-    RR_CUDA_NODE_FORMAT_AUTO = 3
+    RR_CUDA_NODE_FORMAT_AUTO = 3,
+    /* Binary nodes plus 4-wide 64-byte nodes whose child bounds are 8-bit
+     * offsets from a per-node fp32 origin in per-axis power-of-two steps,
+     * rounded outward, so every quantised box contains the exact one; leaf
+     * children are the binary leaf nodes, and the traversal re-tests each
+     * leaf triangle's exact box with the reference's slab arithmetic before
+     * its triangle test.  Half the bytes of a BVH4 node per fetch. */
+    RR_CUDA_NODE_FORMAT_BVH4Q8 = 4
 } RRCudaNodeFormat;
 
 /* Passed through RRBuildOptions::backend_specific_info.  A null
@@ -67,8 +74,9 @@ typedef enum
     /* Persistent warp-scheduled kernel over the binary nodes, reference visit
      * order (hits bit-identical to RR_CUDA_TRAVERSAL_BINARY). */
     RR_CUDA_TRAVERSAL_BINARY_PERSISTENT = 3,
-    /* Persistent warp-scheduled kernel over the 4-wide fp32 nodes of an
-     * RR_CUDA_NODE_FORMAT_BVH4 buffer, nearest child first. */
+    /* Persistent warp-scheduled kernel over the 4-wide nodes of an
+     * RR_CUDA_NODE_FORMAT_BVH4 (fp32 boxes) or RR_CUDA_NODE_FORMAT_BVH4Q8
+     * (8-bit boxes) buffer, nearest child first. */
     RR_CUDA_TRAVERSAL_BVH4 = 4
 } RRCudaTraversal;
 
@@ -88,7 +96,8 @@ typedef enum
      * ray touches.  Supported by RR_CUDA_TRAVERSAL_AUTO,
      * RR_CUDA_TRAVERSAL_BINARY_PERSISTENT and RR_CUDA_TRAVERSAL_BVH4 on
      * triangle geometries (not on scene buffers, AABB lists or the
-     * multi-request launch). */
+     * multi-request launch); on an RR_CUDA_NODE_FORMAT_BVH4Q8 buffer it runs
+     * the persistent binary kernel. */
     RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 1
 } RRCudaTriangleTest;
 
@@ -218,10 +227,11 @@ RR_API RRError rrCudaAutotuneTraversal(RRContext               context,
                                        RRDevicePtr             scratch,
                                        RRCudaTraversalOptions* chosen);
 
-/* Pick the node width for a mesh and a ray workload (no reference
+/* Pick the node format for a mesh and a ray workload (no reference
  * counterpart: the reference has one binary node format).  Builds the mesh
  * (build_input, with build_options' quality flag) into temporary buffers in
- * the 4-wide (BVH4) and the 8-wide quantised (WIDE8) formats -- the only
+ * the 4-wide fp32 (BVH4), 4-wide 8-bit (BVH4Q8) and 8-wide 8-bit (WIDE8)
+ * formats -- the only
  * call of this library that allocates device memory for itself -- runs the
  * traversal autotuner on each with the caller's rays (timed afresh), and
  * keeps the faster.  The choice is remembered for the mesh's size class

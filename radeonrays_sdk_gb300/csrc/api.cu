@@ -401,7 +401,8 @@ bool parse_build_options(const RRBuildOptions* o, BuildParams& bp)
     const RRCudaBuildOptions* c = reinterpret_cast<const RRCudaBuildOptions*>(o->backend_specific_info);
     if (c->struct_size < sizeof(RRCudaBuildOptions)) return false;
     if (c->node_format != RR_CUDA_NODE_FORMAT_BINARY && c->node_format != RR_CUDA_NODE_FORMAT_WIDE8 &&
-        c->node_format != RR_CUDA_NODE_FORMAT_BVH4 && c->node_format != RR_CUDA_NODE_FORMAT_AUTO)
+        c->node_format != RR_CUDA_NODE_FORMAT_BVH4 && c->node_format != RR_CUDA_NODE_FORMAT_AUTO &&
+        c->node_format != RR_CUDA_NODE_FORMAT_BVH4Q8)
         return false;
     if (c->morton_bits != 0 && c->morton_bits != 30 && c->morton_bits != 63) return false;
     bp.format = c->node_format;
@@ -488,7 +489,7 @@ uint32_t resolve_format(Context* ctx, uint32_t requested, uint32_t n)
                     if (!tab) continue;
                     *tab = 0;
                     if (key == line && std::sscanf(tab + 1, "%u", &v) == 1 &&
-                        (v == RR_CUDA_NODE_FORMAT_BVH4 || v == RR_CUDA_NODE_FORMAT_WIDE8))
+                        (is_bvh4_format(v) || v == RR_CUDA_NODE_FORMAT_WIDE8))
                         fmt = v;
                 }
                 std::fclose(f);
@@ -758,9 +759,15 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     // default format; the fastest kernel on incoherent rays), else the
     // persistent binary kernel (bit-identical to BINARY);
     // rrCudaAutotuneTraversal refines the choice per workload.
-    const bool has_bvh4 = bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
-                          bi.prim_kind == kPrimTriangles;
-    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || (trav == RR_CUDA_TRAVERSAL_AUTO && !has_bvh4))
+    // The precise test runs over fp32 4-wide nodes only: a quantised buffer
+    // then takes the persistent binary kernel.
+    const bool precise  = o.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT;
+    const bool has_bvh4 = bi.kind == kKindGeom && is_bvh4_format(bi.format) && bi.n > 0 &&
+                          bi.prim_kind == kPrimTriangles &&
+                          !(precise && bi.format == RR_CUDA_NODE_FORMAT_BVH4Q8);
+    const bool q8_precise = precise && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4Q8 && bi.n > 0;
+    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || (trav == RR_CUDA_TRAVERSAL_AUTO && !has_bvh4) ||
+        (trav == RR_CUDA_TRAVERSAL_BVH4 && q8_precise))
     {
         if (sp)
         {
@@ -777,6 +784,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     if ((trav == RR_CUDA_TRAVERSAL_BVH4 || trav == RR_CUDA_TRAVERSAL_AUTO) && has_bvh4)
     {
         a.bvh4_nodes = reinterpret_cast<const Bvh4Node*>(bvh + bi.wide_off);
+        a.bvh4_q8    = bi.format == RR_CUDA_NODE_FORMAT_BVH4Q8 ? 1 : 0;
         a.wide_limit = (uint32_t)bi.wide_capacity;
         if (sp)
         {
@@ -953,7 +961,7 @@ RRError autotune_traversal(Context* ctx, uint8_t* bvh, RRIntersectQuery query, u
             };
             add(RR_CUDA_TRAVERSAL_BINARY, 0);
             add(RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, 0);
-            if ((bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4 && bi.n > 0 &&
+            if ((bi.kind == kKindGeom && is_bvh4_format(bi.format) && bi.n > 0 &&
                  bi.prim_kind == kPrimTriangles) ||
                 (bi.kind == kKindScene && bi.scene_bvh4))
                 add(RR_CUDA_TRAVERSAL_BVH4, 0);
@@ -1113,9 +1121,10 @@ RR_API RRError rrGetGeometryBuildMemoryRequirements(RRContext                   
             // Sized for either node width the tuner may pick.
             const GeomLayout a = geom_layout(ma.n, build_format(ma, RR_CUDA_NODE_FORMAT_BVH4), bp.bits);
             const GeomLayout b = geom_layout(ma.n, build_format(ma, RR_CUDA_NODE_FORMAT_WIDE8), bp.bits);
-            memory_requirements->result_buffer_size           = std::max(a.total, b.total);
-            memory_requirements->temporary_build_buffer_size  = std::max(a.s_total, b.s_total);
-            memory_requirements->temporary_update_buffer_size = std::max(a.u_total, b.u_total);
+            const GeomLayout c = geom_layout(ma.n, build_format(ma, RR_CUDA_NODE_FORMAT_BVH4Q8), bp.bits);
+            memory_requirements->result_buffer_size           = std::max({a.total, b.total, c.total});
+            memory_requirements->temporary_build_buffer_size  = std::max({a.s_total, b.s_total, c.s_total});
+            memory_requirements->temporary_update_buffer_size = std::max({a.u_total, b.u_total, c.u_total});
             return RR_SUCCESS;
         }
         GeomLayout L                                      = geom_layout(ma.n, build_format(ma, bp.format), bp.bits);
@@ -1204,7 +1213,7 @@ RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_bu
             t.node_count != (n == 0 ? 0u : 2u * n - 1u))
             return RR_ERROR_INVALID_PARAMETER;
         if (t.node_format != RR_CUDA_NODE_FORMAT_BINARY && t.node_format != RR_CUDA_NODE_FORMAT_WIDE8 &&
-            t.node_format != RR_CUDA_NODE_FORMAT_BVH4)
+            !is_bvh4_format(t.node_format))
             return RR_ERROR_INVALID_PARAMETER;
         const GeomLayout L = geom_layout(n, t.node_format, t.morton_bits);
         if (t.wide_nodes_off != L.wide_off || t.wide_tris_off != L.tris_off) return RR_ERROR_INVALID_PARAMETER;
@@ -2064,7 +2073,8 @@ RR_API RRError rrCudaAutotuneNodeFormat(RRContext                   context,
         // Each width: a temporary build on the context's stream (the tuner
         // allocates; a build call never does), then the traversal tuner on
         // the caller's rays, timed afresh.
-        for (uint32_t fmt : {(uint32_t)RR_CUDA_NODE_FORMAT_BVH4, (uint32_t)RR_CUDA_NODE_FORMAT_WIDE8})
+        for (uint32_t fmt : {(uint32_t)RR_CUDA_NODE_FORMAT_BVH4, (uint32_t)RR_CUDA_NODE_FORMAT_BVH4Q8,
+                             (uint32_t)RR_CUDA_NODE_FORMAT_WIDE8})
         {
             PendingGeom pg;
             pg.ma                    = ma;

@@ -945,8 +945,7 @@ cudaError_t run_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cuda
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    if (b.format == RR_CUDA_NODE_FORMAT_WIDE8 || b.format == RR_CUDA_NODE_FORMAT_BVH4)
-        return launch_collapse_batch(b, words, sm_count, s);
+    if (has_wide_collapse(b.format)) return launch_collapse_batch(b, words, sm_count, s);
     return cudaSuccess;
 }
 
@@ -989,7 +988,7 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
         L.tri_capacity  = n;
         off             = L.tris_off + L.tri_capacity * sizeof(WideTri);
     }
-    else if (format == RR_CUDA_NODE_FORMAT_BVH4 && n > 0)
+    else if (is_bvh4_format(format) && n > 0)
     {
         // Only a node whose children are all leaves has fewer than 4
         // children, so with F full nodes and B such nodes 3F + B <= n - 1 and
@@ -998,7 +997,8 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
         L.wide_capacity = ((size_t)n - 1) / 3 + (size_t)n / 3 + 1;
         L.tris_off      = 0;
         L.tri_capacity  = 0;
-        off             = L.wide_off + L.wide_capacity * sizeof(Bvh4Node);
+        off             = L.wide_off + L.wide_capacity *
+                                       (format == RR_CUDA_NODE_FORMAT_BVH4Q8 ? sizeof(Bvh4QNode) : sizeof(Bvh4Node));
     }
     L.total = align_up(off, kAlign);
     // Scratch: batch descriptor of one | bounds | codes | codes_alt | idx |
@@ -1014,7 +1014,7 @@ GeomLayout geom_layout(uint32_t n, uint32_t format, uint32_t morton_bits)
     L.s_sort_bytes  = radix_sort_scratch_bytes(n, (int)L.morton_bits, &L.sort_tiles, &L.sort_passes);
     L.s_queue       = align_up(L.s_sort + L.s_sort_bytes, kAlign);
     L.s_queue_bytes =
-        ((format == RR_CUDA_NODE_FORMAT_WIDE8 || format == RR_CUDA_NODE_FORMAT_BVH4) && n > 0) ? 2 * kAlign + 2ull * 8ull * n : 0;
+        (has_wide_collapse(format) && n > 0) ? 2 * kAlign + 2ull * 8ull * n : 0;
     L.s_topo        = align_up(L.s_queue + L.s_queue_bytes, kAlign);
     L.s_total       = align_up(L.s_topo + topo_bytes(n), kAlign);
     // An update re-collapses the wide nodes: descriptor of one + queues.
@@ -1080,7 +1080,7 @@ cudaError_t launch_update_mesh(const MeshArgs& m, const GeomLayout& L, uint8_t* 
     k_update_reset<<<grid_for(2ull * L.n - 1, kBlk), kBlk, 0, s>>>(reinterpret_cast<BvhNode*>(result), 2 * L.n - 1);
     k_update_fit<<<grid_for(L.n, kBlk), kBlk, 0, s>>>(it, words);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || (L.format != RR_CUDA_NODE_FORMAT_WIDE8 && L.format != RR_CUDA_NODE_FORMAT_BVH4)) return e;
+    if (e != cudaSuccess || !has_wide_collapse(L.format)) return e;
     BuildItem* items = nullptr;
     uint32_t * tp = nullptr, *lp = nullptr;
     BatchCtl*  ctl = nullptr;

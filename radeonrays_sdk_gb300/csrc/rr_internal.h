@@ -86,6 +86,33 @@ struct __align__(16) Bvh4Node
 static_assert(sizeof(Bvh4Node) == 128, "4-wide node layout");
 constexpr uint32_t kBvh4Leaf = 0x80000000u;
 
+// 4-wide node with 8-bit conservative child bounds (64 bytes, four 16-byte
+// words): per-node origin p and per-axis scale 2^(e - 127); child box of
+// slot k on axis a = [p + q[a][k] * s, p + q[3 + a][k] * s], rounded
+// outward at build time so that it contains the exact child box.  The child
+// references are those of Bvh4Node.
+struct __align__(16) Bvh4QNode
+{
+    float    p[3];
+    uint8_t  e[3];
+    uint8_t  pad0;
+    uint32_t child[4];
+    uint8_t  q[6][4];   // planes lo x, y, z, hi x, y, z; [plane][slot]
+    uint32_t pad1[2];
+};
+static_assert(sizeof(Bvh4QNode) == 64, "quantised 4-wide node layout");
+
+// Formats whose buffer carries 4-wide nodes (fp32 or 8-bit bounds).
+inline __host__ __device__ bool is_bvh4_format(uint32_t f)
+{
+    return f == RR_CUDA_NODE_FORMAT_BVH4 || f == RR_CUDA_NODE_FORMAT_BVH4Q8;
+}
+// Formats with a wide collapse after the binary build.
+inline __host__ __device__ bool has_wide_collapse(uint32_t f)
+{
+    return f == RR_CUDA_NODE_FORMAT_WIDE8 || is_bvh4_format(f);
+}
+
 // Trailer written after the binary node array of every result buffer; it
 // makes the buffer self-describing (kind, counts, section offsets).
 struct __align__(16) Trailer
@@ -286,7 +313,8 @@ struct TraceArgs
     const uint8_t*  bvh;          // result buffer base (binary nodes at offset 0)
     const WideNode* wide_nodes;   // wide path
     const WideTri*  wide_tris;
-    const Bvh4Node* bvh4_nodes;   // 4-wide path
+    const Bvh4Node* bvh4_nodes;   // 4-wide path (Bvh4QNode when bvh4_q8)
+    int             bvh4_q8;      // the 4-wide nodes have 8-bit bounds
     const uint8_t*  rays;         // RRRay[]
     uint32_t        ray_count;
     const uint32_t* indirect;     // optional device count

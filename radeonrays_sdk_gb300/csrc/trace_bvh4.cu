@@ -31,7 +31,7 @@ using namespace stream_detail;
 // kernel's streamed variant.
 // The short stack is dynamic shared memory of kPBlock x depth entries; the
 // depth (12..32, default kPShort) is a launch parameter the autotuner picks.
-template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise>
+template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise, bool kQ8>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t gcap, int depth)
 {
     extern __shared__ uint32_t s_stack[];
@@ -159,7 +159,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
         if (active &&
-            b4_step<kAny, kPrecise>(s, wn, nodes, a.wide_limit, first_leaf, a.node_limit, st, a.words, nf, tf))
+            b4_step<kAny, kPrecise, false, kQ8>(s, wn, nodes, a.wide_limit, first_leaf, a.node_limit, st, a.words, nf,
+                                                tf))
         {
             active  = false;
             pending = true;
@@ -172,10 +173,10 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_bvh4(TraceArgs a, uint32_t
     }
 }
 
-template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise>
+template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise, bool kQ8 = false>
 cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 {
-    auto         kern   = k_trace_bvh4<kAny, kFull, kStats, kStream, kPrecise>;
+    auto         kern   = k_trace_bvh4<kAny, kFull, kStats, kStream, kPrecise, kQ8>;
     const int    depth  = a.short_stack > 0 ? a.short_stack : kPShort;
     const size_t smem   = (size_t)kPBlock * depth * sizeof(uint32_t);
     int          per_sm = a.blocks_per_sm;
@@ -194,6 +195,9 @@ cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 template <bool kAny, bool kFull, bool kStats, bool kStream>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
+    // The precise test runs over fp32 4-wide nodes only (the host routes a
+    // quantised buffer to the persistent binary kernel in that mode).
+    if (a.bvh4_q8) return go2<kAny, kFull, kStats, kStream, false, true>(a, s);
     if (a.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return go2<kAny, kFull, kStats, kStream, true>(a, s);
     return go2<kAny, kFull, kStats, kStream, false>(a, s);
 }

@@ -135,6 +135,72 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
     return h;
 }
 
+// The same test on a quantised node (Bvh4QNode, four 16-byte loads instead of
+// seven): each child plane decodes exactly to 2^23 + q (byte permute, no
+// conversion) and is evaluated as fma(2^23 + q, A, B -+ eps) with
+// A = 2^e * inv (exact) and B = fma(p, inv, oxi) - 2^23 A, on the near (-)
+// and far (+) planes picked by the direction's signs.  eps = 1.25 |A| +
+// 2^-20 |B| bounds the roundings of B and of B -+ eps, so the near distance
+// is never above the reference's on the exact child box and the far distance
+// never below it (the same margin as the 8-wide kernel): a child the
+// reference's slab test admits on its exact box is always admitted.
+__device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct)
+{
+    const uint4* p  = reinterpret_cast<const uint4*>(node);
+    const uint4  w0 = __ldg(p), cr = __ldg(p + 1), q0 = __ldg(p + 2), q1 = __ldg(p + 3);
+    // Planes: q0 = lo x, lo y, lo z, hi x; q1 = hi y, hi z.
+    const bool     sx = inv.x < 0.f, sy = inv.y < 0.f, sz = inv.z < 0.f;
+    const uint32_t nxw = sx ? q0.w : q0.x, fxw = sx ? q0.x : q0.w;
+    const uint32_t nyw = sy ? q1.x : q0.y, fyw = sy ? q0.y : q1.x;
+    const uint32_t nzw = sz ? q1.y : q0.z, fzw = sz ? q0.z : q1.y;
+    float          A[3], Bn[3], Bf[3];
+    {
+        const float p3[3] = {__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z)};
+        const float i3[3] = {inv.x, inv.y, inv.z}, o3[3] = {oxi.x, oxi.y, oxi.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const float sc  = __uint_as_float(((w0.w >> (8 * k)) & 0xffu) << 23);
+            const float a   = sc * i3[k];
+            const float b   = fmaf(p3[k], i3[k], o3[k]);
+            const float eps = fmaf(fabsf(a), 1.25f, fabsf(b) * 9.5367431640625e-07f);
+            const float m   = fmaf(-8388608.0f, a, b);
+            A[k]            = a;
+            Bn[k]           = m - eps;
+            Bf[k]           = m + eps;
+        }
+    }
+#define RR_B4Q(w, c) __int_as_float((int)__byte_perm((w), 0x4B000000u, 0x7540u | (c)))
+    auto key = [&](int c, uint32_t r) {
+        const float t0 = fmaxf(b4_max3(fmaf(RR_B4Q(nxw, c), A[0], Bn[0]), fmaf(RR_B4Q(nyw, c), A[1], Bn[1]),
+                                       fmaf(RR_B4Q(nzw, c), A[2], Bn[2])),
+                               tmin);
+        const float t1 = fminf(b4_min3(fmaf(RR_B4Q(fxw, c), A[0], Bf[0]), fmaf(RR_B4Q(fyw, c), A[1], Bf[1]),
+                                       fmaf(RR_B4Q(fzw, c), A[2], Bf[2])),
+                               ct);
+        return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
+    };
+#undef RR_B4Q
+    float  k0 = key(0, cr.x), k1 = key(1, cr.y), k2 = key(2, cr.z), k3 = key(3, cr.w);
+    B4Hits h;
+    h.r0 = cr.x;
+    h.r1 = cr.y;
+    h.r2 = cr.z;
+    h.r3 = cr.w;
+    h.n  = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
+    if (h.n > 1)
+    {
+        b4_cas(k0, h.r0, k1, h.r1);
+        b4_cas(k2, h.r2, k3, h.r3);
+        b4_cas(k0, h.r0, k2, h.r2);
+        b4_cas(k1, h.r1, k3, h.r3);
+        b4_cas(k1, h.r1, k2, h.r2);
+    }
+    else if (h.n == 1)
+        h.r0 = k0 < INFINITY ? h.r0 : (k1 < INFINITY ? h.r1 : (k2 < INFINITY ? h.r2 : h.r3));
+    return h;
+}
+
 // Pushes the hit children after the nearest (farthest first) and returns the
 // nearest; the caller has h.n >= 1.
 __device__ __forceinline__ uint32_t b4_descend(const B4Hits& h, int& sp, uint32_t& gsp, const PStack& st,
@@ -180,7 +246,12 @@ __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
 // One step; returns true when the ray is finished (stack empty, or a hit
 // accepted by an any-hit query).  nf / tf count node and leaf fetches.
 // kRuntime: the query is `any` (requests of both kinds in one launch).
-template <bool kAny, bool kPrecise, bool kRuntime = false>
+// kQ8: the nodes are Bvh4QNode (quantised bounds); each leaf triangle is then
+// first tested on its exact box (min / max of its vertices, the box its
+// binary parent holds) with the reference's slab arithmetic, so a triangle
+// whose exact box the reference culls is not reached through the larger
+// quantised box either.
+template <bool kAny, bool kPrecise, bool kRuntime = false, bool kQ8 = false>
 __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ wn, const BvhNode* __restrict__ nodes,
                                         uint32_t wlim, uint32_t first_leaf, uint32_t node_limit, const PStack& st,
                                         DeviceWords* words, uint32_t& nf, uint32_t& tf, bool any = false)
@@ -200,8 +271,19 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
         const float4* p = reinterpret_cast<const float4*>(nodes + idx);
         const float4  a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
         ++tf;
-        const F3    v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
-        const float t  = kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct) : isect_tri(s.ray, v0, v1, v2, s.ct);
+        const F3 v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
+        bool     reach = true;
+        if (kQ8)
+        {
+            float b0, b1;
+            isect_box(f3(b4_min3(v0.x, v1.x, v2.x), b4_min3(v0.y, v1.y, v2.y), b4_min3(v0.z, v1.z, v2.z)),
+                      f3(b4_max3(v0.x, v1.x, v2.x), b4_max3(v0.y, v1.y, v2.y), b4_max3(v0.z, v1.z, v2.z)), s.inv,
+                      s.oxi, s.ct, s.ray.tmin, b0, b1);
+            reach = b0 <= b1;
+        }
+        const float t = !reach   ? s.ct
+                        : kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct)
+                                   : isect_tri(s.ray, v0, v1, v2, s.ct);
         if (t < s.ct)
         {
             s.ct   = t;
@@ -211,7 +293,9 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        const B4Hits h = b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
+        const B4Hits h = kQ8 ? b4q_children(reinterpret_cast<const Bvh4QNode*>(wn) + idx, s.inv, s.oxi, s.ray.tmin,
+                                            s.ct)
+                             : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
         if (h.n)
         {

@@ -180,6 +180,27 @@ __global__ void k_collapse_init(BatchArgs b)
     WideNode*      wn    = reinterpret_cast<WideNode*>(it.result + it.wide_off);
     WideTri*       wt    = reinterpret_cast<WideTri*>(it.result + it.tris_off);
     for (int i = 0; i < kMaxLevels + 2; ++i) ctl->level_count[i] = 0;
+    if (n == 1 && b.format == RR_CUDA_NODE_FORMAT_BVH4Q8)
+    {
+        // A one-triangle mesh: one quantised 4-wide node whose only child is
+        // the leaf (slot 0 spans the node's whole quantisation frame).
+        const Bx  bx = node_union(nodes[0]);
+        Bvh4QNode o{};
+        for (int a = 0; a < 3; ++a)
+        {
+            o.p[a]         = bx.lo[a];
+            const int   e  = pick_exp(bx.lo[a], bx.hi[a]);
+            const float iv = __uint_as_float((uint32_t)(254 - e) << 23);
+            o.e[a]         = (uint8_t)e;
+            o.q[a][0]      = 0;
+            o.q[3 + a][0]  = (uint8_t)fminf(255.f, ceilf(__fmul_ru(__fsub_ru(bx.hi[a], bx.lo[a]), iv)));
+        }
+        for (int k = 0; k < 4; ++k) o.child[k] = k == 0 ? kBvh4Leaf : kInvalid;
+        reinterpret_cast<Bvh4QNode*>(it.result + it.wide_off)[0] = o;
+        ctl->wide_count = 1;
+        ctl->tri_count  = 0;
+        return;
+    }
     if (n == 1 && b.format == RR_CUDA_NODE_FORMAT_BVH4)
     {
         // A one-triangle mesh: one 4-wide node whose only child is the leaf.
@@ -276,7 +297,8 @@ __global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int leve
 // One level of the collapse for every geometry: work item `it` of the level
 // belongs to the geometry found in the level prefix (a batch of one reads
 // its count directly).
-template <int W>
+// kQ8 (W == 4): the 4-wide nodes store 8-bit conservative bounds (Bvh4QNode).
+template <int W, bool kQ8 = false>
 __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, DeviceWords* words)
 {
     const uint32_t total = b.count == 1 ? *((volatile uint32_t*)&ctl_of(b.items[0])->level_count[level])
@@ -362,6 +384,54 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
         if (child_base + n_int > wide_capacity || tri_base + n_leaf > tri_capacity)
         {
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            continue;
+        }
+        if (W == 4 && kQ8)
+        {
+            // Quantised 4-wide node: the frame of the union of the child
+            // boxes, bounds rounded outward as for the 8-wide node (below),
+            // children numbered as in the fp32 4-wide node.
+            Bvh4QNode o;
+            Bx        u = cb[0];
+            for (int k = 1; k < nc; ++k)
+                for (int a = 0; a < 3; ++a)
+                {
+                    u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+                    u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+                }
+            float iv[3];
+            for (int a = 0; a < 3; ++a)
+            {
+                o.p[a]  = u.lo[a];
+                int e   = pick_exp(u.lo[a], u.hi[a]);
+                o.e[a]  = (uint8_t)e;
+                iv[a]   = __uint_as_float((uint32_t)(254 - e) << 23);
+            }
+            o.pad0    = 0;
+            o.pad1[0] = o.pad1[1] = 0;
+            uint32_t ri = 0;
+            for (int k = 0; k < 4; ++k)
+            {
+                const bool used = k < nc;
+                for (int a = 0; a < 3; ++a)
+                {
+                    const float ql = used ? floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], o.p[a]), iv[a])) : 0.f;
+                    const float qh = used ? ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], o.p[a]), iv[a])) : 0.f;
+                    o.q[a][k]     = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
+                    o.q[3 + a][k] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
+                }
+                if (!used)
+                    o.child[k] = kInvalid;
+                else if (cint[k])
+                {
+                    o.child[k]      = child_base + ri;
+                    qout[qpos + ri] = Item{ch[k], child_base + ri};
+                    ++ri;
+                }
+                else
+                    o.child[k] = kBvh4Leaf | ch[k];
+            }
+            reinterpret_cast<Bvh4QNode*>(bi->result + bi->wide_off)[item.w] = o;
             continue;
         }
         if (W == 4)
@@ -543,9 +613,11 @@ cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm
                 1, std::min<uint64_t>((cap + 127) / 128, (uint64_t)sm_count * 16));
             if (b.format == RR_CUDA_NODE_FORMAT_BVH4)
                 k_collapse_level<4><<<blocks, 128, 0, s>>>(b, level, words);
+            else if (b.format == RR_CUDA_NODE_FORMAT_BVH4Q8)
+                k_collapse_level<4, true><<<blocks, 128, 0, s>>>(b, level, words);
             else
                 k_collapse_level<8><<<blocks, 128, 0, s>>>(b, level, words);
-            bound = std::min<uint64_t>(bound * (b.format == RR_CUDA_NODE_FORMAT_BVH4 ? 4 : 8), b.total_prims);
+            bound = std::min<uint64_t>(bound * (is_bvh4_format(b.format) ? 4 : 8), b.total_prims);
         }
     }
     k_collapse_finish<<<per_geom, 128, 0, s>>>(b, words);

@@ -42,6 +42,7 @@ RR_INTERSECT_QUERY_CLOSEST, RR_INTERSECT_QUERY_ANY = 0, 1
 RR_INTERSECT_QUERY_OUTPUT_FULL_HIT, RR_INTERSECT_QUERY_OUTPUT_INSTANCE_ID = 0, 1
 RR_LOG_LEVEL_DEBUG, RR_LOG_LEVEL_INFO, RR_LOG_LEVEL_WARN, RR_LOG_LEVEL_ERROR, RR_LOG_LEVEL_OFF = 1, 2, 3, 4, 5
 RR_CUDA_NODE_FORMAT_BINARY, RR_CUDA_NODE_FORMAT_WIDE8, RR_CUDA_NODE_FORMAT_BVH4, RR_CUDA_NODE_FORMAT_AUTO = 0, 1, 2, 3
+RR_CUDA_NODE_FORMAT_BVH4Q8 = 4
 RR_CUDA_TRAVERSAL_AUTO, RR_CUDA_TRAVERSAL_BINARY, RR_CUDA_TRAVERSAL_WIDE = 0, 1, 2
 RR_CUDA_TRAVERSAL_BINARY_PERSISTENT, RR_CUDA_TRAVERSAL_BVH4 = 3, 4
 RR_CUDA_TRIANGLE_TEST_REFERENCE, RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 0, 1

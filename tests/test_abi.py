@@ -90,11 +90,19 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     optsa = rr.RRBuildOptions(1, C.cast(C.pointer(auto_opts), C.c_void_p))
     req_a = rr.RRMemoryRequirements()
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsa), C.byref(req_a)) == 0
-    assert req_a.result_buffer_size == max(req.result_buffer_size, req_8.result_buffer_size)
+    q8_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_BVH4Q8, 30, 0)
+    optsq = rr.RRBuildOptions(1, C.cast(C.pointer(q8_opts), C.c_void_p))
+    req_q = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsq), C.byref(req_q)) == 0
+    cap4 = (1000 - 1) // 3 + 1000 // 3 + 1  # 64-byte quantised 4-wide nodes
+    assert req_q.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 64 + 255) // 256 * 256
+    assert req_a.result_buffer_size == max(req.result_buffer_size, req_8.result_buffer_size,
+                                           req_q.result_buffer_size)
     assert req_a.temporary_build_buffer_size == max(req.temporary_build_buffer_size,
-                                                    req_8.temporary_build_buffer_size)
+                                                    req_8.temporary_build_buffer_size,
+                                                    req_q.temporary_build_buffer_size)
     # An unknown node format is rejected.
-    bad_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), 4, 30, 0)
+    bad_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), 5, 30, 0)
     optsx = rr.RRBuildOptions(1, C.cast(C.pointer(bad_opts), C.c_void_p))
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsx), C.byref(req_8)) == \
         rr.RR_ERROR_INVALID_PARAMETER
