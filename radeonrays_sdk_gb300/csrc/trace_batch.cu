@@ -220,7 +220,11 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch_bvh4(BatchTraceArgs 
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        if (active &&
+        // Leaf batching, as in the single-request 4-wide kernel: leaf steps
+        // wait for a quarter of the active lanes.
+        const bool at_leaf = active && (s.ref & kBvh4Leaf) != 0;
+        const bool do_leaf = 4 * __popc(__ballot_sync(0xffffffffu, at_leaf)) >= __popc(amask);
+        if (active && at_leaf == do_leaf &&
             b4_step<false, false, true>(s, wn, nodes, wlim, first_leaf, nlim, st, a.words, nf, tf, any))
         {
             active  = false;

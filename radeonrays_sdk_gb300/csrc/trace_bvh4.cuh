@@ -122,16 +122,13 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
     h.r3 = cr.w;
     // A box hit has a finite entry distance: tmin <= t0 <= t1 <= closest t.
     h.n = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
-    if (h.n > 1)
-    {
-        b4_cas(k0, h.r0, k1, h.r1);
-        b4_cas(k2, h.r2, k3, h.r3);
-        b4_cas(k0, h.r0, k2, h.r2);
-        b4_cas(k1, h.r1, k3, h.r3);
-        b4_cas(k1, h.r1, k2, h.r2);
-    }
-    else if (h.n == 1)
-        h.r0 = k0 < INFINITY ? h.r0 : (k1 < INFINITY ? h.r1 : (k2 < INFINITY ? h.r2 : h.r3));
+    // The network runs whatever n is (no branch): misses carry +inf, so the
+    // hit children end up first, nearest first, and a single hit in slot 0.
+    b4_cas(k0, h.r0, k1, h.r1);
+    b4_cas(k2, h.r2, k3, h.r3);
+    b4_cas(k0, h.r0, k2, h.r2);
+    b4_cas(k1, h.r1, k3, h.r3);
+    b4_cas(k1, h.r1, k2, h.r2);
     return h;
 }
 
@@ -188,16 +185,11 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
     h.r2 = cr.z;
     h.r3 = cr.w;
     h.n  = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
-    if (h.n > 1)
-    {
-        b4_cas(k0, h.r0, k1, h.r1);
-        b4_cas(k2, h.r2, k3, h.r3);
-        b4_cas(k0, h.r0, k2, h.r2);
-        b4_cas(k1, h.r1, k3, h.r3);
-        b4_cas(k1, h.r1, k2, h.r2);
-    }
-    else if (h.n == 1)
-        h.r0 = k0 < INFINITY ? h.r0 : (k1 < INFINITY ? h.r1 : (k2 < INFINITY ? h.r2 : h.r3));
+    b4_cas(k0, h.r0, k1, h.r1);
+    b4_cas(k2, h.r2, k3, h.r3);
+    b4_cas(k0, h.r0, k2, h.r2);
+    b4_cas(k1, h.r1, k3, h.r3);
+    b4_cas(k1, h.r1, k2, h.r2);
     return h;
 }
 

@@ -241,6 +241,9 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_scene_bvh4(SceneTraceArgs 
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
+        // No leaf batching here (unlike the single-level kernel): with the
+        // instance-tree steps as a third kind, holding the leaf lanes back
+        // measured 4-6 % slower.
         if (active && s4_step<kAny>(s, sa, gid, st, nf))
         {
             active  = false;

@@ -436,18 +436,25 @@ class Context:
         self._keep = (scratch, inputs)
         return [result[int(r_off[k]): int(r_off[k]) + reqs[k][1]] for k in range(n)]
 
+    def scene_build_input(self, geometries, transforms):
+        """The RRSceneBuildInput of `geometries` (result tensors) placed by
+        `transforms` ((I, 3, 4) object->world); keep the returned instance
+        array alive while the input is in use."""
+        n = len(geometries)
+        inst = (RRInstance * max(n, 1))()
+        tf = np.asarray(transforms, dtype=np.float32).reshape(n, 3, 4) if n else np.zeros((0, 3, 4), np.float32)
+        rec = np.zeros(max(n, 1), dtype=np.dtype([("geometry", "<u8"), ("transform", "<f4", (3, 4))]))
+        assert rec.itemsize == C.sizeof(RRInstance)
+        rec["geometry"][:n] = [self.ptr(g).value or 0 for g in geometries]
+        rec["transform"][:n] = tf
+        C.memmove(inst, rec.ctypes.data, rec.nbytes)
+        return RRSceneBuildInput(inst, n), inst
+
     def build_scene(self, geometries, transforms, stream=None):
         """geometries: list of result tensors; transforms: (I, 3, 4) float array (object->world)."""
         torch = _torch()
         n = len(geometries)
-        inst = (RRInstance * max(n, 1))()
-        tf = np.asarray(transforms, dtype=np.float32).reshape(n, 3, 4) if n else np.zeros((0, 3, 4), np.float32)
-        for i, g in enumerate(geometries):
-            inst[i].geometry = self.ptr(g)
-            for r in range(3):
-                for c in range(4):
-                    inst[i].transform[r][c] = float(tf[i, r, c])
-        sbi = RRSceneBuildInput(inst, n)
+        sbi, inst = self.scene_build_input(geometries, transforms)
         req = RRMemoryRequirements()
         check(self.L.rrGetSceneBuildMemoryRequirements(self.ctx, C.byref(sbi), None, C.byref(req)),
               "rrGetSceneBuildMemoryRequirements")

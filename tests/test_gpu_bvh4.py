@@ -168,7 +168,7 @@ def test_bvh4_stack_depth_and_launch_shape_keep_hits(ctx, orc):
 
 
 def test_node_format_autotuner_and_auto_builds(ctx, orc, tmp_path, monkeypatch):
-    """rrCudaAutotuneNodeFormat builds the mesh in both wide formats, tunes the
+    """rrCudaAutotuneNodeFormat builds the mesh in the three wide formats, tunes the
     traversal of each, and remembers the faster width for the mesh's size
     class; builds with RR_CUDA_NODE_FORMAT_AUTO then use it, from the context
     and, through RR_CUDA_TUNE_CACHE, in a fresh one."""
@@ -177,7 +177,7 @@ def test_node_format_autotuner_and_auto_builds(ctx, orc, tmp_path, monkeypatch):
     v, i, rays = scenes.config1(grid=257, nrays=1 << 18)
     with rr.Context() as c:
         fmt = c.autotune_node_format(to_dev(v), to_dev(i), to_dev(rays))
-        assert fmt in (rr.RR_CUDA_NODE_FORMAT_BVH4, rr.RR_CUDA_NODE_FORMAT_WIDE8)
+        assert fmt in (rr.RR_CUDA_NODE_FORMAT_BVH4, rr.RR_CUDA_NODE_FORMAT_BVH4Q8, rr.RR_CUDA_NODE_FORMAT_WIDE8)
         res = c.build_geometry(to_dev(v), to_dev(i), node_format=rr.RR_CUDA_NODE_FORMAT_AUTO)
         assert trailer_of(res, i.shape[0])["node_format"] == fmt
         nodes, _, _ = orc.build_mesh(v, i)
