@@ -96,8 +96,9 @@ typedef enum
      * ray touches.  Supported by RR_CUDA_TRAVERSAL_AUTO,
      * RR_CUDA_TRAVERSAL_BINARY_PERSISTENT and RR_CUDA_TRAVERSAL_BVH4 on
      * triangle geometries (not on scene buffers, AABB lists or the
-     * multi-request launch); on an RR_CUDA_NODE_FORMAT_BVH4Q8 buffer it runs
-     * the persistent binary kernel. */
+     * multi-request launch); over RR_CUDA_NODE_FORMAT_BVH4Q8 nodes the
+     * 4-wide kernel decodes the 8-bit bounds rounded outward before the
+     * conservative box test. */
     RR_CUDA_TRIANGLE_TEST_WATERTIGHT = 1
 } RRCudaTriangleTest;
 

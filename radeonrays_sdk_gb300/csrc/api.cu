@@ -759,15 +759,11 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
     // default format; the fastest kernel on incoherent rays), else the
     // persistent binary kernel (bit-identical to BINARY);
     // rrCudaAutotuneTraversal refines the choice per workload.
-    // The precise test runs over fp32 4-wide nodes only: a quantised buffer
-    // then takes the persistent binary kernel.
-    const bool precise  = o.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT;
+    // With the precise test, fp32 and quantised 4-wide nodes take the robust
+    // box test (trace_bvh4.cuh).
     const bool has_bvh4 = bi.kind == kKindGeom && is_bvh4_format(bi.format) && bi.n > 0 &&
-                          bi.prim_kind == kPrimTriangles &&
-                          !(precise && bi.format == RR_CUDA_NODE_FORMAT_BVH4Q8);
-    const bool q8_precise = precise && bi.kind == kKindGeom && bi.format == RR_CUDA_NODE_FORMAT_BVH4Q8 && bi.n > 0;
-    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || (trav == RR_CUDA_TRAVERSAL_AUTO && !has_bvh4) ||
-        (trav == RR_CUDA_TRAVERSAL_BVH4 && q8_precise))
+                          bi.prim_kind == kPrimTriangles;
+    if (trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT || (trav == RR_CUDA_TRAVERSAL_AUTO && !has_bvh4))
     {
         if (sp)
         {

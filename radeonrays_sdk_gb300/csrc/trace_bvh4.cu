@@ -34,9 +34,10 @@ using namespace stream_detail;
 // Residency: 8 blocks per SM (64 registers) over fp32 nodes; 9 (56
 // registers, no spill) over quantised nodes, whose half-size fetches leave
 // the L1 room for more rays in flight (measured 6 % faster; the fp32 nodes
-// were 2 % slower at 9).
+// were 2 % slower at 9).  The precise test needs the 64 registers.
 template <bool kAny, bool kFull, bool kStats, bool kStream, bool kPrecise, bool kQ8>
-__global__ void __launch_bounds__(kPBlock, kQ8 ? 9 : 8) k_trace_bvh4(TraceArgs a, uint32_t gcap, int depth)
+__global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
+    k_trace_bvh4(TraceArgs a, uint32_t gcap, int depth)
 {
     extern __shared__ uint32_t s_stack[];
     const uint32_t             tglob = blockIdx.x * blockDim.x + threadIdx.x;
@@ -207,11 +208,11 @@ cudaError_t go2(const TraceArgs& a, cudaStream_t s)
 template <bool kAny, bool kFull, bool kStats, bool kStream>
 cudaError_t go(const TraceArgs& a, cudaStream_t s)
 {
-    // The precise test runs over fp32 4-wide nodes only (the host routes a
-    // quantised buffer to the persistent binary kernel in that mode).
-    if (a.bvh4_q8) return go2<kAny, kFull, kStats, kStream, false, true>(a, s);
-    if (a.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT) return go2<kAny, kFull, kStats, kStream, true>(a, s);
-    return go2<kAny, kFull, kStats, kStream, false>(a, s);
+    const bool precise = a.triangle_test == RR_CUDA_TRIANGLE_TEST_WATERTIGHT;
+    if (a.bvh4_q8)
+        return precise ? go2<kAny, kFull, kStats, kStream, true, true>(a, s)
+                       : go2<kAny, kFull, kStats, kStream, false, true>(a, s);
+    return precise ? go2<kAny, kFull, kStats, kStream, true>(a, s) : go2<kAny, kFull, kStats, kStream, false>(a, s);
 }
 }  // namespace
 

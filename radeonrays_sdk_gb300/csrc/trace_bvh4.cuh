@@ -141,6 +141,14 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
 // is never above the reference's on the exact child box and the far distance
 // never below it (the same margin as the 8-wide kernel): a child the
 // reference's slab test admits on its exact box is always admitted.
+//
+// kRobust (the precise triangle test's traversal): `inv` is the exact
+// reciprocal and `oxi` the origin.  Each plane is decoded to p + q 2^e with
+// the fma rounded down (lo planes) or up (hi planes), so the decoded box
+// still contains the exact child box, and is then tested with the robust
+// slab distances of b4_children<true>: a child box the exact ray segment
+// touches is never culled.
+template <bool kRobust = false>
 __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct)
 {
     const uint4* p  = reinterpret_cast<const uint4*>(node);
@@ -150,6 +158,44 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
     const uint32_t nxw = sx ? q0.w : q0.x, fxw = sx ? q0.x : q0.w;
     const uint32_t nyw = sy ? q1.x : q0.y, fyw = sy ? q0.y : q1.x;
     const uint32_t nzw = sz ? q1.y : q0.z, fzw = sz ? q0.z : q1.y;
+    if (kRobust)
+    {
+        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        const float ex = __uint_as_float((w0.w & 0xffu) << 23), ey = __uint_as_float(((w0.w >> 8) & 0xffu) << 23),
+                    ez = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+        // Byte c of a plane word as a float (exact: 2^23 + q - 2^23).
+        auto qf = [](uint32_t w, int c) {
+            return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | c)) - 8388608.0f;
+        };
+        // The near plane of an axis is lo for a non-negative direction.
+        auto plane = [](float q, float e, float o, bool is_lo) {
+            return is_lo ? __fmaf_rd(q, e, o) : __fmaf_ru(q, e, o);
+        };
+        auto key = [&](int c, uint32_t r) {
+            const float ax = plane(qf(nxw, c), ex, px, !sx), ay = plane(qf(nyw, c), ey, py, !sy),
+                        az = plane(qf(nzw, c), ez, pz, !sz);
+            const float bx = plane(qf(fxw, c), ex, px, sx), by = plane(qf(fyw, c), ey, py, sy),
+                        bz = plane(qf(fzw, c), ez, pz, sz);
+            const float t0 =
+                fmaxf(b4_max3((ax - oxi.x) * inv.x, (ay - oxi.y) * inv.y, (az - oxi.z) * inv.z), tmin);
+            const float t1 =
+                robust_far(fminf(b4_min3((bx - oxi.x) * inv.x, (by - oxi.y) * inv.y, (bz - oxi.z) * inv.z), ct));
+            return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
+        };
+        float  k0 = key(0, cr.x), k1 = key(1, cr.y), k2 = key(2, cr.z), k3 = key(3, cr.w);
+        B4Hits h;
+        h.r0 = cr.x;
+        h.r1 = cr.y;
+        h.r2 = cr.z;
+        h.r3 = cr.w;
+        h.n  = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
+        b4_cas(k0, h.r0, k1, h.r1);
+        b4_cas(k2, h.r2, k3, h.r3);
+        b4_cas(k0, h.r0, k2, h.r2);
+        b4_cas(k1, h.r1, k3, h.r3);
+        b4_cas(k1, h.r1, k2, h.r2);
+        return h;
+    }
     float          A[3], Bn[3], Bf[3];
     {
         const float p3[3] = {__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z)};
@@ -242,7 +288,9 @@ __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
 // first tested on its exact box (min / max of its vertices, the box its
 // binary parent holds) with the reference's slab arithmetic, so a triangle
 // whose exact box the reference culls is not reached through the larger
-// quantised box either.
+// quantised box either.  With kPrecise the nodes take the robust test and the
+// leaves go straight to the precise triangle test (no box test decides a hit
+// there, so no re-test is needed).
 template <bool kAny, bool kPrecise, bool kRuntime = false, bool kQ8 = false>
 __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ wn, const BvhNode* __restrict__ nodes,
                                         uint32_t wlim, uint32_t first_leaf, uint32_t node_limit, const PStack& st,
@@ -265,7 +313,7 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
         ++tf;
         const F3 v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
         bool     reach = true;
-        if (kQ8)
+        if (kQ8 && !kPrecise)  // the precise test needs no re-test: its box test is conservative
         {
             float b0, b1;
             isect_box(f3(b4_min3(v0.x, v1.x, v2.x), b4_min3(v0.y, v1.y, v2.y), b4_min3(v0.z, v1.z, v2.z)),
@@ -285,8 +333,8 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        const B4Hits h = kQ8 ? b4q_children(reinterpret_cast<const Bvh4QNode*>(wn) + idx, s.inv, s.oxi, s.ray.tmin,
-                                            s.ct)
+        const B4Hits h = kQ8 ? b4q_children<kPrecise>(reinterpret_cast<const Bvh4QNode*>(wn) + idx, s.inv, s.oxi,
+                                                      s.ray.tmin, s.ct)
                              : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
         if (h.n)

@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import gc
 import time
 
 import numpy as np
@@ -264,6 +265,18 @@ class Server:
             if r.rays.shape[0] > self.slot_rays:
                 raise ValueError(f"request {r.rid} has {r.rays.shape[0]} rays, more than a slot holds")
         self._pin(requests)
+        # The loop allocates little, but a cyclic-garbage pass in the middle
+        # of it delays every request in flight: collection waits until the
+        # requests are served.
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            return self._serve(requests, poll_sleep)
+        finally:
+            if gc_on:
+                gc.enable()
+
+    def _serve(self, requests: list[Request], poll_sleep: float) -> dict:
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         queue: collections.deque[Request] = collections.deque()
         t0 = time.perf_counter()

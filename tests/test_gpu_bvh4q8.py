@@ -105,17 +105,35 @@ def test_bvh4q8_soup_heightfield_quality_and_update(ctx, orc):
     assert ctx.device_errors() == 0
 
 
-def test_bvh4q8_precise_mode_falls_back_to_binary(ctx, orc):
-    """The precise test is not run over quantised nodes: with it, a BVH4Q8
-    buffer is traced by the persistent binary kernel (the oracle twin's order)."""
+def test_bvh4q8_precise_mode(ctx, orc):
+    """With the precise test the 4-wide kernel decodes each quantised plane
+    with outward rounding and runs the robust box test, so no box the exact
+    ray segment touches is culled: hits equal the oracle twin's (binary
+    nodes, reference order) except exact equal-t ties, and the persistent
+    binary kernel over the same buffer is bit-identical to the twin."""
+    from gpu_util import hits_np, to_dev
     from radeonrays_sdk_gb300 import scenes
-    v, i, rays = scenes.config1(grid=129, nrays=1 << 15)
+    v, i, rays = scenes.config1(grid=129, nrays=1 << 16)
     res = build(ctx, v, i, node_format=Q8_FORMAT)
     nodes, _, _ = orc.build_mesh(v, i)
     want, _ = orc.trace_precise(nodes, rays, threads=16)
-    for trav in (0, 4):
+    got = {}
+    for trav in (0, 3, 4):
         ctx.set_traversal(trav, triangle_test=1)
-        from gpu_util import hits_np, to_dev
-        got = hits_np(ctx.intersect(res, to_dev(rays)))
+        got[trav] = hits_np(ctx.intersect(res, to_dev(rays)))
         ctx.set_traversal(0)
-        assert np.array_equal(got, want), trav
+    assert np.array_equal(got[3], want)
+    assert np.array_equal(got[0], got[4])  # AUTO runs the 4-wide kernel
+    assert np.array_equal(got[4][:, 2] != INVALID, want[:, 2] != INVALID)
+    tie_only_mismatch(orc, rays, got[4], want, v, i, precise=True)
+    same = got[4][:, 3] == want[:, 3]
+    assert np.array_equal(got[4][same], want[same])
+    # Any hit: the same occlusion flags.
+    occl = rays.copy()
+    occl[:, 7] = np.float32(0.05)
+    wa, _ = orc.trace_precise(nodes, occl, query=1, threads=16)
+    ctx.set_traversal(4, triangle_test=1)
+    ga = hits_np(ctx.intersect(res, to_dev(occl), query=1))
+    ctx.set_traversal(0)
+    assert np.array_equal(ga[:, 2] != INVALID, wa[:, 2] != INVALID)
+    assert ctx.device_errors() == 0
