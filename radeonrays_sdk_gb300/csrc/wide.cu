@@ -21,6 +21,7 @@
 // monotonic and the bounds are floats).  A traversal slab test on the decoded
 // box therefore never rejects a ray that the exact box accepts.
 #include <algorithm>
+#include <cstdlib>
 
 #include "rr_internal.h"
 
@@ -264,16 +265,18 @@ __global__ void k_collapse_init(BatchArgs b)
     ctl->tri_count     = 0;
 }
 
-// Exclusive prefix over geometries of this level's work items (one block).
+// Exclusive prefix over geometries of this level's work items, by one block
+// of kScanBlock threads.  The counts are read from L2 (the drain below runs
+// this after its own atomics in the same launch).
 constexpr int kScanBlock = 1024;
-__global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int level)
+__device__ __forceinline__ void level_scan_block(const BatchArgs& b, int level)
 {
     __shared__ uint32_t warp_sum[kScanBlock / 32];
     const uint32_t per = (b.count + kScanBlock - 1) / kScanBlock;
     const uint32_t g0  = threadIdx.x * per;
     uint32_t       sum = 0;
     for (uint32_t g = g0; g < g0 + per && g < b.count; ++g)
-        if (b.items[g].n > 0) sum += ctl_of(b.items[g])->level_count[level];
+        if (b.items[g].n > 0) sum += __ldcg(&ctl_of(b.items[g])->level_count[level]);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t  x    = sum;
     for (int o = 1; o < 32; o <<= 1)
@@ -289,28 +292,59 @@ __global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int leve
     for (uint32_t g = g0; g < g0 + per && g < b.count; ++g)
     {
         b.level_prefix[g] = run;
-        if (b.items[g].n > 0) run += ctl_of(b.items[g])->level_count[level];
+        if (b.items[g].n > 0) run += __ldcg(&ctl_of(b.items[g])->level_count[level]);
     }
     if (threadIdx.x == kScanBlock - 1) b.level_prefix[b.count] = x + add;
 }
+__global__ void __launch_bounds__(kScanBlock) k_level_scan(BatchArgs b, int level) { level_scan_block(b, level); }
 
-// One level of the collapse for every geometry: work item `it` of the level
-// belongs to the geometry found in the level prefix (a batch of one reads
-// its count directly).
-// kQ8 (W == 4): the 4-wide nodes store 8-bit conservative bounds (Bvh4QNode).
-template <int W, bool kQ8 = false>
-__global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, DeviceWords* words)
+// Work items of a level in the batch: its total (a batch of one reads its
+// count directly).
+__device__ __forceinline__ uint32_t level_total(const BatchArgs& b, int level)
 {
-    const uint32_t total = b.count == 1 ? *((volatile uint32_t*)&ctl_of(b.items[0])->level_count[level])
-                                        : *((volatile uint32_t*)&b.level_prefix[b.count]);
-    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < ((total + 31u) & ~31u);
-         it += gridDim.x * blockDim.x)
+    return b.count == 1 ? *((volatile uint32_t*)&ctl_of(b.items[0])->level_count[level])
+                        : *((volatile uint32_t*)&b.level_prefix[b.count]);
+}
+
+// Geometry of work item t: the last prefix entry <= t, read from L2.
+__device__ __forceinline__ uint32_t batch_find_cg(const uint32_t* prefix, uint32_t count, uint32_t t)
+{
+    uint32_t lo = 0, hi = count;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldcg(prefix + mid) <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// One level of the collapse for every geometry, items first, first + stride,
+// ...: work item `it` of the level belongs to the geometry found in the
+// level prefix.  Warps stay whole (the item range is rounded up to 32).
+// kQ8 (W == 4): the 4-wide nodes store 8-bit conservative bounds (Bvh4QNode).
+// kCoherent: the queue and the prefix were written earlier in the same
+// launch (the drain), so they are read from L2, never through the
+// read-only path.
+template <int W, bool kQ8, bool kCoherent>
+__device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, DeviceWords* words, uint32_t total,
+                                              uint32_t first, uint32_t stride)
+{
+    for (uint32_t it = first; it < ((total + 31u) & ~31u); it += stride)
     {
         const bool     active = it < total;
-        const uint32_t g      = !active ? 0xffffffffu : (b.count == 1 ? 0u : batch_find(b.level_prefix, b.count, it));
+        const uint32_t g      = !active ? 0xffffffffu
+                                        : (b.count == 1 ? 0u
+                                           : kCoherent ? batch_find_cg(b.level_prefix, b.count, it)
+                                                       : batch_find(b.level_prefix, b.count, it));
         const uint32_t peers  = __match_any_sync(0xffffffffu, g);
         const BuildItem* bi   = active ? b.items + g : b.items;
-        const uint32_t local  = active ? it - (b.count == 1 ? 0u : __ldg(b.level_prefix + g)) : 0u;
+        const uint32_t local  = active ? it - (b.count == 1 ? 0u
+                                                : kCoherent ? __ldcg(b.level_prefix + g)
+                                                            : __ldg(b.level_prefix + g))
+                                       : 0u;
         const BvhNode* __restrict__ nodes = reinterpret_cast<const BvhNode*>(bi->result);
         CollapseCtl*   ctl           = ctl_of(*bi);
         const Item* __restrict__ qin = queue_of(*bi, level);
@@ -329,7 +363,13 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
             // a child's kind follows from its index; each expansion of the
             // largest internal child is one node load.
             const uint32_t first_leaf = bi->n - 1;
-            item          = qin[local];
+            if (kCoherent)
+            {
+                const uint2 q = __ldcg(reinterpret_cast<const uint2*>(qin) + local);
+                item          = Item{q.x, q.y};
+            }
+            else
+                item = qin[local];
             BvhNode root  = load_node(nodes, item.b);
             ch[0]         = root.child0;
             ch[1]         = root.child1;
@@ -579,6 +619,33 @@ __global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, 
     }
 }
 
+template <int W, bool kQ8 = false>
+__global__ void __launch_bounds__(128) k_collapse_level(BatchArgs b, int level, DeviceWords* words)
+{
+    collapse_pass<W, kQ8, false>(b, level, words, level_total(b, level), blockIdx.x * blockDim.x + threadIdx.x,
+                                 gridDim.x * blockDim.x);
+}
+
+// The levels from `first_level` on, by one block, level after level (a
+// barrier between them), until a level has no work items.  The host
+// launches one k_collapse_level per level for as many levels as a tree of
+// the batch's largest size normally has; a deeper tree (many equal Morton
+// codes, for instance) ends here, correctly if slowly, instead of the host
+// launching the maximum number of levels, most of them empty.
+template <int W, bool kQ8 = false>
+__global__ void __launch_bounds__(kScanBlock) k_collapse_drain(BatchArgs b, int first_level, DeviceWords* words)
+{
+    for (int level = first_level; level < kMaxLevels; ++level)
+    {
+        if (b.count > 1) level_scan_block(b, level);
+        __syncthreads();
+        const uint32_t total = level_total(b, level);  // the same for every thread: written before the barrier
+        if (total == 0) break;
+        collapse_pass<W, kQ8, true>(b, level, words, total, threadIdx.x, blockDim.x);
+        __syncthreads();
+    }
+}
+
 __global__ void k_collapse_finish(BatchArgs b, DeviceWords* words)
 {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -604,8 +671,24 @@ cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm
     {
         // Work items of a level are bounded by count * 8^level and by the
         // number of triangles (every item is a distinct internal subtree).
+        // Launched levels: ceil(log_W(largest n)) + 8 (a collapsed LBVH of n
+        // triangles measured 4 to 16 levels deep for n up to 4.2 M: soups
+        // and heightfields, fast and restructured); the drain takes any
+        // deeper level.
+        const uint32_t fan    = is_bvh4_format(b.format) ? 4u : 8u;
+        int            levels = 8;
+        for (uint64_t c = 1; c < b.max_n; c *= fan) ++levels;
+        levels         = std::min(levels, kMaxLevels);
+        // RR_CUDA_COLLAPSE_LEVELS=k (1 .. the count above) launches only k
+        // level kernels and leaves the rest to the drain, so that tests run
+        // the drain on ordinary trees.
+        if (const char* e = std::getenv("RR_CUDA_COLLAPSE_LEVELS"))
+        {
+            const int k = std::atoi(e);
+            if (k >= 1 && k < levels) levels = k;
+        }
         uint64_t bound = b.count;
-        for (int level = 0; level < kMaxLevels; ++level)
+        for (int level = 0; level < levels; ++level)
         {
             if (b.count > 1) k_level_scan<<<1, kScanBlock, 0, s>>>(b, level);
             const uint64_t cap    = std::min<uint64_t>(bound, b.total_prims);
@@ -617,7 +700,16 @@ cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm
                 k_collapse_level<4, true><<<blocks, 128, 0, s>>>(b, level, words);
             else
                 k_collapse_level<8><<<blocks, 128, 0, s>>>(b, level, words);
-            bound = std::min<uint64_t>(bound * (is_bvh4_format(b.format) ? 4 : 8), b.total_prims);
+            bound = std::min<uint64_t>(bound * fan, b.total_prims);
+        }
+        if (levels < kMaxLevels)
+        {
+            if (b.format == RR_CUDA_NODE_FORMAT_BVH4)
+                k_collapse_drain<4><<<1, kScanBlock, 0, s>>>(b, levels, words);
+            else if (b.format == RR_CUDA_NODE_FORMAT_BVH4Q8)
+                k_collapse_drain<4, true><<<1, kScanBlock, 0, s>>>(b, levels, words);
+            else
+                k_collapse_drain<8><<<1, kScanBlock, 0, s>>>(b, levels, words);
         }
     }
     k_collapse_finish<<<per_geom, 128, 0, s>>>(b, words);
