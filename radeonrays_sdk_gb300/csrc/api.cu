@@ -1563,8 +1563,10 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
     uint64_t total = 0;
     // The 4-wide kernel when the traversal option allows it and every request
     // with rays has a triangle geometry with 4-wide nodes (or none at all).
+    // The 4-wide nodes must all have the same form (fp32 or 8-bit bounds).
     const uint32_t trav = ctx->topts.traversal;
     bool           use4 = trav == RR_CUDA_TRAVERSAL_AUTO || trav == RR_CUDA_TRAVERSAL_BVH4;
+    uint32_t       fmt4 = 0;
     for (uint32_t k = 0; k < count && use4; ++k)
     {
         auto it = ctx->registry.find((uintptr_t)dq[k].bvh);
@@ -1574,9 +1576,15 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
             continue;
         }
         const BufInfo& b = it->second;
-        use4 = b.kind == kKindGeom && (b.n == 0 || dq[k].ray_count == 0 ||
-                                       (b.format == RR_CUDA_NODE_FORMAT_BVH4 && b.prim_kind == kPrimTriangles &&
-                                        b.wide_off % 256 == 0 && b.wide_off / 256 <= 0xffffffffull));
+        if (b.kind != kKindGeom)
+        {
+            use4 = false;
+            continue;
+        }
+        if (b.n == 0 || dq[k].ray_count == 0) continue;
+        use4 = is_bvh4_format(b.format) && (fmt4 == 0 || fmt4 == b.format) && b.prim_kind == kPrimTriangles &&
+               b.wide_off % 256 == 0 && b.wide_off / 256 <= 0xffffffffull;
+        fmt4 = b.format;
     }
     for (uint32_t k = 0; k < count; ++k)
     {
@@ -1599,7 +1607,7 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
                   (q.output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? kReqFull : 0u) |
                   (bi.kind == kKindGeom && bi.n == 0 ? kReqEmpty : 0u) |
                   (bi.kind == kKindGeom && bi.prim_kind == kPrimAabbs ? kReqBoxes : 0u);
-        if (use4 && bi.kind == kKindGeom && bi.n > 0 && bi.format == RR_CUDA_NODE_FORMAT_BVH4)
+        if (use4 && bi.kind == kKindGeom && bi.n > 0 && is_bvh4_format(bi.format))
         {
             r.flags |= kReqBvh4;
             r.wide_off256 = (uint32_t)(bi.wide_off / 256);
@@ -1625,6 +1633,7 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
     a.blocks_per_sm    = (int)ctx->topts.blocks_per_sm;
     a.collect_stats    = ctx->topts.collect_stats ? 1 : 0;
     a.use_bvh4         = use4 ? 1 : 0;
+    a.bvh4_q8          = use4 && fmt4 == RR_CUDA_NODE_FORMAT_BVH4Q8 ? 1 : 0;
     const size_t bytes = gap + pre;
     *out               = [=](cudaStream_t s) -> cudaError_t {
         cudaError_t e = cudaMemcpyAsync(sc + L.req_off, stage->p, bytes, cudaMemcpyHostToDevice, s);

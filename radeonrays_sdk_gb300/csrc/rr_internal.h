@@ -400,6 +400,7 @@ struct BatchTraceArgs
     int                  blocks_per_sm;
     int                  collect_stats;
     int                  use_bvh4;  // every request kReqBvh4 or empty: the 4-wide kernel
+    int                  bvh4_q8;   // ... and their 4-wide nodes have 8-bit bounds (Bvh4QNode)
 };
 // Every request's rays in one persistent launch (per ray the visit order of
 // the single-request kernel it stands for -- the reference's binary order, or

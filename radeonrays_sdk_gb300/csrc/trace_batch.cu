@@ -11,9 +11,9 @@
 // hit is bit-identical to tracing that request alone with rrCmdIntersect.
 //
 // With 4-wide geometries (use_bvh4: every request's buffer carries 4-wide
-// nodes) the lanes run the 4-wide kernel's state machine (trace_bvh4.cuh)
-// instead, so each hit equals that request traced alone with
-// RR_CUDA_TRAVERSAL_BVH4.
+// nodes, all fp32 or all 8-bit) the lanes run the 4-wide kernel's state
+// machine (trace_bvh4.cuh) instead, so each hit equals that request traced
+// alone with RR_CUDA_TRAVERSAL_BVH4.
 #include "trace_bvh4.cuh"
 #include "trace_persistent.cuh"
 
@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch(BatchTraceArgs a, ui
 // The 4-wide variant: the same refill loop around b4_step; a request's
 // 4-wide nodes sit wide_off256 * 256 bytes into its buffer, its binary leaves
 // (the triangles) at [n - 1, 2n - 2].
-template <bool kStats>
+// kQ8: every request's 4-wide nodes have 8-bit bounds (b4_step's kQ8).
+template <bool kStats, bool kQ8>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch_bvh4(BatchTraceArgs a, uint32_t gcap)
 {
     __shared__ uint32_t s_stack[kPBlock * kPShort];
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch_bvh4(BatchTraceArgs 
         const bool at_leaf = active && (s.ref & kBvh4Leaf) != 0;
         const bool do_leaf = 4 * __popc(__ballot_sync(0xffffffffu, at_leaf)) >= __popc(amask);
         if (active && at_leaf == do_leaf &&
-            b4_step<false, false, true>(s, wn, nodes, wlim, first_leaf, nlim, st, a.words, nf, tf, any))
+            b4_step<false, false, true, kQ8>(s, wn, nodes, wlim, first_leaf, nlim, st, a.words, nf, tf, any))
         {
             active  = false;
             pending = true;
@@ -236,7 +237,9 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_batch_bvh4(BatchTraceArgs 
 template <bool kStats>
 cudaError_t go(const BatchTraceArgs& a, cudaStream_t s)
 {
-    auto kern   = a.use_bvh4 ? k_trace_batch_bvh4<kStats> : k_trace_batch<kStats>;
+    auto kern   = !a.use_bvh4 ? k_trace_batch<kStats>
+                  : a.bvh4_q8 ? k_trace_batch_bvh4<kStats, true>
+                              : k_trace_batch_bvh4<kStats, false>;
     int  per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {

@@ -75,14 +75,16 @@ def test_server_results_equal_alone_under_eviction(ctx):
         assert np.array_equal(r.hits, want), r.rid
 
 
-def test_batch_bvh4_equals_alone_and_oracle(ctx, orc):
-    """Requests whose geometries all carry 4-wide nodes run the 4-wide
-    multi-request kernel: each request's hits equal the 4-wide kernel's on
-    that request alone, bit for bit, and the oracle's up to equal-t ties."""
+@pytest.mark.parametrize("fmt", [2, 4])  # fp32 and 8-bit 4-wide nodes
+def test_batch_bvh4_equals_alone_and_oracle(ctx, orc, fmt):
+    """Requests whose geometries all carry 4-wide nodes of one form run the
+    4-wide multi-request kernel: each request's hits equal the 4-wide
+    kernel's on that request alone, bit for bit, and the oracle's up to
+    equal-t ties."""
     from radeonrays_sdk_gb300 import scenes
     from gpu_util import tie_only_mismatch
     ms = _scenes()
-    bvhs = [ctx.build_geometry(to_dev(v), to_dev(i)) for v, i in ms]
+    bvhs = [ctx.build_geometry(to_dev(v), to_dev(i), node_format=fmt) for v, i in ms]
     empty = ctx.build_geometry(to_dev(np.zeros((0, 3), np.float32)), to_dev(np.zeros((0, 3), np.uint32)))
     spec = [(0, 5000, 0, 0), (1, 1, 1, 0), (2, 77777, 0, 1), (0, 0, 0, 0), (1, 20000, 1, 1), (-1, 300, 0, 0),
             (2, 4096, 1, 0), (1, 30000, 0, 0)]
@@ -118,3 +120,21 @@ def test_batch_bvh4_equals_alone_and_oracle(ctx, orc):
                 tie_only_mismatch(orc, rays, gf, want, v, i)
         else:
             assert np.array_equal(g != INVALID, want[:, 2] != INVALID)
+
+
+def test_batch_mixed_4wide_forms_take_the_binary_kernel(ctx):
+    """fp32 and 8-bit 4-wide geometries in one launch: the launch runs the
+    reference-order kernel, so each request equals the binary kernel alone."""
+    from radeonrays_sdk_gb300 import scenes
+    ms = _scenes()
+    bvhs = [ctx.build_geometry(to_dev(v), to_dev(i), node_format=2 + 2 * (k % 2)) for k, (v, i) in enumerate(ms)]
+    reqs, host = [], []
+    for k, (v, i) in enumerate(ms):
+        rays = scenes.incoherent_rays(3000 + 500 * k, v.min(axis=0), v.max(axis=0), scenes.rng(54, k))
+        reqs.append((bvhs[k], to_dev(rays), 0, 0))
+        host.append(rays)
+    ctx.set_traversal(0)
+    got = [hits_np(h) for h in ctx.intersect_batch(reqs)]
+    for (bvh, _, _, _), rays, g in zip(reqs, host, got):
+        assert np.array_equal(g, _alone(ctx, bvh, rays, 0, 0, traversal=1))
+    assert ctx.device_errors() == 0
