@@ -112,8 +112,9 @@ def parse():
     ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--requests", type=int, default=10000, help="serving: requests per load point")
     ap.add_argument("--slots", type=int, default=3)
-    ap.add_argument("--scene-format", default="bvh4", choices=["bvh4", "binary"],
-                    help="serving: node format of the resident scenes (bvh4 runs the 4-wide multi-request kernel)")
+    ap.add_argument("--scene-format", default="bvh4q8", choices=["bvh4", "bvh4q8", "binary"],
+                    help="serving: node format of the resident scenes (bvh4 and bvh4q8 run the 4-wide "
+                         "multi-request kernel over fp32 or 8-bit nodes)")
     ap.add_argument("--slot-rays", type=int, default=1 << 22)
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0)
     ap.add_argument("--chosen-format", default="auto", choices=["auto", "wide8", "bvh4", "bvh4q8"],
@@ -879,8 +880,8 @@ def serving_summary(args):
     ntri = sum(i.shape[0] for _, i in meshes)
     ctx = rr.Context()
     pool = serving.ScenePool(ctx, int(args.hbm_budget_gb * (1 << 30)),
-                             node_format=rr.RR_CUDA_NODE_FORMAT_BINARY if args.scene_format == "binary" else
-                             rr.RR_CUDA_NODE_FORMAT_BVH4)
+                             node_format={"binary": rr.RR_CUDA_NODE_FORMAT_BINARY, "bvh4": rr.RR_CUDA_NODE_FORMAT_BVH4,
+                                          "bvh4q8": rr.RR_CUDA_NODE_FORMAT_BVH4Q8}[args.scene_format])
     for k, (v, i) in enumerate(meshes):
         pool.register(k, v, i)
     torch.cuda.synchronize()
@@ -928,7 +929,8 @@ def serving_summary(args):
             "latency_definition": "arrival to hits copied to the request's pinned host buffer",
             "scene_format": "binary nodes only (launches run the reference-order multi-request kernel)"
                             if args.scene_format == "binary" else
-                            "binary + 4-wide nodes (launches run the 4-wide multi-request kernel)",
+                            "binary + 4-wide nodes with " + ("8-bit" if args.scene_format == "bvh4q8" else "fp32")
+                            + " bounds (launches run the 4-wide multi-request kernel)",
             "hits_checked": {"requests": len(check), "identical_to_alone": same,
                              "against": "each request traced alone by rrCmdIntersect with "
                                         + ("RR_CUDA_TRAVERSAL_BINARY" if args.scene_format == "binary" else

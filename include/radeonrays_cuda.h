@@ -328,9 +328,10 @@ RR_API RRError rrCudaCmdIntersectHostBuffers(RRContext              context,
  * requests it admits into one call: every request's rays are traced by one
  * persistent launch whose lanes take rays from all requests.  When the
  * context's traversal option is RR_CUDA_TRAVERSAL_AUTO or _BVH4 and every
- * request with rays has a triangle geometry with 4-wide nodes
- * (RR_CUDA_NODE_FORMAT_BVH4, the default) or no triangles, each request is
- * traced exactly like rrCmdIntersect with RR_CUDA_TRAVERSAL_BVH4; otherwise
+ * request with rays has a triangle geometry with 4-wide nodes of one form
+ * (all RR_CUDA_NODE_FORMAT_BVH4, the default, or all _BVH4Q8) or no
+ * triangles, each request is traced exactly like rrCmdIntersect with
+ * RR_CUDA_TRAVERSAL_BVH4; otherwise
  * exactly like rrCmdIntersect with RR_CUDA_TRAVERSAL_BINARY (the reference's
  * visit order).  Either way a request's hits do not depend on what it is
  * packed with.  The precise triangle test is not applied here. */

@@ -170,6 +170,56 @@ struct DevicePtr
     uint8_t* addr() const { return base + offset; }
 };
 
+// Page-locked host blocks for the staging of ops, reused.  cudaMallocHost
+// pins pages (milliseconds for large blocks) and cudaFreeHost can wait for
+// the device, which serialised multi-request launches that should overlap
+// on different streams.  Blocks come in power-of-two sizes from 4 KiB; up to
+// kKeep bytes of returned blocks are kept, the rest freed.  Ops hold the
+// pool by shared pointer, so it outlives the context if an op does.
+struct PinnedPool
+{
+    static constexpr size_t         kKeep = size_t(256) << 20;
+    std::mutex                      mu;
+    std::multimap<size_t, void*>    free_blocks;  // capacity -> block
+    size_t                          held = 0;
+    void* take(size_t bytes, size_t& cap)
+    {
+        cap = 4096;
+        while (cap < bytes) cap <<= 1;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            auto it = free_blocks.find(cap);
+            if (it != free_blocks.end())
+            {
+                void* p = it->second;
+                free_blocks.erase(it);
+                held -= cap;
+                return p;
+            }
+        }
+        void* p = nullptr;
+        check(cudaMallocHost(&p, cap), "cudaMallocHost");
+        return p;
+    }
+    void give(void* p, size_t cap)
+    {
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            if (held + cap <= kKeep)
+            {
+                free_blocks.emplace(cap, p);
+                held += cap;
+                return;
+            }
+        }
+        cudaFreeHost(p);
+    }
+    ~PinnedPool()
+    {
+        for (auto& b : free_blocks) cudaFreeHost(b.second);
+    }
+};
+
 struct Context
 {
     int                    device   = 0;
@@ -184,6 +234,7 @@ struct Context
     std::map<std::string, uint32_t> fmt_choice;  // node-format tuner results by mesh-size key
     std::map<std::string, RRCudaTraversalOptions> tuned;  // autotuner results by workload key
     std::map<uintptr_t, BufInfo> registry;
+    std::shared_ptr<PinnedPool>  pinned = std::make_shared<PinnedPool>();
     // Ops run at once on external streams, kept (with the memory they own)
     // until an event after them has completed; ops enqueued into a stream
     // capture are kept until the context goes.
@@ -589,17 +640,20 @@ void inverse34(const float* m, float* out)
     }
 }
 
+// A staging block of the context's pinned pool, returned to it when the op
+// that owns it is destroyed (after the op's copies have completed).
 struct PinnedBlock
 {
-    void*  p = nullptr;
-    size_t n = 0;
-    explicit PinnedBlock(size_t bytes) : n(bytes)
+    std::shared_ptr<PinnedPool> pool;
+    void*                       p   = nullptr;
+    size_t                      cap = 0;
+    PinnedBlock(const std::shared_ptr<PinnedPool>& from, size_t bytes) : pool(from)
     {
-        if (bytes) check(cudaMallocHost(&p, bytes), "cudaMallocHost");
+        if (bytes) p = pool->take(bytes, cap);
     }
     ~PinnedBlock()
     {
-        if (p) cudaFreeHost(p);
+        if (p) pool->give(p, cap);
     }
 };
 
@@ -1310,7 +1364,7 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
             if (!build_input->instances[i].geometry) return RR_ERROR_INVALID_PARAMETER;
         // Host staging: [xforms 2n x 12 floats: inverse, forward][InstanceDesc n].
         const size_t xbytes = (size_t)n * 2 * 48, ibytes = (size_t)n * sizeof(InstanceDesc);
-        auto         stage  = std::make_shared<PinnedBlock>(xbytes + ibytes);
+        auto         stage  = std::make_shared<PinnedBlock>(ctx->pinned, xbytes + ibytes);
         float*       xf     = reinterpret_cast<float*>(stage->p);
         InstanceDesc* id    = reinterpret_cast<InstanceDesc*>(reinterpret_cast<uint8_t*>(stage->p) + xbytes);
         bool          all_wide = n > 0;
@@ -1556,7 +1610,7 @@ RRError batch_trace_op(Context* ctx, const std::vector<DevRequest>& dq, uint8_t*
     const BatchTraceLayout L0    = batch_trace_layout(count, 0);
     const size_t           pre   = ((size_t)count + 1) * sizeof(uint32_t);
     const size_t           gap   = L0.prefix_off - L0.req_off;
-    auto                   stage = std::make_shared<PinnedBlock>(gap + pre);
+    auto                   stage = std::make_shared<PinnedBlock>(ctx->pinned, gap + pre);
     BatchTraceReq*         rq    = reinterpret_cast<BatchTraceReq*>(stage->p);
     uint32_t*              pf    = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(stage->p) + gap);
     std::memset(stage->p, 0, gap + pre);

@@ -61,11 +61,12 @@ class Request:
 
 class ScenePool:
     """Resident BVHs of many meshes under a byte budget.  The default node
-    format (binary + 4-wide nodes) lets a launch whose requests all have
-    4-wide nodes run the 4-wide multi-request kernel; with binary-only
-    scenes the launches run the reference-order binary kernel."""
+    format (binary + 4-wide nodes with 8-bit bounds, half the bytes of the
+    fp32 ones) lets a launch whose requests all have such nodes run the
+    4-wide multi-request kernel; with binary-only scenes the launches run
+    the reference-order binary kernel."""
 
-    def __init__(self, ctx: rr.Context, budget_bytes: int, node_format: int = rr.RR_CUDA_NODE_FORMAT_BVH4):
+    def __init__(self, ctx: rr.Context, budget_bytes: int, node_format: int = rr.RR_CUDA_NODE_FORMAT_BVH4Q8):
         self.ctx = ctx
         self.budget = int(budget_bytes)
         self.node_format = node_format
