@@ -87,7 +87,8 @@ struct BufInfo
     size_t   trailer_off = 0, wide_off = 0, tris_off = 0, xforms_off = 0, inst_off = 0;
     size_t   wide_capacity = 0;  // geometry: 8-wide or 4-wide node capacity
     bool     scene_wide = false;  // scene: every instance has 8-wide nodes
-    bool     scene_bvh4 = false;  // scene: every instance has 4-wide nodes
+    bool     scene_bvh4 = false;  // scene: every instance has 4-wide nodes of one form
+    bool     scene_bvh4_q8 = false;  // ... with 8-bit bounds
     uint32_t prim_kind  = kPrimTriangles;  // geometry: triangles or AABB list
 };
 
@@ -802,6 +803,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         sa.use_wide       = bi.scene_wide && trav == RR_CUDA_TRAVERSAL_WIDE;
         sa.use_persistent = trav == RR_CUDA_TRAVERSAL_AUTO || trav == RR_CUDA_TRAVERSAL_BINARY_PERSISTENT;
         sa.use_bvh4       = bi.scene_bvh4 && trav == RR_CUDA_TRAVERSAL_BVH4;
+        sa.bvh4_q8        = bi.scene_bvh4_q8 ? 1 : 0;
         if (sp) return Op();
         return [=](cudaStream_t s) { return launch_trace_scene(sa, s); };
     }
@@ -1368,7 +1370,8 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
         float*       xf     = reinterpret_cast<float*>(stage->p);
         InstanceDesc* id    = reinterpret_cast<InstanceDesc*>(reinterpret_cast<uint8_t*>(stage->p) + xbytes);
         bool          all_wide = n > 0;
-        bool          all_bvh4 = n > 0;  // every instance 4-wide (or empty)
+        bool          all_bvh4 = n > 0;  // every instance 4-wide of one form (or empty)
+        uint32_t      fmt4     = 0;
         for (uint32_t i = 0; i < n; ++i)
         {
             const RRInstance& in = build_input->instances[i];
@@ -1391,8 +1394,12 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
                 }
                 else
                     all_wide = false;
-                if (it->second.format == RR_CUDA_NODE_FORMAT_BVH4 && it->second.n > 0)
+                if (is_bvh4_format(it->second.format) && it->second.n > 0 &&
+                    (fmt4 == 0 || fmt4 == it->second.format))
+                {
                     d.wide_nodes = (uint64_t)(uintptr_t)(blas + it->second.wide_off);  // its 4-wide nodes
+                    fmt4         = it->second.format;
+                }
                 else if (it->second.n > 0)
                     all_bvh4 = false;
                 d.flags = 1;  // known geometry
@@ -1435,6 +1442,7 @@ RR_API RRError rrCmdBuildScene(RRContext                context,
         bi.inst_off    = L.inst_off;
         bi.scene_wide  = all_wide;
         bi.scene_bvh4  = all_bvh4;
+        bi.scene_bvh4_q8 = all_bvh4 && fmt4 == RR_CUDA_NODE_FORMAT_BVH4Q8;
         ctx->registry[(uintptr_t)result] = bi;
         return RR_SUCCESS;
     })

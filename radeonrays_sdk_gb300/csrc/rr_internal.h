@@ -421,7 +421,8 @@ struct SceneTraceArgs
     uint32_t            inst_count;
     int                 use_wide;        // 8-wide BLAS kernel
     int                 use_persistent;  // persistent binary two-level kernel
-    int                 use_bvh4;        // persistent kernel over 4-wide BLASes (all instances BVH4)
+    int                 use_bvh4;        // persistent kernel over 4-wide BLASes (all instances of one 4-wide form)
+    int                 bvh4_q8;         // ... BVH4Q8 (8-bit bounds)
 };
 cudaError_t launch_trace_scene(const SceneTraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_scene_persistent(const SceneTraceArgs& a, cudaStream_t s);

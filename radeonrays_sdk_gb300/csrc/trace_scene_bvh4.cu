@@ -1,6 +1,7 @@
 // trace_scene_bvh4.cu -- persistent lane-refill two-level traversal of a
-// scene whose instances all have 4-wide nodes (RR_CUDA_NODE_FORMAT_BVH4
-// BLASes; no reference counterpart for the BLAS part, see trace_bvh4.cu).
+// scene whose instances all have 4-wide nodes of one form
+// (RR_CUDA_NODE_FORMAT_BVH4 or _BVH4Q8 BLASes; no reference counterpart for
+// the BLAS part, see trace_bvh4.cu).
 //
 // The instance tree is binary and traversed as in isect_2l.comp:153-322:
 // near child first, one stack for both levels, an instance leaf pushes the
@@ -54,7 +55,10 @@ __device__ __forceinline__ void set_frame(S4Ray& s, const Ray& r)
 }
 
 // One step; true when the ray is finished.
-template <bool kAny>
+// kQ8: the BLASes' 4-wide nodes have 8-bit bounds (Bvh4QNode); as in the
+// single-level kernel, a leaf triangle is first tested on its exact box with
+// the reference's slab arithmetic.
+template <bool kAny, bool kQ8>
 __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint32_t gid, const PStack& st,
                                         uint32_t& nf)
 {
@@ -129,7 +133,18 @@ __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint
         {
             const float4* p = reinterpret_cast<const float4*>(s.blas + idx);
             const float4  v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
-            const float   t = isect_tri(s.ray, f3(v0.x, v0.y, v0.z), f3(v1.x, v1.y, v1.z), f3(v2.x, v2.y, v2.z), s.ct);
+            bool          reach = true;
+            if (kQ8)
+            {
+                float b0, b1;
+                isect_box(f3(b4_min3(v0.x, v1.x, v2.x), b4_min3(v0.y, v1.y, v2.y), b4_min3(v0.z, v1.z, v2.z)),
+                          f3(b4_max3(v0.x, v1.x, v2.x), b4_max3(v0.y, v1.y, v2.y), b4_max3(v0.z, v1.z, v2.z)), s.inv,
+                          s.oxi, s.ct, s.ray.tmin, b0, b1);
+                reach = b0 <= b1;
+            }
+            const float t = reach ? isect_tri(s.ray, f3(v0.x, v0.y, v0.z), f3(v1.x, v1.y, v1.z),
+                                              f3(v2.x, v2.y, v2.z), s.ct)
+                                  : s.ct;
             if (t < s.ct)
             {
                 s.ct    = t;
@@ -140,7 +155,9 @@ __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint
         }
         else
         {
-            const B4Hits h = b4_children(s.blas4 + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
+            const B4Hits h = kQ8 ? b4q_children(reinterpret_cast<const Bvh4QNode*>(s.blas4) + idx, s.inv, s.oxi,
+                                                s.ray.tmin, s.ct)
+                                 : b4_children(s.blas4 + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
             if (h.n)
             {
                 s.addr  = b4_descend(h, s.sp, s.gsp, st, a.words);
@@ -159,7 +176,7 @@ __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint
     return false;
 }
 
-template <bool kAny, bool kFull, bool kStats>
+template <bool kAny, bool kFull, bool kStats, bool kQ8>
 __global__ void __launch_bounds__(kPBlock, 8) k_trace_scene_bvh4(SceneTraceArgs sa, uint32_t gcap)
 {
     const TraceArgs&    a = sa.base;
@@ -244,7 +261,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_scene_bvh4(SceneTraceArgs 
         // No leaf batching here (unlike the single-level kernel): with the
         // instance-tree steps as a third kind, holding the leaf lanes back
         // measured 4-6 % slower.
-        if (active && s4_step<kAny>(s, sa, gid, st, nf))
+        if (active && s4_step<kAny, kQ8>(s, sa, gid, st, nf))
         {
             active  = false;
             pending = true;
@@ -256,7 +273,8 @@ template <bool kAny, bool kFull, bool kStats>
 cudaError_t go(const SceneTraceArgs& sa, cudaStream_t s)
 {
     const TraceArgs& a      = sa.base;
-    auto             kern   = k_trace_scene_bvh4<kAny, kFull, kStats>;
+    auto             kern   = sa.bvh4_q8 ? k_trace_scene_bvh4<kAny, kFull, kStats, true>
+                                         : k_trace_scene_bvh4<kAny, kFull, kStats, false>;
     int              per_sm = a.blocks_per_sm;
     if (per_sm <= 0)
     {

@@ -136,11 +136,12 @@ def _tie_tolerant(got, want, q, o, ties=2):
         assert np.array_equal(got != INVALID, want != INVALID)
 
 
-def test_scene_trace_bvh4(ctx, orc):
+@pytest.mark.parametrize("fmt", [2, 4])  # fp32 and 8-bit 4-wide BLASes
+def test_scene_trace_bvh4(ctx, orc, fmt):
     """4-wide BLASes: RR_CUDA_TRAVERSAL_BVH4 runs the two-level 4-wide kernel;
     hit flags equal the oracle's, primitives except exact equal-t ties."""
     g = golden("scene6")
-    _, scene = scene_from_fixture(ctx, g, 2)
+    _, scene = scene_from_fixture(ctx, g, fmt)
     rays = to_dev(g["rays"])
     for q in (0, 1):
         for o in (0, 1):
@@ -151,8 +152,9 @@ def test_scene_trace_bvh4(ctx, orc):
     assert ctx.device_errors() == 0
 
 
-def test_scene_bvh4_larger_with_empty_blas(ctx, orc):
-    """40 uneven BLASes (one empty) built fused in the 4-wide format, a
+@pytest.mark.parametrize("fmt", [2, 4])
+def test_scene_bvh4_larger_with_empty_blas(ctx, orc, fmt):
+    """40 uneven BLASes (one empty) built fused in a 4-wide format, a
     60,000-ray batch: the two-level 4-wide kernel against the oracle."""
     import torch
     from radeonrays_sdk_gb300 import scenes
@@ -160,7 +162,7 @@ def test_scene_bvh4_larger_with_empty_blas(ctx, orc):
     blas_np[7] = (np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
     fused = ctx.build_geometries([(to_dev(v) if v.size else torch.zeros((3, 3), dtype=torch.float32, device="cuda"),
                                    to_dev(i) if i.size else torch.zeros((0, 3), dtype=torch.int32, device="cuda"))
-                                  for v, i in blas_np], node_format=2)
+                                  for v, i in blas_np], node_format=fmt)
     scene = ctx.build_scene(fused, M)
     onodes = [orc.build_mesh(v, i)[0] if i.size else None for v, i in blas_np]
     tlas, xf = orc.build_scene(onodes, [i.shape[0] for _, i in blas_np], M)
