@@ -352,11 +352,23 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
         WideNode*      wn            = reinterpret_cast<WideNode*>(bi->result + bi->wide_off);
         WideTri*       wt            = reinterpret_cast<WideTri*>(bi->result + bi->tris_off);
         const uint32_t wide_capacity = bi->wide_capacity, tri_capacity = bi->tri_capacity;
-        uint32_t   ch[8];
-        Bx         cb[8];
-        bool       cint[8];
-        int        nc = 0;
-        Item       item{0, 0};
+        // The children.  For W == 4 every loop over them is unrolled, so
+        // each index is a compile-time constant and the arrays stay in
+        // registers (a variable index would put them in local memory).  The
+        // 8-wide node's slot assignment indexes them by variable anyway, so
+        // W == 8 keeps the short loops to nc and the indexed updates.
+        uint32_t ch[W];
+        Bx       cb[W];
+        bool     cint[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k)
+        {
+            ch[k]   = 0;
+            cint[k] = false;
+            cb[k]   = Bx{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        }
+        int  nc = 0;
+        Item item{0, 0};
         if (active)
         {
             // Binary layout: internal nodes [0, n-2], leaves [n-1, 2n-2], so
@@ -380,37 +392,83 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
             nc            = 2;
             while (nc < W)
             {
-                int   best = -1;
-                float ba   = -1.f;
-                for (int k = 0; k < nc; ++k)
-                    if (cint[k])
-                    {
-                        float a = half_area(cb[k]);
-                        if (a > ba)
+                int      best  = -1;
+                float    ba    = -1.f;
+                uint32_t cbest = 0;
+                if constexpr (W == 4)
+                {
+#pragma unroll
+                    for (int k = 0; k < W; ++k)
+                        if (k < nc && cint[k])
                         {
-                            ba   = a;
-                            best = k;
+                            const float a = half_area(cb[k]);
+                            if (a > ba)
+                            {
+                                ba    = a;
+                                best  = k;
+                                cbest = ch[k];
+                            }
+                        }
+                }
+                else
+                {
+                    for (int k = 0; k < nc; ++k)
+                        if (cint[k])
+                        {
+                            const float a = half_area(cb[k]);
+                            if (a > ba)
+                            {
+                                ba   = a;
+                                best = k;
+                            }
+                        }
+                    if (best >= 0) cbest = ch[best];
+                }
+                if (best < 0) break;
+                const BvhNode nd = load_node(nodes, cbest);
+                if constexpr (W == 4)
+                {
+                    const Bx   b0 = child_box(nd, 0), b1 = child_box(nd, 1);
+                    const bool i0 = nd.child0 < first_leaf, i1 = nd.child1 < first_leaf;
+#pragma unroll
+                    for (int k = 0; k < W; ++k)
+                    {
+                        if (k == best)
+                        {
+                            ch[k]   = nd.child0;
+                            cb[k]   = b0;
+                            cint[k] = i0;
+                        }
+                        if (k == nc)
+                        {
+                            ch[k]   = nd.child1;
+                            cb[k]   = b1;
+                            cint[k] = i1;
                         }
                     }
-                if (best < 0) break;
-                const BvhNode nd = load_node(nodes, ch[best]);
-                ch[best]   = nd.child0;
-                cb[best]   = child_box(nd, 0);
-                cint[best] = nd.child0 < first_leaf;
-                ch[nc]     = nd.child1;
-                cb[nc]     = child_box(nd, 1);
-                cint[nc]   = nd.child1 < first_leaf;
+                }
+                else
+                {
+                    ch[best]   = nd.child0;
+                    cb[best]   = child_box(nd, 0);
+                    cint[best] = nd.child0 < first_leaf;
+                    ch[nc]     = nd.child1;
+                    cb[nc]     = child_box(nd, 1);
+                    cint[nc]   = nd.child1 < first_leaf;
+                }
                 ++nc;
             }
         }
         // Leaf slots hold one triangle each (the meta byte's count field
-        // allows up to 3; one measured fastest).
-        uint32_t ccnt[8];
-        for (int k = 0; k < nc; ++k) ccnt[k] = (cint[k] || W == 4) ? 0u : 1u;  // 4-wide: no triangle array
+        // allows up to 3; one measured fastest); the 4-wide nodes have no
+        // triangle array.
+        uint32_t ccnt[W];
         uint32_t n_int = 0, n_leaf = 0;
-        for (int k = 0; k < nc; ++k)
+#pragma unroll
+        for (int k = 0; k < W; ++k)
         {
-            if (cint[k])
+            ccnt[k] = (k < nc && !cint[k] && W == 8) ? 1u : 0u;
+            if (k < nc && cint[k])
                 ++n_int;
             else
                 n_leaf += ccnt[k];
@@ -426,19 +484,21 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
             atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
             continue;
         }
-        if (W == 4 && kQ8)
+        if constexpr (W == 4 && kQ8)
         {
             // Quantised 4-wide node: the frame of the union of the child
             // boxes, bounds rounded outward as for the 8-wide node (below),
             // children numbered as in the fp32 4-wide node.
             Bvh4QNode o;
             Bx        u = cb[0];
-            for (int k = 1; k < nc; ++k)
-                for (int a = 0; a < 3; ++a)
-                {
-                    u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
-                    u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
-                }
+#pragma unroll
+            for (int k = 1; k < W; ++k)
+                if (k < nc)
+                    for (int a = 0; a < 3; ++a)
+                    {
+                        u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+                        u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+                    }
             float iv[3];
             for (int a = 0; a < 3; ++a)
             {
@@ -474,7 +534,7 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
             reinterpret_cast<Bvh4QNode*>(bi->result + bi->wide_off)[item.w] = o;
             continue;
         }
-        if (W == 4)
+        if constexpr (W == 4)
         {
             // 4-wide node: exact child boxes (read from the parents), internal
             // children numbered in slot order, leaf children by their binary
@@ -504,118 +564,121 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
             reinterpret_cast<Bvh4Node*>(bi->result + bi->wide_off)[item.w] = o;
             continue;
         }
-        // Quantisation frame.
-        WideNode w;
-        Bx       u = cb[0];
-        for (int k = 1; k < nc; ++k)
+        if constexpr (W == 8)
+        {
+            // Quantisation frame.
+            WideNode w;
+            Bx       u = cb[0];
+            for (int k = 1; k < nc; ++k)
+                for (int a = 0; a < 3; ++a)
+                {
+                    u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+                    u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+                }
+            float inv[3];
             for (int a = 0; a < 3; ++a)
             {
-                u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
-                u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+                w.p[a] = u.lo[a];
+                int e  = pick_exp(u.lo[a], u.hi[a]);
+                w.e[a] = (uint8_t)e;
+                inv[a] = __uint_as_float((uint32_t)(254 - e) << 23);
             }
-        float inv[3];
-        for (int a = 0; a < 3; ++a)
-        {
-            w.p[a] = u.lo[a];
-            int e  = pick_exp(u.lo[a], u.hi[a]);
-            w.e[a] = (uint8_t)e;
-            inv[a] = __uint_as_float((uint32_t)(254 - e) << 23);
-        }
-        w.child_base = child_base;
-        w.tri_base   = tri_base;
-        // Octant slot order: slot s holds a child on the + side of the node
-        // centre along x if s & 4, y if s & 2, z if s & 1 (greedy assignment,
-        // smallest cost first).  A ray with direction octant o visits slots
-        // i ^ o for i = 0..7, which is then roughly front to back.
-        int slot_child[8];
-        {
-            float dc[8][3];
-            for (int k = 0; k < nc; ++k)
-                for (int a = 0; a < 3; ++a)
-                    dc[k][a] = 0.5f * (cb[k].lo[a] + cb[k].hi[a]) - 0.5f * (u.lo[a] + u.hi[a]);
-            for (int s2 = 0; s2 < 8; ++s2) slot_child[s2] = -1;
-            uint32_t used = 0;
-            for (int round = 0; round < nc; ++round)
+            w.child_base = child_base;
+            w.tri_base   = tri_base;
+            // Octant slot order: slot s holds a child on the + side of the node
+            // centre along x if s & 4, y if s & 2, z if s & 1 (greedy assignment,
+            // smallest cost first).  A ray with direction octant o visits slots
+            // i ^ o for i = 0..7, which is then roughly front to back.
+            int slot_child[8];
             {
-                float bc = INFINITY;
-                int   bk = -1, bs = -1;
+                float dc[8][3];
                 for (int k = 0; k < nc; ++k)
+                    for (int a = 0; a < 3; ++a)
+                        dc[k][a] = 0.5f * (cb[k].lo[a] + cb[k].hi[a]) - 0.5f * (u.lo[a] + u.hi[a]);
+                for (int s2 = 0; s2 < 8; ++s2) slot_child[s2] = -1;
+                uint32_t used = 0;
+                for (int round = 0; round < nc; ++round)
                 {
-                    if (used >> k & 1u) continue;
-                    for (int s2 = 0; s2 < 8; ++s2)
+                    float bc = INFINITY;
+                    int   bk = -1, bs = -1;
+                    for (int k = 0; k < nc; ++k)
                     {
-                        if (slot_child[s2] >= 0) continue;
-                        const float cost = ((s2 & 4) ? -dc[k][0] : dc[k][0]) + ((s2 & 2) ? -dc[k][1] : dc[k][1]) +
-                                           ((s2 & 1) ? -dc[k][2] : dc[k][2]);
-                        if (cost < bc || bk < 0)
+                        if (used >> k & 1u) continue;
+                        for (int s2 = 0; s2 < 8; ++s2)
                         {
-                            bc = cost;
-                            bk = k;
-                            bs = s2;
+                            if (slot_child[s2] >= 0) continue;
+                            const float cost = ((s2 & 4) ? -dc[k][0] : dc[k][0]) + ((s2 & 2) ? -dc[k][1] : dc[k][1]) +
+                                               ((s2 & 1) ? -dc[k][2] : dc[k][2]);
+                            if (cost < bc || bk < 0)
+                            {
+                                bc = cost;
+                                bk = k;
+                                bs = s2;
+                            }
+                        }
+                    }
+                    slot_child[bs] = bk;
+                    used |= 1u << bk;
+                }
+            }
+            uint8_t  imask = 0;
+            uint32_t ri = 0, rl = 0;
+            for (int slot = 0; slot < 8; ++slot)
+            {
+                const int k = slot_child[slot];
+                if (k >= 0)
+                {
+                    for (int a = 0; a < 3; ++a)
+                    {
+                        float ql = floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], w.p[a]), inv[a]));
+                        float qh = ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], w.p[a]), inv[a]));
+                        w.qlo[a][slot] = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
+                        w.qhi[a][slot] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
+                    }
+                    if (cint[k])
+                    {
+                        imask |= (uint8_t)(1u << slot);
+                        w.meta[slot] = (uint8_t)(0x80u | ri);
+                        qout[qpos + ri] = Item{ch[k], child_base + ri};
+                        ++ri;
+                    }
+                    else
+                    {
+                        w.meta[slot] = (uint8_t)((ccnt[k] << 5) | rl);
+                        for (uint32_t j = 0; j < ccnt[k]; ++j)
+                        {
+                            BvhNode lf = load_node(nodes, ch[k]);
+                            WideTri t;
+                            t.v0[0] = lf.a0[0];
+                            t.v0[1] = lf.a0[1];
+                            t.v0[2] = lf.a0[2];
+                            t.prim  = lf.child1;
+                            t.v1[0] = lf.a1[0];
+                            t.v1[1] = lf.a1[1];
+                            t.v1[2] = lf.a1[2];
+                            t.pad1  = 0;
+                            t.v2[0] = lf.b0[0];
+                            t.v2[1] = lf.b0[1];
+                            t.v2[2] = lf.b0[2];
+                            t.pad2  = 0;
+                            wt[tri_base + rl] = t;
+                            ++rl;
                         }
                     }
                 }
-                slot_child[bs] = bk;
-                used |= 1u << bk;
-            }
-        }
-        uint8_t  imask = 0;
-        uint32_t ri = 0, rl = 0;
-        for (int slot = 0; slot < 8; ++slot)
-        {
-            const int k = slot_child[slot];
-            if (k >= 0)
-            {
-                for (int a = 0; a < 3; ++a)
-                {
-                    float ql = floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], w.p[a]), inv[a]));
-                    float qh = ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], w.p[a]), inv[a]));
-                    w.qlo[a][slot] = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
-                    w.qhi[a][slot] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
-                }
-                if (cint[k])
-                {
-                    imask |= (uint8_t)(1u << slot);
-                    w.meta[slot] = (uint8_t)(0x80u | ri);
-                    qout[qpos + ri] = Item{ch[k], child_base + ri};
-                    ++ri;
-                }
                 else
                 {
-                    w.meta[slot] = (uint8_t)((ccnt[k] << 5) | rl);
-                    for (uint32_t j = 0; j < ccnt[k]; ++j)
+                    w.meta[slot] = 0;
+                    for (int a = 0; a < 3; ++a)
                     {
-                        BvhNode lf = load_node(nodes, ch[k]);
-                        WideTri t;
-                        t.v0[0] = lf.a0[0];
-                        t.v0[1] = lf.a0[1];
-                        t.v0[2] = lf.a0[2];
-                        t.prim  = lf.child1;
-                        t.v1[0] = lf.a1[0];
-                        t.v1[1] = lf.a1[1];
-                        t.v1[2] = lf.a1[2];
-                        t.pad1  = 0;
-                        t.v2[0] = lf.b0[0];
-                        t.v2[1] = lf.b0[1];
-                        t.v2[2] = lf.b0[2];
-                        t.pad2  = 0;
-                        wt[tri_base + rl] = t;
-                        ++rl;
+                        w.qlo[a][slot] = 0;
+                        w.qhi[a][slot] = 0;
                     }
                 }
             }
-            else
-            {
-                w.meta[slot] = 0;
-                for (int a = 0; a < 3; ++a)
-                {
-                    w.qlo[a][slot] = 0;
-                    w.qhi[a][slot] = 0;
-                }
-            }
+            w.imask       = imask;
+            wn[item.w]    = w;
         }
-        w.imask       = imask;
-        wn[item.w]    = w;
     }
 }
 
