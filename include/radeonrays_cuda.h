@@ -30,11 +30,11 @@ typedef enum
      * bounds and a 48-byte triangle array. */
     RR_CUDA_NODE_FORMAT_WIDE8 = 1,
     /* Binary nodes plus 4-wide 128-byte nodes with exact fp32 child boxes
-     * whose leaf children are the binary leaf nodes (the default). */
+     * whose leaf children are the binary leaf nodes. */
     RR_CUDA_NODE_FORMAT_BVH4 = 2,
     /* The node width rrCudaAutotuneNodeFormat picked for meshes of the same
      * size class (triangle-count octave) on this GPU, from this context or
-     * the RR_CUDA_TUNE_CACHE file; BVH4 when none was picked.  Memory
+     * the RR_CUDA_TUNE_CACHE file; BVH4Q8 when none was picked.  Memory
      * requirements with AUTO are sized for any of the wide formats.  A fused build
      * (rrCudaCmdBuildGeometries) takes its largest mesh's width. */
     RR_CUDA_NODE_FORMAT_AUTO = 3,
@@ -43,12 +43,13 @@ typedef enum
      * rounded outward, so every quantised box contains the exact one; leaf
      * children are the binary leaf nodes, and the traversal re-tests each
      * leaf triangle's exact box with the reference's slab arithmetic before
-     * its triangle test.  Half the bytes of a BVH4 node per fetch. */
+     * its triangle test.  Half the bytes of a BVH4 node per fetch.  The
+     * default. */
     RR_CUDA_NODE_FORMAT_BVH4Q8 = 4
 } RRCudaNodeFormat;
 
 /* Passed through RRBuildOptions::backend_specific_info.  A null
- * backend_specific_info selects the defaults (BVH4, 30-bit Morton codes). */
+ * backend_specific_info selects the defaults (BVH4Q8, 30-bit Morton codes). */
 typedef struct
 {
     uint32_t struct_size;   /* sizeof(RRCudaBuildOptions) */
@@ -61,10 +62,10 @@ typedef struct
 typedef enum
 {
     /* The default: on a triangle geometry buffer with 4-wide nodes
-     * (RR_CUDA_NODE_FORMAT_BVH4, the default build format) the 4-wide kernel
-     * (RR_CUDA_TRAVERSAL_BVH4); on every other buffer (scenes included) the
-     * persistent binary kernel, whose hits are bit-identical to
-     * RR_CUDA_TRAVERSAL_BINARY.  rrCudaAutotuneTraversal replaces it with the
+     * (RR_CUDA_NODE_FORMAT_BVH4Q8, the default build format, or _BVH4) the
+     * 4-wide kernel (RR_CUDA_TRAVERSAL_BVH4); on every other buffer (scenes
+     * included) the persistent binary kernel, whose hits are bit-identical
+     * to RR_CUDA_TRAVERSAL_BINARY.  rrCudaAutotuneTraversal replaces it with the
      * fastest kernel for a workload. */
     RR_CUDA_TRAVERSAL_AUTO = 0,
     /* One thread per ray, 64-byte binary nodes, reference visit order. */
@@ -329,7 +330,7 @@ RR_API RRError rrCudaCmdIntersectHostBuffers(RRContext              context,
  * persistent launch whose lanes take rays from all requests.  When the
  * context's traversal option is RR_CUDA_TRAVERSAL_AUTO or _BVH4 and every
  * request with rays has a triangle geometry with 4-wide nodes of one form
- * (all RR_CUDA_NODE_FORMAT_BVH4, the default, or all _BVH4Q8) or no
+ * (all RR_CUDA_NODE_FORMAT_BVH4Q8, the default, or all _BVH4) or no
  * triangles, each request is traced exactly like rrCmdIntersect with
  * RR_CUDA_TRAVERSAL_BVH4; otherwise
  * exactly like rrCmdIntersect with RR_CUDA_TRAVERSAL_BINARY (the reference's

@@ -437,7 +437,7 @@ void record(CommandStream* cs, Op op, bool owns = false)
 
 struct BuildParams
 {
-    uint32_t format      = RR_CUDA_NODE_FORMAT_BVH4;
+    uint32_t format      = RR_CUDA_NODE_FORMAT_BVH4Q8;  // the default: 4-wide nodes with 8-bit bounds
     uint32_t bits        = 30;
     bool     restructure = false;
 };
@@ -529,7 +529,7 @@ uint32_t resolve_format(Context* ctx, uint32_t requested, uint32_t n)
     auto              hit = ctx->fmt_choice.find(key);
     if (hit == ctx->fmt_choice.end())
     {
-        uint32_t fmt = RR_CUDA_NODE_FORMAT_BVH4;
+        uint32_t fmt = RR_CUDA_NODE_FORMAT_BVH4Q8;  // the default format when nothing was tuned
         if (const char* path = std::getenv("RR_CUDA_TUNE_CACHE"))
             if (FILE* f = std::fopen(path, "r"))
             {

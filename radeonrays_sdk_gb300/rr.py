@@ -279,14 +279,14 @@ class Context:
         return bi, mesh
 
     @staticmethod
-    def _options(node_format=RR_CUDA_NODE_FORMAT_BVH4, morton_bits=30, quality=False):
+    def _options(node_format=RR_CUDA_NODE_FORMAT_BVH4Q8, morton_bits=30, quality=False):
         """quality=True clears RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD: the build adds the treelet restructure."""
         cuda_opts = RRCudaBuildOptions(C.sizeof(RRCudaBuildOptions), node_format, morton_bits, 0)
         flags = 0 if quality else RR_BUILD_FLAG_BITS_PREFER_FAST_BUILD
         opts = RRBuildOptions(flags, C.cast(C.pointer(cuda_opts), C.c_void_p))
         return opts, cuda_opts
 
-    def geometry_requirements(self, ntri, node_format=RR_CUDA_NODE_FORMAT_BVH4, morton_bits=30, nvert=0, stride=12,
+    def geometry_requirements(self, ntri, node_format=RR_CUDA_NODE_FORMAT_BVH4Q8, morton_bits=30, nvert=0, stride=12,
                               index16=False):
         bi, mesh = self._build_input(None, nvert, stride, None, ntri, index16)
         opts, keep = self._options(node_format, morton_bits)
@@ -295,7 +295,7 @@ class Context:
               "rrGetGeometryBuildMemoryRequirements")
         return req.temporary_build_buffer_size, req.result_buffer_size
 
-    def build_geometry(self, vertices, indices, node_format=RR_CUDA_NODE_FORMAT_BVH4, morton_bits=30,
+    def build_geometry(self, vertices, indices, node_format=RR_CUDA_NODE_FORMAT_BVH4Q8, morton_bits=30,
                        stride=None, stream=None, scratch=None, result=None, quality=False):
         """vertices: cuda float32 tensor (V, k>=3) or flat; indices: cuda int32/int16 (T, 3).
         quality=True: build flags without PREFER_FAST_BUILD (treelet restructure)."""
@@ -379,7 +379,7 @@ class Context:
             self.release_stream(cs)
         return result
 
-    def build_geometries(self, meshes, node_format=RR_CUDA_NODE_FORMAT_BVH4, morton_bits=30, stream=None,
+    def build_geometries(self, meshes, node_format=RR_CUDA_NODE_FORMAT_BVH4Q8, morton_bits=30, stream=None,
                          api="batch", quality=False):
         """Build many meshes [(vertices (V, 3) float32, indices (T, 3) int32), ...] (cuda tensors).
 

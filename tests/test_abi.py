@@ -76,10 +76,15 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts), C.byref(req_b)) == 0
     nodes = (2 * 1000 - 1) * 64
     assert req_b.result_buffer_size == (nodes + 255) // 256 * 256 + 256
-    # Default (null options): binary nodes + trailer + 4-wide nodes of 128 B,
-    # capacity (n-1)//3 + n//3 + 1, 256-byte aligned.
+    # Default (null options): binary nodes + trailer + quantised 4-wide nodes
+    # of 64 B, capacity (n-1)//3 + n//3 + 1, 256-byte aligned; BVH4 has 128 B.
     cap4 = (1000 - 1) // 3 + 1000 // 3 + 1
-    assert req.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 128 + 255) // 256 * 256
+    assert req.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 64 + 255) // 256 * 256
+    f4_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_BVH4, 30, 0)
+    opts4 = rr.RRBuildOptions(1, C.cast(C.pointer(f4_opts), C.c_void_p))
+    req_4 = rr.RRMemoryRequirements()
+    assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(opts4), C.byref(req_4)) == 0
+    assert req_4.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 128 + 255) // 256 * 256
     w8_opts = rr.RRCudaBuildOptions(C.sizeof(rr.RRCudaBuildOptions), rr.RR_CUDA_NODE_FORMAT_WIDE8, 30, 0)
     opts8 = rr.RRBuildOptions(1, C.cast(C.pointer(w8_opts), C.c_void_p))
     req_8 = rr.RRMemoryRequirements()
@@ -96,7 +101,8 @@ def test_memory_requirements_host_logic(rrlib, tmp_path):
     assert rrlib.rrGetGeometryBuildMemoryRequirements(fake, C.byref(bi), C.byref(optsq), C.byref(req_q)) == 0
     cap4 = (1000 - 1) // 3 + 1000 // 3 + 1  # 64-byte quantised 4-wide nodes
     assert req_q.result_buffer_size == ((nodes + 255) // 256 * 256 + 256 + cap4 * 64 + 255) // 256 * 256
-    assert req_a.result_buffer_size == max(req.result_buffer_size, req_8.result_buffer_size,
+    assert req_q.result_buffer_size == req.result_buffer_size  # the default is BVH4Q8
+    assert req_a.result_buffer_size == max(req_4.result_buffer_size, req_8.result_buffer_size,
                                            req_q.result_buffer_size)
     assert req_a.temporary_build_buffer_size == max(req.temporary_build_buffer_size,
                                                     req_8.temporary_build_buffer_size,

@@ -106,19 +106,21 @@ def test_node_range_is_reported(ctx):
         assert ctx.device_errors() & NODE_RANGE, trav
         ctx.intersect(res, rd)
         assert ctx.device_errors() == 0, trav
-    # 4-wide nodes: an internal reference past the 4-wide array, and a leaf
-    # reference past the binary leaves.
-    res4 = ctx.build_geometry(to_dev(v), to_dev(i))
-    off = int(trailer_of(res4, n)["wide_nodes_off"])
-    for ref in (0x7FFFFFF0, 0x80000000 | (2 * n + 5)):
-        bad4 = _registered_copy(ctx, res4, n)
-        child = bad4[off + 96: off + 112].view(torch.int32)
-        child[:] = torch.tensor(np.array([ref] * 4, np.uint32).view(np.int32), device="cuda")
-        ctx.set_traversal(4)
-        ctx.intersect(bad4, rd)
-        assert ctx.device_errors() & NODE_RANGE, hex(ref)
-        ctx.intersect(res4, rd)
-        assert ctx.device_errors() == 0
+    # 4-wide nodes (fp32: child words at byte 96 of a 128-byte node; 8-bit:
+    # at byte 16 of a 64-byte node): an internal reference past the 4-wide
+    # array, and a leaf reference past the binary leaves.
+    for fmt, coff in ((2, 96), (4, 16)):
+        res4 = ctx.build_geometry(to_dev(v), to_dev(i), node_format=fmt)
+        off = int(trailer_of(res4, n)["wide_nodes_off"])
+        for ref in (0x7FFFFFF0, 0x80000000 | (2 * n + 5)):
+            bad4 = _registered_copy(ctx, res4, n)
+            child = bad4[off + coff: off + coff + 16].view(torch.int32)
+            child[:] = torch.tensor(np.array([ref] * 4, np.uint32).view(np.int32), device="cuda")
+            ctx.set_traversal(4)
+            ctx.intersect(bad4, rd)
+            assert ctx.device_errors() & NODE_RANGE, (fmt, hex(ref))
+            ctx.intersect(res4, rd)
+            assert ctx.device_errors() == 0
     ctx.set_traversal(0)
 
 
