@@ -284,9 +284,9 @@ __device__ __forceinline__ void b4_start(B4Ray& s, const Ray& r)
 // One step; returns true when the ray is finished (stack empty, or a hit
 // accepted by an any-hit query).  nf / tf count node and leaf fetches.
 // kRuntime: the query is `any` (requests of both kinds in one launch).
-// kQ8: the nodes are Bvh4QNode (quantised bounds); each leaf triangle is then
-// first tested on its exact box (min / max of its vertices, the box its
-// binary parent holds) with the reference's slab arithmetic, so a triangle
+// kQ8: the nodes are Bvh4QNode (quantised bounds); a leaf triangle's hit
+// then counts only if its exact box (min / max of its vertices, the box its
+// binary parent holds) passes the reference's slab test too, so a triangle
 // whose exact box the reference culls is not reached through the larger
 // quantised box either.  With kPrecise the nodes take the robust test and the
 // leaves go straight to the precise triangle test (no box test decides a hit
@@ -312,18 +312,19 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
         const float4  a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
         ++tf;
         const F3 v0 = f3(a.x, a.y, a.z), v1 = f3(b.x, b.y, b.z), v2 = f3(c.x, c.y, c.z);
-        bool     reach = true;
-        if (kQ8 && !kPrecise)  // the precise test needs no re-test: its box test is conservative
+        float t = kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct) : isect_tri(s.ray, v0, v1, v2, s.ct);
+        // The exact-box re-test decides only whether a triangle hit counts,
+        // so it runs after the triangle test and only on a hit (the same
+        // outcome as testing the box first; the precise test needs no
+        // re-test, its box test being conservative).
+        if (kQ8 && !kPrecise && t < s.ct)
         {
             float b0, b1;
             isect_box(f3(b4_min3(v0.x, v1.x, v2.x), b4_min3(v0.y, v1.y, v2.y), b4_min3(v0.z, v1.z, v2.z)),
                       f3(b4_max3(v0.x, v1.x, v2.x), b4_max3(v0.y, v1.y, v2.y), b4_max3(v0.z, v1.z, v2.z)), s.inv,
                       s.oxi, s.ct, s.ray.tmin, b0, b1);
-            reach = b0 <= b1;
+            if (!(b0 <= b1)) t = s.ct;
         }
-        const float t = !reach   ? s.ct
-                        : kPrecise ? isect_tri_precise(s.ray, v0, v1, v2, s.ct)
-                                   : isect_tri(s.ray, v0, v1, v2, s.ct);
         if (t < s.ct)
         {
             s.ct   = t;

@@ -56,8 +56,8 @@ __device__ __forceinline__ void set_frame(S4Ray& s, const Ray& r)
 
 // One step; true when the ray is finished.
 // kQ8: the BLASes' 4-wide nodes have 8-bit bounds (Bvh4QNode); as in the
-// single-level kernel, a leaf triangle is first tested on its exact box with
-// the reference's slab arithmetic.
+// single-level kernel, a leaf triangle's hit counts only if its exact box
+// passes the reference's slab test too.
 template <bool kAny, bool kQ8>
 __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint32_t gid, const PStack& st,
                                         uint32_t& nf)
@@ -133,18 +133,15 @@ __device__ __forceinline__ bool s4_step(S4Ray& s, const SceneTraceArgs& sa, uint
         {
             const float4* p = reinterpret_cast<const float4*>(s.blas + idx);
             const float4  v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
-            bool          reach = true;
-            if (kQ8)
+            float t = isect_tri(s.ray, f3(v0.x, v0.y, v0.z), f3(v1.x, v1.y, v1.z), f3(v2.x, v2.y, v2.z), s.ct);
+            if (kQ8 && t < s.ct)  // exact-box re-test of a hit (see b4_step)
             {
                 float b0, b1;
                 isect_box(f3(b4_min3(v0.x, v1.x, v2.x), b4_min3(v0.y, v1.y, v2.y), b4_min3(v0.z, v1.z, v2.z)),
                           f3(b4_max3(v0.x, v1.x, v2.x), b4_max3(v0.y, v1.y, v2.y), b4_max3(v0.z, v1.z, v2.z)), s.inv,
                           s.oxi, s.ct, s.ray.tmin, b0, b1);
-                reach = b0 <= b1;
+                if (!(b0 <= b1)) t = s.ct;
             }
-            const float t = reach ? isect_tri(s.ray, f3(v0.x, v0.y, v0.z), f3(v1.x, v1.y, v1.z),
-                                              f3(v2.x, v2.y, v2.z), s.ct)
-                                  : s.ct;
             if (t < s.ct)
             {
                 s.ct    = t;
