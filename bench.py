@@ -668,7 +668,14 @@ def run_ours(args):
                      "fallback 6800 GB/s",
                      "alg_bytes_per_ray": c["alg_bytes"] / R,
                      "node_fetches_per_ray": c["stats"]["node_fetches"] / R,
-                     "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R},
+                     "tri_fetches_per_ray": c["stats"]["triangle_fetches"] / R,
+                     "bytes_per_node_fetch": {rr.RR_CUDA_TRAVERSAL_WIDE: 80,
+                                              rr.RR_CUDA_TRAVERSAL_BVH4: 64 if cfmt == rr.RR_CUDA_NODE_FORMAT_BVH4Q8
+                                              else 128}.get(c["trav"], 64) if key == "chosen" else 64,
+                     "note": "achieved = algorithmic bytes (ray, hit, node and leaf fetches at their sizes) per "
+                             "launch / launch time; the traversal kernels are latency- and issue-bound (DRAM "
+                             "traffic well below the algorithmic bytes: nodes hit in L1/L2), so frac is not "
+                             "their limit, and 64-byte 8-bit nodes lower it while raising throughput"},
         "clocks": c["clocks"], "gpu_launches": args.steps, "build": build, "traversal": key,
         "chosen_format": {"format": format_tuned or args.chosen_format,
                           "selected_by": "rrCudaAutotuneNodeFormat" if format_tuned else "command line"},

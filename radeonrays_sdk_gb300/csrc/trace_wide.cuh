@@ -258,17 +258,19 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
             // The binary path reaches a triangle only through its exact box
             // (its slot in the binary parent: the refit's min / max of the
             // vertices) and the reference's fp32 slab test.  The quantised
-            // slot box here is larger, so the exact box is tested first: a
-            // grazing ray that the fp32 slab test rejects on the exact box
-            // does not reach the triangle here either.
-            float b0, b1;
-            isect_box(f3(fminf(fminf(A.x, B.x), C.x), fminf(fminf(A.y, B.y), C.y), fminf(fminf(A.z, B.z), C.z)),
-                      f3(fmaxf(fmaxf(A.x, B.x), C.x), fmaxf(fmaxf(A.y, B.y), C.y), fmaxf(fmaxf(A.z, B.z), C.z)),
-                      s.inv, s.oxi, s.ct, s.ray.tmin, b0, b1);
-            if (b0 > b1) continue;
+            // slot box here is larger, so a hit counts only if the exact box
+            // passes that test too: a grazing ray that the fp32 slab test
+            // rejects on the exact box does not hit the triangle here either.
+            // (The box decides only whether a hit counts, so it is tested
+            // after the triangle, on hits only.)
             const float t = isect_tri(s.ray, f3(A.x, A.y, A.z), f3(B.x, B.y, B.z), f3(C.x, C.y, C.z), s.ct);
             if (t < s.ct)
             {
+                float b0, b1;
+                isect_box(f3(fminf(fminf(A.x, B.x), C.x), fminf(fminf(A.y, B.y), C.y), fminf(fminf(A.z, B.z), C.z)),
+                          f3(fmaxf(fmaxf(A.x, B.x), C.x), fmaxf(fmaxf(A.y, B.y), C.y), fmaxf(fmaxf(A.z, B.z), C.z)),
+                          s.inv, s.oxi, s.ct, s.ray.tmin, b0, b1);
+                if (b0 > b1) continue;
                 s.ct   = t;
                 s.best = ti;
                 if (kAny) done = true;
