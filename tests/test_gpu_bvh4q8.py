@@ -137,3 +137,35 @@ def test_bvh4q8_precise_mode(ctx, orc):
     ctx.set_traversal(0)
     assert np.array_equal(ga[:, 2] != INVALID, wa[:, 2] != INVALID)
     assert ctx.device_errors() == 0
+
+
+def test_default_build_is_bvh4q8_and_auto_runs_the_4wide_kernel(ctx, orc):
+    """A build with null RRBuildOptions (what a drop-in client passes) makes
+    8-bit 4-wide nodes, and the default traversal option runs the 4-wide
+    kernel on them: hit flags are the reference's."""
+    import ctypes as C
+    import torch
+    from gpu_util import to_dev
+    from radeonrays_sdk_gb300 import rr, scenes
+    v, i, rays = scenes.config1(grid=129, nrays=1 << 15)
+    n = i.shape[0]
+    vd, idd = to_dev(v), to_dev(i)
+    bi, mesh = ctx._build_input(ctx.ptr(vd), v.shape[0], 12, ctx.ptr(idd), n, False)
+    req = rr.RRMemoryRequirements()
+    rr.check(ctx.L.rrGetGeometryBuildMemoryRequirements(ctx.ctx, C.byref(bi), None, C.byref(req)), "requirements")
+    assert req.result_buffer_size == ctx.geometry_requirements(n, rr.RR_CUDA_NODE_FORMAT_BVH4Q8, 30, v.shape[0], 12)[1]
+    scratch = torch.empty(req.temporary_build_buffer_size, dtype=torch.uint8, device="cuda")
+    res = torch.empty(req.result_buffer_size, dtype=torch.uint8, device="cuda")
+    cs = ctx.command_stream()
+    rr.check(ctx.L.rrCmdBuildGeometry(ctx.ctx, rr.RR_BUILD_OPERATION_BUILD, C.byref(bi), None, ctx.ptr(scratch),
+                                      ctx.ptr(res), cs), "rrCmdBuildGeometry")
+    ctx.submit(cs)
+    ctx.release_stream(cs)
+    assert trailer_of(res, n)["node_format"] == Q8_FORMAT
+    check_conservative(res, v, i)
+    nodes, _, _ = orc.build_mesh(v, i)
+    want = orc.trace(nodes, rays, threads=16)
+    got = trace(ctx, res, rays, traversal=0)
+    assert np.array_equal(got, trace(ctx, res, rays, traversal=BVH4))
+    compare(orc, rays, got, want, v, i)
+    assert ctx.device_errors() == 0
