@@ -551,6 +551,27 @@ __device__ __forceinline__ void best_split(const TreeletDp& t, uint32_t s, uint3
     }
 }
 
+// An internal node as one 64-byte load: its children and their boxes (the
+// copies its own slots hold, which the refit and every restructure keep equal
+// to the child's own box), and its parent.
+struct NodeLd
+{
+    uint32_t c0, c1, parent;
+    Bx3      b0, b1;
+};
+__device__ __forceinline__ NodeLd load_node_cg(const BvhNode* nodes, uint32_t x)
+{
+    const float4* p4 = reinterpret_cast<const float4*>(nodes + x);
+    const float4  w0 = __ldcg(p4), w1 = __ldcg(p4 + 1), w2 = __ldcg(p4 + 2), w3 = __ldcg(p4 + 3);
+    NodeLd        d;
+    d.c0     = __float_as_uint(w0.w);
+    d.c1     = __float_as_uint(w1.w);
+    d.parent = __float_as_uint(w2.w);
+    d.b0     = Bx3{f3(w0.x, w0.y, w0.z), f3(w1.x, w1.y, w1.z)};
+    d.b1     = Bx3{f3(w2.x, w2.y, w2.z), f3(w3.x, w3.y, w3.z)};
+    return d;
+}
+
 // Restructure the treelet rooted at internal node x with the whole warp (all
 // 32 lanes call it with the same x).  Same treelet, same tables, same tie rules
 // as the sequential restatement (oracle rro_restructure), so the tree is
@@ -558,16 +579,24 @@ __device__ __forceinline__ void best_split(const TreeletDp& t, uint32_t s, uint3
 // spread over the lanes; subsets are costed by size, one lane per subset, and
 // the largest subset (the whole treelet) by all lanes with a min reduction
 // that keeps the first minimum in enumeration order; lane 0 rebuilds.
+// Latency: forming the treelet costs one node load per expansion (the child
+// boxes come from the parent's slots), and the rebuild writes each new node
+// whole from boxes it unions in registers, bottom-up, exactly as the child's
+// own node would give them (child_box).
 __device__ void restructure_treelet_warp(BvhNode* nodes, uint32_t n, uint32_t x, TreeletDp& t, uint32_t lane)
 {
     uint32_t leaf[7], inner[6];
-    float    la[7];
+    float    la[7], ia[6];
+    Bx3      bx[7];
     int      nl = 2, ni = 1;
-    inner[0]    = x;
-    leaf[0]     = __ldcg(&nodes[x].child0);
-    leaf[1]     = __ldcg(&nodes[x].child1);
-    la[0]       = half_area3(box_of(nodes, leaf[0]));
-    la[1]       = half_area3(box_of(nodes, leaf[1]));
+    const NodeLd r = load_node_cg(nodes, x);
+    inner[0]       = x;
+    leaf[0]        = r.c0;
+    leaf[1]        = r.c1;
+    bx[0]          = r.b0;
+    bx[1]          = r.b1;
+    la[0]          = half_area3(bx[0]);
+    la[1]          = half_area3(bx[1]);
     while (nl < 7)
     {
         int   best = -1;
@@ -580,17 +609,19 @@ __device__ void restructure_treelet_warp(BvhNode* nodes, uint32_t n, uint32_t x,
             }
         if (best < 0) break;
         const uint32_t c = leaf[best];
+        const NodeLd   d = load_node_cg(nodes, c);
+        ia[ni]           = la[best];  // the area of c's box, which its parent's slot holds
         inner[ni++]      = c;
-        leaf[best]       = __ldcg(&nodes[c].child0);
-        la[best]         = half_area3(box_of(nodes, leaf[best]));
-        leaf[nl]         = __ldcg(&nodes[c].child1);
-        la[nl]           = half_area3(box_of(nodes, leaf[nl]));
+        leaf[best]       = d.c0;
+        bx[best]         = d.b0;
+        la[best]         = half_area3(d.b0);
+        leaf[nl]         = d.c1;
+        bx[nl]           = d.b1;
+        la[nl]           = half_area3(d.b1);
         ++nl;
     }
     if (nl < 3) return;  // warp-uniform: every lane formed the same treelet
     const uint32_t full = (1u << nl) - 1;
-    Bx3            bx[7];
-    for (int k = 0; k < nl; ++k) bx[k] = box_of(nodes, leaf[k]);
     for (uint32_t s = lane + 1; s <= full; s += 32)
     {
         const int lo = __ffs(s) - 1;
@@ -649,40 +680,58 @@ __device__ void restructure_treelet_warp(BvhNode* nodes, uint32_t n, uint32_t x,
     if (lane == 0)
     {
         float cur = t.area[full];
-        for (int k = 1; k < ni; ++k) cur += half_area3(box_of(nodes, inner[k]));
+        for (int k = 1; k < ni; ++k) cur += ia[k];
         for (int k = 0; k < nl; ++k) cur += la[k];
         if (t.cost[full] < cur)
         {
-            uint32_t sset[6], sslot[6], order[6];
-            int      sp = 0, next = 1, no = 0;
-            sset[sp]    = full;
-            sslot[sp++] = x;
+            // New topology, top-down: node k of the rebuild takes slot
+            // inner[k] (k = 0 is x), covers the treelet leaves in subset
+            // sub[k], and has children c0/c1 (a slot, or a treelet leaf).
+            // Slots go to the inner nodes in the order of a depth-first walk
+            // with a stack (the order the oracle's rebuild assigns them).
+            uint32_t sub[6], c0[6], c1[6], par[6];
+            int      kid0[6], kid1[6];  // rebuild index of an inner child, -1 for a treelet leaf
+            int      stk[6], sp = 0, no = 1;
+            sub[0]    = full;
+            par[0]    = r.parent;
+            stk[sp++] = 0;
             while (sp > 0)
             {
-                --sp;
-                const uint32_t s = sset[sp], slot = sslot[sp];
-                order[no++]      = slot;
-                const uint32_t sides[2] = {t.part[s], s ^ t.part[s]};
-                uint32_t       ch[2];
-                for (int k = 0; k < 2; ++k)
+                const int k = stk[--sp];
+                const uint32_t sides[2] = {t.part[sub[k]], sub[k] ^ t.part[sub[k]]};
+                for (int e = 0; e < 2; ++e)
                 {
-                    const uint32_t u = sides[k];
+                    const uint32_t u = sides[e];
+                    uint32_t       c;
+                    int            kid = -1;
                     if ((u & (u - 1)) == 0)
-                        ch[k] = leaf[__ffs(u) - 1];
+                        c = leaf[__ffs(u) - 1];
                     else
                     {
-                        ch[k]       = inner[next++];
-                        sset[sp]    = u;
-                        sslot[sp++] = ch[k];
+                        kid       = no++;
+                        c         = inner[kid];
+                        sub[kid]  = u;
+                        par[kid]  = inner[k];
+                        stk[sp++] = kid;
                     }
+                    (e ? c1 : c0)[k]     = c;
+                    (e ? kid1 : kid0)[k] = kid;
                 }
-                __stcg(&nodes[slot].child0, ch[0]);
-                __stcg(&nodes[slot].child1, ch[1]);
-                __stcg(&nodes[ch[0]].parent, slot);
-                __stcg(&nodes[ch[1]].parent, slot);
             }
-            __threadfence();
-            for (int k = no - 1; k >= 0; --k) store_child_boxes(nodes, order[k]);
+            // Boxes bottom-up (children have larger rebuild indices), each
+            // node written whole; treelet leaves take their new parent.
+            Bx3 nb[6];
+            for (int k = no - 1; k >= 0; --k)
+            {
+                const Bx3 l0 = kid0[k] < 0 ? bx[__ffs(t.part[sub[k]]) - 1] : nb[kid0[k]];
+                const Bx3 l1 = kid1[k] < 0 ? bx[__ffs(sub[k] ^ t.part[sub[k]]) - 1] : nb[kid1[k]];
+                nb[k]        = Bx3{vmin(l0.lo, l1.lo), vmax(l0.hi, l1.hi)};
+                // Every internal node under the node being restructured has
+                // been climbed through in this pass, so its flag is 1.
+                store_boxes4(nodes, inner[k], l0.lo, l0.hi, l1.lo, l1.hi, c0[k], c1[k], par[k], 1u);
+                if (kid0[k] < 0) __stcg(&nodes[c0[k]].parent, inner[k]);
+                if (kid1[k] < 0) __stcg(&nodes[c1[k]].parent, inner[k]);
+            }
             __threadfence();
         }
     }
