@@ -231,12 +231,35 @@ def describe(args, ntri):
             "parallelism": "replicas (rays sharded per GPU, BVH replicated)"}
 
 
+def cpu_model():
+    """The host CPU's model name (or its part and implementer codes on Arm)."""
+    try:
+        text = open("/proc/cpuinfo").read()
+    except OSError:
+        return None
+    for key in ("model name", "Model Name"):
+        for ln in text.splitlines():
+            if ln.startswith(key):
+                return ln.split(":", 1)[1].strip()
+    parts = {ln.split(":", 1)[0].strip(): ln.split(":", 1)[1].strip() for ln in text.splitlines() if ":" in ln}
+    if "CPU part" in parts:
+        return f"{os.uname().machine} CPU implementer {parts.get('CPU implementer')} part {parts['CPU part']}"
+    return os.uname().machine
+
+
 def cpu_baseline(v, i, rays, seconds, threads=None):
-    """Oracle port of isect.comp on the host cores over a bounded ray sample."""
+    """Oracle port of isect.comp on the host cores over a bounded ray sample,
+    and the oracle's C++ LBVH restatement (the reference has no CPU builder)
+    timed on one thread and on all cores."""
     import oracle
     oracle.build()
     threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.build_mesh(v, i, threads=1)
+    build_1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
     nodes, _, _ = oracle.build_mesh(v, i, threads=threads)
+    build_n = time.perf_counter() - t0
     n = 1 << 14
     t0 = time.perf_counter()
     oracle.trace(nodes, rays[:n], threads=threads)
@@ -245,8 +268,15 @@ def cpu_baseline(v, i, rays, seconds, threads=None):
     t0 = time.perf_counter()
     oracle.trace(nodes, rays[:target], threads=threads)
     dt = time.perf_counter() - t0
+    ntri = i.shape[0]
     return {"value": target / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"first {target:,} rays of the workload, closest hit, binary nodes built by the oracle"}, nodes
+            "sample": f"first {target:,} rays of the workload, closest hit, binary nodes built by the oracle",
+            "cpu_model": cpu_model(),
+            "build": {"kind": "port (the oracle's C++ LBVH restatement: bounds, Morton codes, stable sort, "
+                              "Karras emit, refit)",
+                      "ms_1_thread": 1e3 * build_1, "mtris_s_1_thread": ntri / build_1 / 1e6,
+                      "ms_all_cores": 1e3 * build_n, "mtris_s_all_cores": ntri / build_n / 1e6,
+                      "cores": threads}}, nodes
 
 
 def precision_report(v, i, rays, hits, nodes, n=1 << 20, precise=False):
