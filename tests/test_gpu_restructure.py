@@ -71,3 +71,22 @@ def test_quality_build_then_update(ctx, orc):
     ctx.update_geometry(to_dev(v2), to_dev(i), res)
     want = orc.fit(_oracle_quality(orc, v, i), v2, i)
     assert same_nodes(nodes_of(res, 3000), want)
+
+
+@pytest.mark.parametrize("bits", [30, 63])
+def test_quality_build_default_format_and_key_widths(ctx, orc, bits):
+    """The quality build in the default node format (8-bit 4-wide nodes) and
+    with either key width: binary nodes bit-identical to the oracle's, and
+    the collapsed nodes conservative over the restructured tree."""
+    from radeonrays_sdk_gb300 import rr, scenes
+    from test_gpu_bvh4q8 import check_conservative
+    v, i = scenes.heightfield(321, scenes.rng(104, bits))
+    n = i.shape[0]
+    res = ctx.build_geometry(to_dev(v), to_dev(i), node_format=rr.RR_CUDA_NODE_FORMAT_BVH4Q8, morton_bits=bits,
+                             quality=True)
+    nodes, _, _ = orc.build_mesh(v, i, bits=bits)
+    want, changed = orc.restructure(nodes, n, 64, 3)
+    assert changed > 0
+    assert same_nodes(nodes_of(res, n), want)
+    check_conservative(res, v, i)
+    assert ctx.device_errors() == 0
