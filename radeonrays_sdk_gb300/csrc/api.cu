@@ -247,6 +247,7 @@ struct Context
     cudaStream_t         pipe[kPipe]      = {};
     cudaEvent_t          pipe_fork        = nullptr;
     cudaEvent_t          pipe_join[kPipe] = {};
+    cudaEvent_t          pipe_kdone       = nullptr;  // streamed plan: after the kernel
     // Stream memory operations (driver entry points looked up once): the
     // streamed host-buffer trace sets arrival flags and waits on done
     // counters with them.  memops: 0 not probed, 1 usable, -1 not available.
@@ -255,6 +256,9 @@ struct Context
     void* write_value = nullptr;
     void* wait_value  = nullptr;
     bool  stream_rays = true;
+    // The streamed plan's late list (trace_stream.cuh), used when the host
+    // hit buffer is device-accessible; RR_CUDA_LATE_LIST=0 turns it off.
+    bool late_list = true;
     // Bounded device waits (rrCudaSetWaitLimits): arrival polls of a streamed
     // trace (0: default) and the test hook that never raises one chunk's
     // arrival flag (kInvalid: none).  The look-back limit lives in `words`.
@@ -269,6 +273,7 @@ struct Context
             check(cudaEventCreateWithFlags(&pipe_join[p], cudaEventDisableTiming), "pipeline event");
         }
         check(cudaEventCreateWithFlags(&pipe_fork, cudaEventDisableTiming), "pipeline event");
+        check(cudaEventCreateWithFlags(&pipe_kdone, cudaEventDisableTiming), "pipeline event");
     }
     void retire(Op&& op, cudaStream_t s)
     {
@@ -313,6 +318,7 @@ struct Context
             if (pipe_join[p]) cudaEventDestroy(pipe_join[p]);
         }
         if (pipe_fork) cudaEventDestroy(pipe_fork);
+        if (pipe_kdone) cudaEventDestroy(pipe_kdone);
         if (words) cudaFree(words);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -737,6 +743,7 @@ bool memops_ok(Context* ctx)
 struct StreamPlan
 {
     uint32_t* words      = nullptr;
+    uint32_t* late       = nullptr;  // late list (ray_count entries), or null
     uint32_t  shift      = 0;
     uint32_t  chunks     = 0;
     uint32_t  part_shift = 0;
@@ -825,11 +832,12 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         {
             if (a.collect_stats || a.indirect) return Op();
             a.stream_words      = sp->words;
+            a.stream_late       = sp->late;
             a.stream_shift      = sp->shift;
             a.stream_chunks     = sp->chunks;
             a.stream_part_shift = sp->part_shift;
             a.stream_parts      = sp->parts;
-            a.scratch_bytes = sp->scratch_bytes;
+            a.scratch_bytes     = sp->scratch_bytes;
         }
         return [=](cudaStream_t s) { return launch_trace_persistent(a, s); };
     }
@@ -842,6 +850,7 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
         {
             if (a.collect_stats || a.indirect) return Op();
             a.stream_words      = sp->words;
+            a.stream_late       = sp->late;
             a.stream_shift      = sp->shift;
             a.stream_chunks     = sp->chunks;
             a.stream_part_shift = sp->part_shift;
@@ -868,12 +877,18 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
 //   pipe[0]:  per chunk, copy its rays in, then set its arrival flag;
 //   s:        the streamed kernel (waits, bounded, for each chunk's flag);
 //   pipe[1]:  per part (four chunks), wait until its done counter reaches
-//             the part's size, then copy its hits out;
+//             the part's size, then copy its hits out; with a late list,
+//             then wait for the kernel and scatter the late-listed hits
+//             (launch_late_scatter) over the parts' copies;
 //   s:        join both side streams.
 // Everything is enqueued after what it depends on, so even side streams that
 // share one hardware queue with s only serialise.  The copy-out waits are
 // enqueued only after the kernel launched, and the kernel counts every ray
-// of every part (traced, or a miss after a failed wait), so each wait ends.
+// of every part (traced, a miss after a failed wait, or late-listed), so
+// each wait ends.
+// Measured on the 16.8 M-ray heightfield: without the late list, the parts
+// completed 1.5-2 ms after their rays were claimed (their slowest rays), and
+// a quarter of the hits were still to copy when the kernel ended.
 Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* host_rays, uint32_t ray_count, int output,
                        uint8_t* host_hits, uint8_t* dr, uint8_t* dh, uint8_t* sc, size_t scratch_total,
                        uint32_t chunk_rays)
@@ -896,13 +911,38 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
     const size_t woff   = (scratch_total - wbytes) / kAlign * kAlign;
     sp.words            = reinterpret_cast<uint32_t*>(sc + woff);
     sp.scratch_bytes    = woff;
+    // The late list needs the host hit buffer to be device-accessible (the
+    // scatter writes it from a kernel): page-locked or registered memory.
+    // It takes 4 bytes per ray below the words; the spill stacks keep the
+    // rest (trace_scratch_bytes leaves 256 bytes per ray).
+    uint8_t* hh_dev = nullptr;
+    if (ctx->late_list)
+    {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, host_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+            pa.devicePointer)
+            hh_dev = static_cast<uint8_t*>(pa.devicePointer);
+        cudaGetLastError();
+        const size_t lbytes = (size_t)ray_count * sizeof(uint32_t);
+        if (hh_dev && woff >= lbytes + 2 * kAlign)  // room for the list, the kernel's 256-byte header
+        {
+            const size_t loff = (woff - lbytes) / kAlign * kAlign;
+            sp.late           = reinterpret_cast<uint32_t*>(sc + loff);
+            sp.scratch_bytes  = loff;
+        }
+        else
+            hh_dev = nullptr;
+    }
     Op tr = trace_op(ctx, bvh, dr, ray_count, nullptr, dh, sc, query, output, ctx->topts, &sp);
     if (!tr) return Op();
     const auto     wr = reinterpret_cast<PfnStreamValue32>(ctx->write_value);
     const auto     wt = reinterpret_cast<PfnStreamValue32>(ctx->wait_value);
     cudaStream_t   in = ctx->pipe[0], out = ctx->pipe[1];
     cudaEvent_t    fork = ctx->pipe_fork, j_in = ctx->pipe_join[0], j_out = ctx->pipe_join[1];
+    cudaEvent_t    kdone = ctx->pipe_kdone;
     uint32_t*      words = sp.words;
+    uint32_t*      late  = sp.late;
+    const int      sms   = ctx->sm_count;
     const uint32_t nch = sp.chunks, nparts = sp.parts, pshift = sp.part_shift;
     const uint32_t drop = ctx->drop_arrival;  // test hook: this chunk's flag is never raised
     const size_t   hs  = output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT ? 16 : 4;
@@ -923,6 +963,7 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
         }
         if (e == cudaSuccess) e = tr(s);
         const bool launched = e == cudaSuccess;
+        if (launched && late) e = cudaEventRecord(kdone, s);
         for (uint32_t p = 0; launched && p < nparts && e == cudaSuccess; ++p)
         {
             const uint64_t off = (uint64_t)p << pshift;
@@ -933,6 +974,10 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
             else
                 e = cudaMemcpyAsync(host_hits + hs * off, dh + hs * off, hs * n, cudaMemcpyDeviceToHost, out);
         }
+        // The late-listed hits, after every part's copy and after the kernel.
+        if (launched && late && e == cudaSuccess) e = cudaStreamWaitEvent(out, kdone, 0);
+        if (launched && late && e == cudaSuccess)
+            e = launch_late_scatter(words + nch + nparts + 1, late, ray_count, dh, hh_dev, (uint32_t)hs, sms, out);
         cudaError_t j = cudaEventRecord(j_in, in);
         if (j == cudaSuccess) j = cudaStreamWaitEvent(s, j_in, 0);
         if (j == cudaSuccess) j = cudaEventRecord(j_out, out);
@@ -1141,6 +1186,8 @@ RR_API RRError rrCreateContext(uint32_t api_version, RRApi api, RRContext* conte
         c->fuse_builds       = !(fb && fb[0] == '0');
         const char* sr       = std::getenv("RR_CUDA_STREAM_RAYS");
         c->stream_rays       = !(sr && sr[0] == '0');
+        const char* ll       = std::getenv("RR_CUDA_LATE_LIST");
+        c->late_list         = !(ll && ll[0] == '0');
         *context             = reinterpret_cast<RRContext>(c.release());
         return RR_SUCCESS;
     })

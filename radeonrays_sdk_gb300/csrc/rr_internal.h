@@ -337,26 +337,32 @@ struct TraceArgs
     int             sm_count;
     int             box_leaves;   // AABB-list geometry: leaves are boxes
     int             triangle_test;  // RRCudaTriangleTest
-    // Streamed rays (host-buffer tracing, persistent binary kernel only): the
-    // rays arrive in chunks of 2^stream_shift while the kernel runs, and the
-    // hits leave in parts of 2^stream_part_shift rays (a part is a whole
-    // number of chunks).
+    // Streamed rays (host-buffer tracing; the persistent binary and 4-wide
+    // kernels): the rays arrive in chunks of 2^stream_shift while the kernel
+    // runs, and the hits leave in parts of 2^stream_part_shift rays (a part
+    // is a whole number of chunks).
     // stream_words[c] turns non-zero when chunk c is in device memory;
     // stream_words[stream_chunks + p] counts part p's finished rays;
     // stream_words[stream_chunks + stream_parts] is set when a lane gave up
-    // waiting for a chunk.
+    // waiting for a chunk; stream_words[stream_chunks + stream_parts + 1]
+    // counts the entries of stream_late.
+    // stream_late (may be null): ray_count ray indices.  A ray counted in its
+    // part's done counter before its hit was written (its part was closed
+    // while the ray was still in flight) is listed here, and its hit is
+    // copied to the host again after the kernel.
     uint32_t*       stream_words;
+    uint32_t*       stream_late;
     uint32_t        stream_shift;
     uint32_t        stream_chunks;
     uint32_t        stream_part_shift;
     uint32_t        stream_parts;
     uint32_t        stream_polls;  // arrival-flag polls (about 1 us each) before giving up (0: default)
 };
-// Words of a streamed trace (arrival flags, done counters, give-up flag),
-// rounded up to 256 bytes.
+// Words of a streamed trace (arrival flags, done counters, give-up flag,
+// late-list count), rounded up to 256 bytes.
 inline size_t stream_words_bytes(uint32_t chunks, uint32_t parts)
 {
-    return ((size_t)(chunks + parts + 1) * 4 + 255) / 256 * 256;
+    return ((size_t)(chunks + parts + 2) * 4 + 255) / 256 * 256;
 }
 // One request of a multi-request traversal launch (rrCudaCmdIntersectBatch).
 constexpr uint32_t kReqAny   = 1;  // any-hit query (else closest)
@@ -438,5 +444,11 @@ cudaError_t launch_build_scene(const SceneBuildArgs& a, const SceneLayout& L, ui
                                DeviceWords* words, cudaStream_t s);
 
 size_t trace_scratch_bytes(uint32_t ray_count);
+// After a streamed trace: copies the hit records of the late-listed rays
+// (count at *late_count, at most cap) from dev_hits to host_hits (a
+// device-accessible pointer to the host buffer), rec_bytes (4 or 16) each.
+cudaError_t launch_late_scatter(const uint32_t* late_count, const uint32_t* late, uint32_t cap,
+                                const uint8_t* dev_hits, uint8_t* host_hits, uint32_t rec_bytes, int sm_count,
+                                cudaStream_t s);
 
 }  // namespace rr

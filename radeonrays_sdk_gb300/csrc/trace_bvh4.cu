@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
     if (kStream)
     {
         if (threadIdx.x == 0) s_seen = -1;
-        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = 0;
+        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = dc.defer = dc.fin = 0;
         __syncthreads();
     }
     for (;;)
@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
                         }
                     }
                     seen = __shfl_sync(0xffffffffu, top, leader);
-                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, lane, dc);
+                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, active || pending, gid, lane,
+                                 dc);
                     __syncwarp();
                 }
             }
@@ -159,7 +160,11 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
                     }
                 }
             }
-            if (kStream) note_done(a, fin, fin_c, lane, dc);
+            if (kStream)
+            {
+                note_done(a, fin, fin_c, lane, dc);
+                if (a.stream_late && exhausted) finalize_done(a, active || pending, gid, lane, dc);
+            }
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;

@@ -20,10 +20,13 @@
 // that chunk's copy.  Each finished ray is counted in the done counter of
 // its part (a copy-out unit of several chunks; release adds, batched per
 // warp and part), and the copy-out stream waits for each counter before it
-// copies that part's hits to the host.  Every claimed ray is counted exactly
-// once, whether it was traced, missed an empty geometry, or gave up waiting,
+// copies that part's hits to the host.  With a late list, a ray still in
+// flight when its warp closes the part is counted early and late-listed, and
+// the late scatter after the kernel brings its hit to the host
+// (trace_stream.cuh).  Every claimed ray is counted exactly once, whether it
+// was traced, missed an empty geometry, gave up waiting, or was late-listed,
 // and the last counts are published before the warp exits, so every counter
-// reaches its part's size when the kernel ends.
+// reaches its part's size by the time the kernel ends.
 #include "trace_persistent.cuh"
 #include "trace_stream.cuh"
 
@@ -59,7 +62,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
     if (kStream)
     {
         if (threadIdx.x == 0) s_seen = -1;
-        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = 0;
+        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = dc.defer = dc.fin = 0;
         __syncthreads();
     }
     for (;;)
@@ -95,7 +98,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         }
                     }
                     seen = __shfl_sync(0xffffffffu, top, leader);
-                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, lane, dc);
+                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, active || pending, gid, lane,
+                                 dc);
                     __syncwarp();
                 }
             }
@@ -159,7 +163,11 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                     }
                 }
             }
-            if (kStream) note_done(a, fin, fin_c, lane, dc);
+            if (kStream)
+            {
+                note_done(a, fin, fin_c, lane, dc);
+                if (a.stream_late && exhausted) finalize_done(a, active || pending, gid, lane, dc);
+            }
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
@@ -214,7 +222,37 @@ cudaError_t go_stream(const TraceArgs& a, cudaStream_t s)
 {
     return a.box_leaves ? go2<kAny, kFull, false, true, true>(a, s) : go_tri<kAny, kFull, false, true>(a, s);
 }
+
+// The late scatter of a streamed trace (trace_stream.cuh): one record per
+// listed ray, device hits to the host buffer.  Indices at or past cap are
+// skipped (a listed ray index is always below the ray count).
+template <typename Rec>
+__global__ void k_late_scatter(const uint32_t* late_count, const uint32_t* late, uint32_t cap, const Rec* dev_hits,
+                               Rec* host_hits)
+{
+    const uint32_t n = min(*late_count, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t g = __ldg(late + i);
+        if (g < cap) host_hits[g] = dev_hits[g];
+    }
+}
 }  // namespace
+
+cudaError_t launch_late_scatter(const uint32_t* late_count, const uint32_t* late, uint32_t cap,
+                                const uint8_t* dev_hits, uint8_t* host_hits, uint32_t rec_bytes, int sm_count,
+                                cudaStream_t s)
+{
+    const int blocks = (sm_count > 0 ? sm_count : 1) * 2;
+    if (rec_bytes == 16)
+        k_late_scatter<uint4><<<blocks, 256, 0, s>>>(late_count, late, cap, reinterpret_cast<const uint4*>(dev_hits),
+                                                     reinterpret_cast<uint4*>(host_hits));
+    else
+        k_late_scatter<uint32_t><<<blocks, 256, 0, s>>>(late_count, late, cap,
+                                                        reinterpret_cast<const uint32_t*>(dev_hits),
+                                                        reinterpret_cast<uint32_t*>(host_hits));
+    return cudaGetLastError();
+}
 
 cudaError_t launch_trace_persistent(const TraceArgs& a, cudaStream_t s)
 {

@@ -78,39 +78,121 @@ __device__ __noinline__ static void add_release(uint32_t* p, uint32_t v)
 // issues one about once per part it works on, not at every refill.  The
 // counts live in shared memory (one record per warp, written by lane 0 only)
 // so that no register stays live across the traversal step for them.
+//
+// With a late list (a.stream_late), a part is not held open by its slowest
+// rays: when the warp publishes a part, a ray it still holds there (in
+// flight, or finished with its hit not yet written) is counted at once and
+// its index late-listed; the same happens to every ray the warp holds once
+// the rays are exhausted.  The copy-out of a part then follows the claim
+// front by about two parts instead of waiting for its longest ray, and the
+// last parts leave while the kernel drains.  A late-listed ray's hit reaches
+// the host through the late scatter after the kernel (launch_late_scatter),
+// which runs after every part's copy.  `defer` holds the lanes whose current
+// ray is late-listed (not counted again when it finishes); `fin` is set once
+// the warp has published everything at exhaustion.
 struct DoneCounts
 {
-    uint32_t cur_c, cur_n, prev_c, prev_n;
+    uint32_t cur_c, cur_n, prev_c, prev_n, defer, fin;
 };
 
+// Appends the rays of the lanes in m (warp-uniform, non-zero) to the late
+// list; `mine` is this lane's bit of m.
+__device__ __forceinline__ void late_append(const TraceArgs& a, uint32_t m, bool mine, uint32_t gid, uint32_t lane)
+{
+    const int leader = __ffs(m) - 1;
+    uint32_t  base   = 0;
+    if ((int)lane == leader) base = atomicAdd(a.stream_words + a.stream_chunks + a.stream_parts + 1, (uint32_t)__popc(m));
+    base                = __shfl_sync(0xffffffffu, base, leader);
+    const uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
+    if (mine && slot < a.ray_count) a.stream_late[slot] = gid;
+}
+
 // Rays finished at this refill (`fin`, part `c`); all 32 lanes call it,
-// after their hits are written.
+// after their hits are written.  A late-listed ray is not counted again.
 __device__ __forceinline__ void note_done(const TraceArgs& a, bool fin, uint32_t c, uint32_t lane,
                                           volatile DoneCounts& d)
 {
-    if (!__ballot_sync(0xffffffffu, fin)) return;
-    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c;
-    const uint32_t in_cur  = __ballot_sync(0xffffffffu, fin && c == cur_c);
-    const uint32_t in_prev = __ballot_sync(0xffffffffu, fin && c == prev_c && prev_c != cur_c);
+    const uint32_t fm = __ballot_sync(0xffffffffu, fin);
+    if (!fm) return;
+    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c, dm = d.defer;
+    const bool     cnt     = fin && !((dm >> lane) & 1u);
+    const uint32_t in_cur  = __ballot_sync(0xffffffffu, cnt && c == cur_c);
+    const uint32_t in_prev = __ballot_sync(0xffffffffu, cnt && c == prev_c && prev_c != cur_c);
     if (lane == 0)
     {
         d.cur_n  = d.cur_n + __popc(in_cur);
         d.prev_n = d.prev_n + __popc(in_prev);
+        d.defer  = dm & ~fm;
     }
-    if (fin && !(((in_cur | in_prev) >> lane) & 1u)) add_release(a.stream_words + a.stream_chunks + c, 1u);
+    if (cnt && !(((in_cur | in_prev) >> lane) & 1u)) add_release(a.stream_words + a.stream_chunks + c, 1u);
     __syncwarp();
 }
 
 // The warp's claims reached part `hi` (warp-uniform): publish `prev` and
 // shift.  The counted hits were written before the loop's __syncwarp.
-__device__ __forceinline__ void advance_done(const TraceArgs& a, uint32_t hi, uint32_t lane, volatile DoneCounts& d)
+// `holds`: the lane has a ray not yet counted (gid); with a late list, such a
+// ray in a part that is not open after the shift is counted now (with prev
+// when it lies there) and late-listed.  Rays the warp holds lie in parts up
+// to cur (claimed earlier), so that is every held ray outside cur.
+__device__ __forceinline__ void advance_done(const TraceArgs& a, uint32_t hi, bool holds, uint32_t gid, uint32_t lane,
+                                             volatile DoneCounts& d)
 {
-    if (lane != 0 || hi <= d.cur_c) return;
-    if (d.prev_n) add_release(a.stream_words + a.stream_chunks + d.prev_c, d.prev_n);
-    d.prev_c = d.cur_c;
+    const uint32_t cur_c = d.cur_c;
+    if (hi <= cur_c) return;
+    const uint32_t prev_c = d.prev_c;
+    uint32_t       nlate  = 0, lm = 0;
+    if (a.stream_late)
+    {
+        const uint32_t rc   = gid >> a.stream_part_shift;
+        const bool     late = holds && !((d.defer >> lane) & 1u) && rc != cur_c;
+        lm                  = __ballot_sync(0xffffffffu, late);
+        if (lm)
+        {
+            late_append(a, lm, late, gid, lane);
+            const bool to_prev = late && rc == prev_c && prev_c != cur_c;
+            nlate              = __popc(__ballot_sync(0xffffffffu, to_prev));
+            if (late && !to_prev) add_release(a.stream_words + a.stream_chunks + rc, 1u);
+        }
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    const uint32_t n = d.prev_n + nlate;
+    if (n) add_release(a.stream_words + a.stream_chunks + prev_c, n);
+    d.defer  = d.defer | lm;
+    d.prev_c = cur_c;
     d.prev_n = d.cur_n;
     d.cur_c  = hi;
     d.cur_n  = 0;
+}
+
+// With a late list: the warp's claims are exhausted (warp-uniform call at
+// each refill after that): once, count and late-list every ray the warp
+// still holds and publish both open counts.  Later finishes are all
+// late-listed rays, so nothing is left to publish at exit.
+__device__ __forceinline__ void finalize_done(const TraceArgs& a, bool holds, uint32_t gid, uint32_t lane,
+                                              volatile DoneCounts& d)
+{
+    if (d.fin) return;
+    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c;
+    const uint32_t rc      = gid >> a.stream_part_shift;
+    const bool     late    = holds && !((d.defer >> lane) & 1u);
+    const bool     in_cur  = late && rc == cur_c;
+    const bool     in_prev = late && rc == prev_c && prev_c != cur_c;
+    const uint32_t lm      = __ballot_sync(0xffffffffu, late);
+    const uint32_t nc      = __popc(__ballot_sync(0xffffffffu, in_cur));
+    const uint32_t np      = __popc(__ballot_sync(0xffffffffu, in_prev));
+    if (lm) late_append(a, lm, late, gid, lane);
+    if (late && !in_cur && !in_prev) add_release(a.stream_words + a.stream_chunks + rc, 1u);
+    __syncwarp();
+    if (lane == 0)
+    {
+        if (d.cur_n + nc) add_release(a.stream_words + a.stream_chunks + cur_c, d.cur_n + nc);
+        if (d.prev_n + np) add_release(a.stream_words + a.stream_chunks + prev_c, d.prev_n + np);
+        d.cur_n = d.prev_n = 0;
+        d.defer = d.defer | lm;
+        d.fin   = 1;
+    }
+    __syncwarp();
 }
 
 // Publish both open counts (lane 0); after a __syncwarp that follows the

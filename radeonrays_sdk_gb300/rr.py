@@ -497,14 +497,17 @@ class Context:
         return hits
 
     def intersect_host(self, bvh, rays_host, query=RR_INTERSECT_QUERY_CLOSEST, output=RR_INTERSECT_QUERY_OUTPUT_FULL_HIT,
-                       chunk_rays=0, staging=None):
+                       chunk_rays=0, staging=None, pinned_hits=True):
         """rays_host: CPU float32 tensor (R, 8), pinned for copy/compute overlap.  Returns the hits as a CPU
         int32 tensor ((R, 4) or (R,)) through one rrCudaCmdIntersectHostBuffers call.  `staging` may pass
-        (rays_dev, hits_dev, scratch) to reuse device buffers."""
+        (rays_dev, hits_dev, scratch) to reuse device buffers; pinned_hits=False returns the hits in pageable
+        memory."""
         torch = _torch()
         R = rays_host.shape[0]
         full = output == RR_INTERSECT_QUERY_OUTPUT_FULL_HIT
-        hits_host = torch.full((R, 4) if full else (R,), -1, dtype=torch.int32).pin_memory()
+        hits_host = torch.full((R, 4) if full else (R,), -1, dtype=torch.int32)
+        if pinned_hits:
+            hits_host = hits_host.pin_memory()
         if staging is None:
             staging = (torch.empty((R, 8), dtype=torch.float32, device="cuda"),
                        torch.full((R, 4) if full else (R,), -1, dtype=torch.int32, device="cuda"),
