@@ -291,14 +291,16 @@ RR_API RRError rrCudaCmdBuildGeometries(RRContext                   context,
 /* Intersect rays that live in host memory (no counterpart in the reference
  * API, whose rrCmdIntersect takes device buffers, radeonrays.h:391-400).
  * Two plans, with the same hits:
- *   streamed (2^16 rays or more with the persistent binary traversal, the
- *     default, or the 4-wide traversal):
+ *   streamed (2^16 rays or more with the persistent binary or the 4-wide
+ *     traversal, and host_hits page-locked or registered):
  *     one kernel launch over all rays; the rays are copied in chunks of
  *     `chunk_rays` (rounded down to a power of two; 0 = 2^17) on a context
  *     stream that raises a flag per chunk, the kernel traces each chunk once
  *     its flag is up, and a second context stream copies the hits out in
- *     parts of four chunks as each part's rays are all written (stream
- *     memory operations: cuStreamWriteValue32 / cuStreamWaitValue32);
+ *     parts of eight chunks as the kernel's warps publish each part (stream
+ *     memory operations: cuStreamWriteValue32 / cuStreamWaitValue32); the
+ *     hits of rays still in flight when their part was published are then
+ *     written to host_hits by a small kernel after the trace;
  *   chunked (otherwise, inside a stream capture, or RR_CUDA_STREAM_RAYS=0):
  *     chunks of `chunk_rays` (0 = 2^21), each copied in, traced and copied
  *     out on one of three context streams.

@@ -256,9 +256,6 @@ struct Context
     void* write_value = nullptr;
     void* wait_value  = nullptr;
     bool  stream_rays = true;
-    // The streamed plan's late list (trace_stream.cuh), used when the host
-    // hit buffer is device-accessible; RR_CUDA_LATE_LIST=0 turns it off.
-    bool late_list = true;
     // Bounded device waits (rrCudaSetWaitLimits): arrival polls of a streamed
     // trace (0: default) and the test hook that never raises one chunk's
     // arrival flag (kInvalid: none).  The look-back limit lives in `words`.
@@ -743,7 +740,7 @@ bool memops_ok(Context* ctx)
 struct StreamPlan
 {
     uint32_t* words      = nullptr;
-    uint32_t* late       = nullptr;  // late list (ray_count entries), or null
+    uint32_t* late       = nullptr;  // late list (ray_count entries)
     uint32_t  shift      = 0;
     uint32_t  chunks     = 0;
     uint32_t  part_shift = 0;
@@ -871,68 +868,63 @@ Op trace_op(Context* ctx, uint8_t* bvh, const uint8_t* rays, uint32_t ray_count,
 }
 
 // Host-buffer trace as one persistent launch over all rays (empty Op when the
-// plan does not apply: fewer than 2^16 rays, no stream memory operations, or
-// a traversal other than the persistent binary or 4-wide kernel).  On stream s:
+// plan does not apply: fewer than 2^16 rays, no stream memory operations, a
+// host hit buffer the device cannot write, or a traversal other than the
+// persistent binary or 4-wide kernel).  On stream s:
 //   s:        clear the words, fork;
 //   pipe[0]:  per chunk, copy its rays in, then set its arrival flag;
 //   s:        the streamed kernel (waits, bounded, for each chunk's flag);
-//   pipe[1]:  per part (four chunks), wait until its done counter reaches
-//             the part's size, then copy its hits out; with a late list,
-//             then wait for the kernel and scatter the late-listed hits
-//             (launch_late_scatter) over the parts' copies;
+//   pipe[1]:  per part (eight chunks), wait until its done counter reaches
+//             the part's size, then copy its hits out; then wait for the
+//             kernel and scatter the late-listed hits (launch_late_scatter)
+//             over the parts' copies;
 //   s:        join both side streams.
 // Everything is enqueued after what it depends on, so even side streams that
 // share one hardware queue with s only serialise.  The copy-out waits are
 // enqueued only after the kernel launched, and the kernel counts every ray
 // of every part (traced, a miss after a failed wait, or late-listed), so
 // each wait ends.
-// Measured on the 16.8 M-ray heightfield: without the late list, the parts
-// completed 1.5-2 ms after their rays were claimed (their slowest rays), and
-// a quarter of the hits were still to copy when the kernel ended.
+// Measured on the 16.8 M-ray heightfield: when parts were counted by
+// finished rays instead, they completed 1.5-2 ms after their rays were
+// claimed (their slowest rays), and a quarter of the hits were still to copy
+// when the kernel ended.
 Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* host_rays, uint32_t ray_count, int output,
                        uint8_t* host_hits, uint8_t* dr, uint8_t* dh, uint8_t* sc, size_t scratch_total,
                        uint32_t chunk_rays)
 {
     if (ray_count < (1u << 16) || !memops_ok(ctx)) return Op();
+    // The late scatter writes the host hit buffer from a kernel, so the plan
+    // needs it device-accessible (page-locked or registered memory).
+    cudaPointerAttributes pa{};
+    uint8_t*              hh_dev = nullptr;
+    if (cudaPointerGetAttributes(&pa, host_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        hh_dev = static_cast<uint8_t*>(pa.devicePointer);
+    cudaGetLastError();
+    if (!hh_dev) return Op();
     // Copy-in chunks: 2^17 rays by default (4 MiB; the first one is the wait
-    // before the kernel starts).  Copy-out parts: four chunks (8 MiB of full
-    // hits), so that each warp issues few release adds; the last part is the
-    // tail after the kernel.  (Measured on the 16.8 M-ray heightfield: 2^16
-    // / 2^17 / 2^18-ray chunks gave 2,899 / 2,971 / 2,937 Mrays/s end to end.)
+    // before the kernel starts).  Copy-out parts: eight chunks (16 MiB of full
+    // hits), so that each warp publishes few counts and late-lists few rays.
+    // (Measured on the 16.8 M-ray heightfield: 2^16 / 2^17 / 2^18-ray chunks
+    // with 2^20-ray parts gave 3,241 / 3,517 / 3,508 Mrays/s end to end;
+    // parts of two / four / eight chunks 3,145 / 3,465 / 3,500.)
     uint32_t shift = 17;
     if (chunk_rays)
         for (shift = 12; shift < 24 && (2u << shift) <= chunk_rays;) ++shift;
     StreamPlan sp;
     sp.shift            = shift;
     sp.chunks           = (uint32_t)(((uint64_t)ray_count + (1ull << shift) - 1) >> shift);
-    sp.part_shift       = shift + 2;
+    sp.part_shift       = shift + 3;
     sp.parts            = (uint32_t)(((uint64_t)ray_count + (1ull << sp.part_shift) - 1) >> sp.part_shift);
     const size_t wbytes = stream_words_bytes(sp.chunks, sp.parts);
     const size_t woff   = (scratch_total - wbytes) / kAlign * kAlign;
     sp.words            = reinterpret_cast<uint32_t*>(sc + woff);
-    sp.scratch_bytes    = woff;
-    // The late list needs the host hit buffer to be device-accessible (the
-    // scatter writes it from a kernel): page-locked or registered memory.
-    // It takes 4 bytes per ray below the words; the spill stacks keep the
-    // rest (trace_scratch_bytes leaves 256 bytes per ray).
-    uint8_t* hh_dev = nullptr;
-    if (ctx->late_list)
-    {
-        cudaPointerAttributes pa{};
-        if (cudaPointerGetAttributes(&pa, host_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
-            pa.devicePointer)
-            hh_dev = static_cast<uint8_t*>(pa.devicePointer);
-        cudaGetLastError();
-        const size_t lbytes = (size_t)ray_count * sizeof(uint32_t);
-        if (hh_dev && woff >= lbytes + 2 * kAlign)  // room for the list, the kernel's 256-byte header
-        {
-            const size_t loff = (woff - lbytes) / kAlign * kAlign;
-            sp.late           = reinterpret_cast<uint32_t*>(sc + loff);
-            sp.scratch_bytes  = loff;
-        }
-        else
-            hh_dev = nullptr;
-    }
+    // The late list: 4 bytes per ray below the words; the spill stacks keep
+    // the rest (trace_scratch_bytes gives 256 bytes per ray).
+    const size_t lbytes = (size_t)ray_count * sizeof(uint32_t);
+    if (woff < lbytes + 2 * kAlign) return Op();  // room for the list and the kernel's 256-byte header
+    const size_t loff = (woff - lbytes) / kAlign * kAlign;
+    sp.late           = reinterpret_cast<uint32_t*>(sc + loff);
+    sp.scratch_bytes  = loff;
     Op tr = trace_op(ctx, bvh, dr, ray_count, nullptr, dh, sc, query, output, ctx->topts, &sp);
     if (!tr) return Op();
     const auto     wr = reinterpret_cast<PfnStreamValue32>(ctx->write_value);
@@ -963,7 +955,7 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
         }
         if (e == cudaSuccess) e = tr(s);
         const bool launched = e == cudaSuccess;
-        if (launched && late) e = cudaEventRecord(kdone, s);
+        if (launched) e = cudaEventRecord(kdone, s);
         for (uint32_t p = 0; launched && p < nparts && e == cudaSuccess; ++p)
         {
             const uint64_t off = (uint64_t)p << pshift;
@@ -975,8 +967,8 @@ Op streamed_host_trace(Context* ctx, uint8_t* bvh, int query, const uint8_t* hos
                 e = cudaMemcpyAsync(host_hits + hs * off, dh + hs * off, hs * n, cudaMemcpyDeviceToHost, out);
         }
         // The late-listed hits, after every part's copy and after the kernel.
-        if (launched && late && e == cudaSuccess) e = cudaStreamWaitEvent(out, kdone, 0);
-        if (launched && late && e == cudaSuccess)
+        if (launched && e == cudaSuccess) e = cudaStreamWaitEvent(out, kdone, 0);
+        if (launched && e == cudaSuccess)
             e = launch_late_scatter(words + nch + nparts + 1, late, ray_count, dh, hh_dev, (uint32_t)hs, sms, out);
         cudaError_t j = cudaEventRecord(j_in, in);
         if (j == cudaSuccess) j = cudaStreamWaitEvent(s, j_in, 0);
@@ -1186,8 +1178,6 @@ RR_API RRError rrCreateContext(uint32_t api_version, RRApi api, RRContext* conte
         c->fuse_builds       = !(fb && fb[0] == '0');
         const char* sr       = std::getenv("RR_CUDA_STREAM_RAYS");
         c->stream_rays       = !(sr && sr[0] == '0');
-        const char* ll       = std::getenv("RR_CUDA_LATE_LIST");
-        c->late_list         = !(ll && ll[0] == '0');
         *context             = reinterpret_cast<RRContext>(c.release());
         return RR_SUCCESS;
     })

@@ -346,8 +346,8 @@ struct TraceArgs
     // stream_words[stream_chunks + stream_parts] is set when a lane gave up
     // waiting for a chunk; stream_words[stream_chunks + stream_parts + 1]
     // counts the entries of stream_late.
-    // stream_late (may be null): ray_count ray indices.  A ray counted in its
-    // part's done counter before its hit was written (its part was closed
+    // stream_late: room for ray_count ray indices.  A ray counted in its
+    // part's done counter before its hit was written (its part was published
     // while the ray was still in flight) is listed here, and its hit is
     // copied to the host again after the kernel.
     uint32_t*       stream_words;

@@ -64,7 +64,11 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
     if (kStream)
     {
         if (threadIdx.x == 0) s_seen = -1;
-        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = dc.defer = dc.fin = 0;
+        if (lane == 0)
+        {
+            dc.cur_c = dc.cur_n = dc.prev_n = dc.fin = 0;
+            dc.prev_c                               = kInvalid;
+        }
         __syncthreads();
     }
     for (;;)
@@ -73,7 +77,8 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
         if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
         {
-            int            seen = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
+            int            seen     = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
+            uint32_t       jump_end = 0;   // kStream: claim_done's result (warp-uniform)
             const uint32_t n    = exhausted ? 0u : __popc(idle);
             uint32_t       base = 0;
             if (n)
@@ -96,13 +101,10 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
                         }
                     }
                     seen = __shfl_sync(0xffffffffu, top, leader);
-                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, active || pending, gid, lane,
-                                 dc);
-                    __syncwarp();
+                    jump_end = claim_done(a, base, min(base + n, count), active || pending, gid, lane, dc);
                 }
             }
-            bool     fin   = false;
-            uint32_t fin_c = 0;
+            bool fresh = false;  // kStream: took a new ray at this refill
             if (!active)
             {
                 if (pending)
@@ -126,8 +128,6 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
                         atomicAdd(&a.words->tri_fetches, (unsigned long long)tf);
                     }
                     pending = false;
-                    fin     = true;
-                    fin_c   = gid >> a.stream_part_shift;
                 }
                 const uint32_t my = base + __popc(idle & lt);
                 if (n && my < count)
@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
                     gid = my;
                     if (kStream)
                     {
+                        fresh = true;
                         // Traced once its chunk is in; an empty geometry or a
                         // chunk that never arrived finishes as a miss at the
                         // next refill, where it is counted like any other.
@@ -162,8 +163,8 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
             }
             if (kStream)
             {
-                note_done(a, fin, fin_c, lane, dc);
-                if (a.stream_late && exhausted) finalize_done(a, active || pending, gid, lane, dc);
+                if (jump_end) jump_done(a, fresh, gid, jump_end, lane);
+                if (exhausted) finalize_done(a, active || pending, gid, lane, dc);
             }
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
@@ -183,11 +184,6 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
             active  = false;
             pending = true;
         }
-    }
-    if (kStream)
-    {
-        __syncwarp();  // the break above is warp-uniform; order the last hits before their counts
-        publish_done(a, lane, dc);
     }
 }
 

@@ -17,16 +17,15 @@
 // while the copy engine is still bringing them in.  Rays are taken in index
 // order, so a warp only waits (bounded, once per chunk) for the arrival flag
 // of the last chunk its new rays lie in, which the copy stream sets after
-// that chunk's copy.  Each finished ray is counted in the done counter of
+// that chunk's copy.  Each claimed ray is counted once in the done counter of
 // its part (a copy-out unit of several chunks; release adds, batched per
-// warp and part), and the copy-out stream waits for each counter before it
-// copies that part's hits to the host.  With a late list, a ray still in
-// flight when its warp closes the part is counted early and late-listed, and
-// the late scatter after the kernel brings its hit to the host
-// (trace_stream.cuh).  Every claimed ray is counted exactly once, whether it
-// was traced, missed an empty geometry, gave up waiting, or was late-listed,
-// and the last counts are published before the warp exits, so every counter
-// reaches its part's size by the time the kernel ends.
+// warp and part, published as the warp's claims move on and when the rays
+// run out), and the copy-out stream waits for each counter before it copies
+// that part's hits to the host.  A ray the warp still holds when it
+// publishes the ray's part is late-listed; the late scatter after the kernel
+// brings its hit to the host (trace_stream.cuh).  So every counter reaches
+// its part's size by the time the kernel ends, whether its rays were traced,
+// missed an empty geometry, or gave up waiting for their chunk.
 #include "trace_persistent.cuh"
 #include "trace_stream.cuh"
 
@@ -62,7 +61,11 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
     if (kStream)
     {
         if (threadIdx.x == 0) s_seen = -1;
-        if (lane == 0) dc.cur_c = dc.cur_n = dc.prev_c = dc.prev_n = dc.defer = dc.fin = 0;
+        if (lane == 0)
+        {
+            dc.cur_c = dc.cur_n = dc.prev_n = dc.fin = 0;
+            dc.prev_c                               = kInvalid;
+        }
         __syncthreads();
     }
     for (;;)
@@ -73,7 +76,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
         const uint32_t idle = __ballot_sync(0xffffffffu, !active);
         if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
         {
-            int seen = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
+            int      seen     = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
+            uint32_t jump_end = 0;   // kStream: claim_done's result (warp-uniform)
             const uint32_t n    = exhausted ? 0u : __popc(idle);
             uint32_t       base = 0;
             if (n)
@@ -98,13 +102,10 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         }
                     }
                     seen = __shfl_sync(0xffffffffu, top, leader);
-                    advance_done(a, (min(base + n, count) - 1u) >> a.stream_part_shift, active || pending, gid, lane,
-                                 dc);
-                    __syncwarp();
+                    jump_end = claim_done(a, base, min(base + n, count), active || pending, gid, lane, dc);
                 }
             }
-            bool     fin   = false;
-            uint32_t fin_c = 0;
+            bool fresh = false;  // kStream: took a new ray at this refill
             if (!active)
             {
                 if (pending)
@@ -129,8 +130,6 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                         atomicAdd(&a.words->node_fetches, (unsigned long long)nf);
                     }
                     pending = false;
-                    fin     = true;
-                    fin_c   = gid >> a.stream_part_shift;
                 }
                 const uint32_t my = base + __popc(idle & lt);
                 if (n && my < count)
@@ -138,6 +137,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
                     gid = my;
                     if (kStream)
                     {
+                        fresh = true;
                         // Traced once its chunk is in; an empty geometry or a
                         // chunk that never arrived finishes as a miss at the
                         // next refill, where it is counted like any other.
@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
             }
             if (kStream)
             {
-                note_done(a, fin, fin_c, lane, dc);
-                if (a.stream_late && exhausted) finalize_done(a, active || pending, gid, lane, dc);
+                if (jump_end) jump_done(a, fresh, gid, jump_end, lane);
+                if (exhausted) finalize_done(a, active || pending, gid, lane, dc);
             }
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
@@ -176,11 +176,6 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_persistent(TraceArgs a, ui
             active  = false;
             pending = true;
         }
-    }
-    if (kStream)
-    {
-        __syncwarp();  // the break above is warp-uniform; order the last hits before their counts
-        publish_done(a, lane, dc);
     }
 }
 

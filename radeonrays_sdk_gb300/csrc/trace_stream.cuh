@@ -69,30 +69,25 @@ __device__ __noinline__ static void add_release(uint32_t* p, uint32_t v)
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Done counts of a warp: rays finished in the part (copy-out unit, several
-// arrival chunks) the warp is claiming from (cur) and in the one before it
-// (prev), not yet added to the parts' done counters.  `prev` is published
-// when the warp's claims move on to a later part, both at exit; a ray of any
-// other part (a straggler) is added at once.  A release add waits until the
-// SM's earlier stores are visible, which costs microseconds, so a warp
-// issues one about once per part it works on, not at every refill.  The
+// Done counts of a warp, kept by claims: a warp counts the rays it claims in
+// the part (copy-out unit, several arrival chunks) it is claiming from (cur)
+// and in the one before it (prev), and publishes `prev` when its claims move
+// on to a later part, both once the rays are exhausted.  A ray the warp
+// still holds when it publishes the ray's part (in flight, or finished with
+// its hit not yet written) is late-listed: its index goes to the late list,
+// and the late scatter after the kernel (launch_late_scatter), which runs
+// after every part's copy, brings its hit to the host.  Every other ray of
+// the part finished earlier, and its hit was written before the loop's
+// __syncwarp that precedes the release add.  So a part's counter reaches
+// its size about two parts behind the claim front, however long its slowest
+// rays take, and the last parts leave while the kernel drains.
+// A release add waits until the SM's earlier stores are visible, which costs
+// microseconds, so a warp issues one about once per part it works on.  The
 // counts live in shared memory (one record per warp, written by lane 0 only)
 // so that no register stays live across the traversal step for them.
-//
-// With a late list (a.stream_late), a part is not held open by its slowest
-// rays: when the warp publishes a part, a ray it still holds there (in
-// flight, or finished with its hit not yet written) is counted at once and
-// its index late-listed; the same happens to every ray the warp holds once
-// the rays are exhausted.  The copy-out of a part then follows the claim
-// front by about two parts instead of waiting for its longest ray, and the
-// last parts leave while the kernel drains.  A late-listed ray's hit reaches
-// the host through the late scatter after the kernel (launch_late_scatter),
-// which runs after every part's copy.  `defer` holds the lanes whose current
-// ray is late-listed (not counted again when it finishes); `fin` is set once
-// the warp has published everything at exhaustion.
 struct DoneCounts
 {
-    uint32_t cur_c, cur_n, prev_c, prev_n, defer, fin;
+    uint32_t cur_c, cur_n, prev_c, prev_n, fin;
 };
 
 // Appends the rays of the lanes in m (warp-uniform, non-zero) to the late
@@ -107,104 +102,82 @@ __device__ __forceinline__ void late_append(const TraceArgs& a, uint32_t m, bool
     if (mine && slot < a.ray_count) a.stream_late[slot] = gid;
 }
 
-// Rays finished at this refill (`fin`, part `c`); all 32 lanes call it,
-// after their hits are written.  A late-listed ray is not counted again.
-__device__ __forceinline__ void note_done(const TraceArgs& a, bool fin, uint32_t c, uint32_t lane,
-                                          volatile DoneCounts& d)
+// The warp claimed rays [base, end) (all 32 lanes call it, before the new
+// rays are given out; `holds`/gid: the lane's current ray, not yet
+// counted-and-written).  A claim spans at most two parts (it is at most 32
+// rays; a part is at least 2^15).  When it reaches a part beyond cur, prev is
+// published (its held rays late-listed) and the counts shift.  The new rays
+// are then counted in cur, or in prev when they lie there.  Returns the end of
+// the claim's rays that lie in neither (0 if none): the claim skipped a whole
+// part, so those rays' part will not be published by this warp; jump_done
+// counts and late-lists them at once.
+__device__ __forceinline__ uint32_t claim_done(const TraceArgs& a, uint32_t base, uint32_t end, bool holds,
+                                               uint32_t gid, uint32_t lane, volatile DoneCounts& d)
 {
-    const uint32_t fm = __ballot_sync(0xffffffffu, fin);
-    if (!fm) return;
-    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c, dm = d.defer;
-    const bool     cnt     = fin && !((dm >> lane) & 1u);
-    const uint32_t in_cur  = __ballot_sync(0xffffffffu, cnt && c == cur_c);
-    const uint32_t in_prev = __ballot_sync(0xffffffffu, cnt && c == prev_c && prev_c != cur_c);
-    if (lane == 0)
-    {
-        d.cur_n  = d.cur_n + __popc(in_cur);
-        d.prev_n = d.prev_n + __popc(in_prev);
-        d.defer  = dm & ~fm;
-    }
-    if (cnt && !(((in_cur | in_prev) >> lane) & 1u)) add_release(a.stream_words + a.stream_chunks + c, 1u);
-    __syncwarp();
-}
-
-// The warp's claims reached part `hi` (warp-uniform): publish `prev` and
-// shift.  The counted hits were written before the loop's __syncwarp.
-// `holds`: the lane has a ray not yet counted (gid); with a late list, such a
-// ray in a part that is not open after the shift is counted now (with prev
-// when it lies there) and late-listed.  Rays the warp holds lie in parts up
-// to cur (claimed earlier), so that is every held ray outside cur.
-__device__ __forceinline__ void advance_done(const TraceArgs& a, uint32_t hi, bool holds, uint32_t gid, uint32_t lane,
-                                             volatile DoneCounts& d)
-{
+    const uint32_t ps = a.stream_part_shift;
+    const uint32_t hi = (end - 1u) >> ps, lo = base >> ps;
     const uint32_t cur_c = d.cur_c;
-    if (hi <= cur_c) return;
-    const uint32_t prev_c = d.prev_c;
-    uint32_t       nlate  = 0, lm = 0;
-    if (a.stream_late)
+    if (hi > cur_c)
     {
-        const uint32_t rc   = gid >> a.stream_part_shift;
-        const bool     late = holds && !((d.defer >> lane) & 1u) && rc != cur_c;
-        lm                  = __ballot_sync(0xffffffffu, late);
-        if (lm)
+        const uint32_t prev_c = d.prev_c;
+        const bool     late   = holds && (gid >> ps) == prev_c;
+        const uint32_t lm     = __ballot_sync(0xffffffffu, late);
+        if (lm) late_append(a, lm, late, gid, lane);
+        __syncwarp();
+        if (lane == 0)
         {
-            late_append(a, lm, late, gid, lane);
-            const bool to_prev = late && rc == prev_c && prev_c != cur_c;
-            nlate              = __popc(__ballot_sync(0xffffffffu, to_prev));
-            if (late && !to_prev) add_release(a.stream_words + a.stream_chunks + rc, 1u);
+            if (d.prev_n) add_release(a.stream_words + a.stream_chunks + prev_c, d.prev_n);
+            d.prev_c = cur_c;
+            d.prev_n = d.cur_n;
+            d.cur_c  = hi;
+            d.cur_n  = 0;
         }
     }
+    const uint32_t hs       = hi << ps;
+    const bool     in_prev  = base < hs && lo == cur_c;  // cur_c is prev now
+    const uint32_t jump_end = base < hs && !in_prev ? hs : 0u;
+    if (lane == 0)
+    {
+        d.cur_n = d.cur_n + (end - max(base, hs));
+        if (in_prev) d.prev_n = d.prev_n + (hs - base);
+    }
     __syncwarp();
-    if (lane != 0) return;
-    const uint32_t n = d.prev_n + nlate;
-    if (n) add_release(a.stream_words + a.stream_chunks + prev_c, n);
-    d.defer  = d.defer | lm;
-    d.prev_c = cur_c;
-    d.prev_n = d.cur_n;
-    d.cur_c  = hi;
-    d.cur_n  = 0;
+    return jump_end;
 }
 
-// With a late list: the warp's claims are exhausted (warp-uniform call at
-// each refill after that): once, count and late-list every ray the warp
-// still holds and publish both open counts.  Later finishes are all
-// late-listed rays, so nothing is left to publish at exit.
+// The new rays below jump_end (claim_done) are counted and late-listed at
+// once; `fresh`: the lane took a new ray at this refill.  Warp-uniform call.
+__device__ __forceinline__ void jump_done(const TraceArgs& a, bool fresh, uint32_t gid, uint32_t jump_end,
+                                          uint32_t lane)
+{
+    const bool     late = fresh && gid < jump_end;
+    const uint32_t lm   = __ballot_sync(0xffffffffu, late);
+    if (!lm) return;
+    late_append(a, lm, late, gid, lane);
+    if ((int)lane == __ffs(lm) - 1)
+        add_release(a.stream_words + a.stream_chunks + ((jump_end - 1u) >> a.stream_part_shift), (uint32_t)__popc(lm));
+}
+
+// The warp's claims are exhausted (warp-uniform call at each refill after
+// that): once, late-list every ray it holds in prev or cur and publish both
+// counts.  Later finishes need no bookkeeping.
 __device__ __forceinline__ void finalize_done(const TraceArgs& a, bool holds, uint32_t gid, uint32_t lane,
                                               volatile DoneCounts& d)
 {
     if (d.fin) return;
-    const uint32_t cur_c = d.cur_c, prev_c = d.prev_c;
-    const uint32_t rc      = gid >> a.stream_part_shift;
-    const bool     late    = holds && !((d.defer >> lane) & 1u);
-    const bool     in_cur  = late && rc == cur_c;
-    const bool     in_prev = late && rc == prev_c && prev_c != cur_c;
-    const uint32_t lm      = __ballot_sync(0xffffffffu, late);
-    const uint32_t nc      = __popc(__ballot_sync(0xffffffffu, in_cur));
-    const uint32_t np      = __popc(__ballot_sync(0xffffffffu, in_prev));
+    const uint32_t rc   = gid >> a.stream_part_shift;
+    const bool     late = holds && (rc == d.cur_c || rc == d.prev_c);
+    const uint32_t lm   = __ballot_sync(0xffffffffu, late);
     if (lm) late_append(a, lm, late, gid, lane);
-    if (late && !in_cur && !in_prev) add_release(a.stream_words + a.stream_chunks + rc, 1u);
     __syncwarp();
-    if (lane == 0)
-    {
-        if (d.cur_n + nc) add_release(a.stream_words + a.stream_chunks + cur_c, d.cur_n + nc);
-        if (d.prev_n + np) add_release(a.stream_words + a.stream_chunks + prev_c, d.prev_n + np);
-        d.cur_n = d.prev_n = 0;
-        d.defer = d.defer | lm;
-        d.fin   = 1;
-    }
-    __syncwarp();
-}
-
-// Publish both open counts (lane 0); after a __syncwarp that follows the
-// counted hits' writes.
-__device__ __forceinline__ void publish_done(const TraceArgs& a, uint32_t lane, volatile DoneCounts& d)
-{
     if (lane == 0)
     {
         if (d.cur_n) add_release(a.stream_words + a.stream_chunks + d.cur_c, d.cur_n);
-        if (d.prev_n && d.prev_c != d.cur_c) add_release(a.stream_words + a.stream_chunks + d.prev_c, d.prev_n);
+        if (d.prev_n) add_release(a.stream_words + a.stream_chunks + d.prev_c, d.prev_n);
         d.cur_n = d.prev_n = 0;
+        d.fin   = 1;
     }
+    __syncwarp();
 }
 
 // A streamed ray's 32 bytes, read through L2 only: a neighbouring chunk may

@@ -128,7 +128,7 @@ def test_streamed_host_trace_bvh4(ctx, q, o):
 
 def _late_count(sc, R, chunk):
     """The late-list count of the streamed plan that last used scratch `sc`: its words sit at the end of the
-    scratch (arrival flags, one per chunk; done counters, one per part of four chunks; the give-up flag; the
+    scratch (arrival flags, one per chunk; done counters, one per part of eight chunks; the give-up flag; the
     count)."""
     shift = 17
     if chunk:
@@ -136,7 +136,7 @@ def _late_count(sc, R, chunk):
         while shift < 24 and (2 << shift) <= chunk:
             shift += 1
     chunks = -(-R // (1 << shift))
-    parts = -(-R // (1 << (shift + 2)))
+    parts = -(-R // (1 << (shift + 3)))
     wbytes = -(-(chunks + parts + 2) * 4 // 256) * 256
     woff = (sc.numel() - wbytes) // 256 * 256
     w = sc[woff:woff + wbytes].cpu().numpy().view(np.uint32)
@@ -146,7 +146,7 @@ def _late_count(sc, R, chunk):
 @pytest.mark.parametrize("trav,fmt", [(3, 0), (4, 4)])
 @pytest.mark.parametrize("q,o", [(0, 0), (1, 1)])
 def test_streamed_late_list(ctx, trav, fmt, q, o):
-    """Small parts (16,384 rays) and a full grid in flight: warps close parts while some of their rays are still
+    """Small parts (32,768 rays) and a full grid in flight: warps publish parts while some of their rays are still
     traced, and every ray in flight when the rays run out is late-listed.  Those rays' hits reach the host through
     the late scatter after the parts' copies; every hit equals the device trace's."""
     import torch
@@ -174,32 +174,14 @@ def test_streamed_late_list(ctx, trav, fmt, q, o):
     assert ctx.device_errors() == 0
 
 
-def test_streamed_without_late_list(ctx, monkeypatch):
-    """The streamed plan without the late list (RR_CUDA_LATE_LIST=0, and a pageable host hit buffer, which the
-    scatter cannot write) gives the same hits, and lists nothing."""
+def test_pageable_hit_buffer_takes_the_chunked_plan(ctx):
+    """The late scatter writes the host hit buffer from a kernel; a pageable buffer, which it cannot write, takes
+    the chunked plan, with the same hits."""
     import torch
-    from radeonrays_sdk_gb300 import rr
-    R, chunk = 300_001, 4096
+    R = 300_001
     v, i, rays = _heightfield_case(R, 14)
-    rh = torch.from_numpy(rays).pin_memory()
     bvh = ctx.build_geometry(to_dev(v), to_dev(i), node_format=4)
     want = hits_np(ctx.intersect(bvh, to_dev(rays)))
-    sc = torch.empty(ctx.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda")
-    staging = (torch.empty((R, 8), dtype=torch.float32, device="cuda"),
-               torch.full((R, 4), -1, dtype=torch.int32, device="cuda"), sc)
-    got = ctx.intersect_host(bvh, rh, chunk_rays=chunk, staging=staging, pinned_hits=False)
-    torch.cuda.synchronize()
+    got = ctx.intersect_host(bvh, torch.from_numpy(rays).pin_memory(), chunk_rays=65536, pinned_hits=False)
     assert np.array_equal(got.numpy().view(np.uint32), want)
-    assert _late_count(sc, R, chunk) == 0
-    monkeypatch.setenv("RR_CUDA_LATE_LIST", "0")
-    with rr.Context() as c2:
-        b2 = c2.build_geometry(to_dev(v), to_dev(i), node_format=4)
-        sc2 = torch.empty(c2.trace_scratch_bytes(R), dtype=torch.uint8, device="cuda")
-        st2 = (torch.empty((R, 8), dtype=torch.float32, device="cuda"),
-               torch.full((R, 4), -1, dtype=torch.int32, device="cuda"), sc2)
-        got2 = c2.intersect_host(b2, rh, chunk_rays=chunk, staging=st2)
-        torch.cuda.synchronize()
-        assert _late_count(sc2, R, chunk) == 0
-        assert c2.device_errors() == 0
-    assert np.array_equal(got2.numpy().view(np.uint32), want)
     assert ctx.device_errors() == 0
