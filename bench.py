@@ -663,8 +663,9 @@ def run_ours(args):
                "h2d_bytes_per_step": int(rays_h.numel() * 4), "d2h_bytes_per_step": int(hits_h.numel() * 4),
                "ms_per_step": total_e / args.steps,
                "api": "rrCudaCmdIntersectHostBuffers (pinned host rays/hits; one streamed persistent launch: "
-                      f"rays copied in chunks of {args.e2e_chunk or 2 ** 17:,}, hits copied out in parts of 4 "
-                      "chunks as they complete)"}
+                      f"rays copied in chunks of {args.e2e_chunk or 2 ** 17:,}, hits copied out in parts of 8 "
+                      "chunks as the kernel's warps publish them; the hits of rays still in flight at their "
+                      "part's publication written to the host by a small kernel after the trace)"}
         e2e_hits = hits_h.numpy().view(np.uint32)
         if "chosen" in out:
             # A miss writes only inst_id (isect.comp:238-244): compare the

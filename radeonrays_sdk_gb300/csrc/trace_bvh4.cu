@@ -78,30 +78,28 @@ __global__ void __launch_bounds__(kPBlock, (kQ8 && !kPrecise) ? 9 : 8)
         if (idle && (__popc(idle) >= kPRefillMin || exhausted || idle == 0xffffffffu))
         {
             int            seen     = -1;  // kStream: highest chunk known to have arrived (warp-uniform)
-            uint32_t       jump_end = 0;   // kStream: claim_done's result (warp-uniform)
+            uint32_t       jump_end = 0;   // kStream: ClaimNote::jump_end (warp-uniform)
             const uint32_t n    = exhausted ? 0u : __popc(idle);
             uint32_t       base = 0;
             if (n)
             {
                 const int leader = __ffs(idle) - 1;
-                if ((int)lane == leader) base = atomicAdd(ray_ctr, n);
+                ClaimNote note{-1, kInvalid, 0u};
+                if ((int)lane == leader)
+                {
+                    base = atomicAdd(ray_ctr, n);
+                    // The streamed variant's arrival wait and claim counts
+                    // (trace_stream.cuh), by the claiming lane alone.
+                    if (kStream && base < count) note = claim_leader(a, base, min(base + n, count), &s_seen, dc);
+                }
                 base      = __shfl_sync(0xffffffffu, base, leader);
                 exhausted = base + n >= count;
                 if (kStream && base < count)
                 {
-                    const int hi  = (int)((min(base + n, count) - 1u) >> a.stream_shift);
-                    int       top = -1;
-                    if ((int)lane == leader)
-                    {
-                        top = *reinterpret_cast<volatile int*>(&s_seen);
-                        if (top < hi)
-                        {
-                            top = wait_arrival(a, (uint32_t)hi);
-                            if (top >= 0) atomicMax(&s_seen, top);
-                        }
-                    }
-                    seen = __shfl_sync(0xffffffffu, top, leader);
-                    jump_end = claim_done(a, base, min(base + n, count), active || pending, gid, lane, dc);
+                    seen                     = __shfl_sync(0xffffffffu, note.seen, leader);
+                    jump_end                 = __shfl_sync(0xffffffffu, note.jump_end, leader);
+                    const uint32_t late_part = __shfl_sync(0xffffffffu, note.late_part, leader);
+                    if (late_part != kInvalid) late_held(a, active || pending, gid, late_part, lane);
                 }
             }
             bool fresh = false;  // kStream: took a new ray at this refill

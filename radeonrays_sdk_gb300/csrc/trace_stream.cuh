@@ -83,8 +83,9 @@ __device__ __noinline__ static void add_release(uint32_t* p, uint32_t v)
 // rays take, and the last parts leave while the kernel drains.
 // A release add waits until the SM's earlier stores are visible, which costs
 // microseconds, so a warp issues one about once per part it works on.  The
-// counts live in shared memory (one record per warp, written by lane 0 only)
-// so that no register stays live across the traversal step for them.
+// counts live in shared memory (one record per warp, written by one lane at
+// a time: the refill's claiming lane, or lane 0 at exhaustion) so that no
+// register stays live across the traversal step for them.
 struct DoneCounts
 {
     uint32_t cur_c, cur_n, prev_c, prev_n, fin;
@@ -102,50 +103,70 @@ __device__ __forceinline__ void late_append(const TraceArgs& a, uint32_t m, bool
     if (mine && slot < a.ray_count) a.stream_late[slot] = gid;
 }
 
-// The warp claimed rays [base, end) (all 32 lanes call it, before the new
-// rays are given out; `holds`/gid: the lane's current ray, not yet
-// counted-and-written).  A claim spans at most two parts (it is at most 32
-// rays; a part is at least 2^15).  When it reaches a part beyond cur, prev is
-// published (its held rays late-listed) and the counts shift.  The new rays
-// are then counted in cur, or in prev when they lie there.  Returns the end of
-// the claim's rays that lie in neither (0 if none): the claim skipped a whole
-// part, so those rays' part will not be published by this warp; jump_done
-// counts and late-lists them at once.
-__device__ __forceinline__ uint32_t claim_done(const TraceArgs& a, uint32_t base, uint32_t end, bool holds,
-                                               uint32_t gid, uint32_t lane, volatile DoneCounts& d)
+// What the lane that claimed a refill's rays tells its warp (claim_leader).
+struct ClaimNote
 {
-    const uint32_t ps = a.stream_part_shift;
-    const uint32_t hi = (end - 1u) >> ps, lo = base >> ps;
+    int      seen;       // highest chunk known to have arrived
+    uint32_t late_part;  // part just published (its held rays are late-listed), or kInvalid
+    uint32_t jump_end;   // new rays below this lie in neither open part (0: none)
+};
+
+// Run by the lane that claimed rays [base, end) at a refill, right after its
+// atomic: waits (bounded, once per block and chunk) for the arrival of the
+// claim's last chunk, then keeps the warp's claim counts.  A claim spans at
+// most two parts (it is at most 32 rays; a part is at least 2^15).  When it
+// reaches a part beyond cur, prev is published and the counts shift; the
+// warp then late-lists the rays it holds in the published part
+// (late_held: their hits, written later, reach the host through the late
+// scatter).  The new rays are counted in cur, or in prev when they lie
+// there; rays in neither (the claim skipped a whole part, so this warp will
+// not publish theirs) are counted and late-listed at once (jump_done).
+// One lane does all of it, so the refill pays for one divergent block.
+__device__ __forceinline__ ClaimNote claim_leader(const TraceArgs& a, uint32_t base, uint32_t end, int* s_seen,
+                                                  volatile DoneCounts& d)
+{
+    ClaimNote      c;
+    const int      hc  = (int)((end - 1u) >> a.stream_shift);
+    int            top = *reinterpret_cast<volatile int*>(s_seen);
+    if (top < hc)
+    {
+        top = wait_arrival(a, (uint32_t)hc);
+        if (top >= 0) atomicMax(s_seen, top);
+    }
+    c.seen              = top;
+    const uint32_t ps   = a.stream_part_shift;
+    const uint32_t hi   = (end - 1u) >> ps, lo = base >> ps;
     const uint32_t cur_c = d.cur_c;
+    c.late_part          = kInvalid;
     if (hi > cur_c)
     {
-        const uint32_t prev_c = d.prev_c;
-        const bool     late   = holds && (gid >> ps) == prev_c;
-        const uint32_t lm     = __ballot_sync(0xffffffffu, late);
-        if (lm) late_append(a, lm, late, gid, lane);
-        __syncwarp();
-        if (lane == 0)
-        {
-            if (d.prev_n) add_release(a.stream_words + a.stream_chunks + prev_c, d.prev_n);
-            d.prev_c = cur_c;
-            d.prev_n = d.cur_n;
-            d.cur_c  = hi;
-            d.cur_n  = 0;
-        }
+        const uint32_t prev_c = d.prev_c, prev_n = d.prev_n;
+        if (prev_n) add_release(a.stream_words + a.stream_chunks + prev_c, prev_n);
+        c.late_part = prev_c;
+        d.prev_c    = cur_c;
+        d.prev_n    = d.cur_n;
+        d.cur_c     = hi;
+        d.cur_n     = 0;
     }
-    const uint32_t hs       = hi << ps;
-    const bool     in_prev  = base < hs && lo == cur_c;  // cur_c is prev now
-    const uint32_t jump_end = base < hs && !in_prev ? hs : 0u;
-    if (lane == 0)
-    {
-        d.cur_n = d.cur_n + (end - max(base, hs));
-        if (in_prev) d.prev_n = d.prev_n + (hs - base);
-    }
-    __syncwarp();
-    return jump_end;
+    const uint32_t hs      = hi << ps;
+    const bool     in_prev = base < hs && lo == cur_c;  // cur_c is prev now
+    c.jump_end             = base < hs && !in_prev ? hs : 0u;
+    d.cur_n                = d.cur_n + (end - max(base, hs));
+    if (in_prev) d.prev_n = d.prev_n + (hs - base);
+    return c;
 }
 
-// The new rays below jump_end (claim_done) are counted and late-listed at
+// All lanes, after a claim published part p (ClaimNote::late_part): the
+// rays the warp still holds there (in flight, or finished with the hit not
+// yet written: `holds`) go to the late list.
+__device__ __forceinline__ void late_held(const TraceArgs& a, bool holds, uint32_t gid, uint32_t p, uint32_t lane)
+{
+    const bool     late = holds && (gid >> a.stream_part_shift) == p;
+    const uint32_t lm   = __ballot_sync(0xffffffffu, late);
+    if (lm) late_append(a, lm, late, gid, lane);
+}
+
+// The new rays below jump_end (claim_leader) are counted and late-listed at
 // once; `fresh`: the lane took a new ray at this refill.  Warp-uniform call.
 __device__ __forceinline__ void jump_done(const TraceArgs& a, bool fresh, uint32_t gid, uint32_t jump_end,
                                           uint32_t lane)
