@@ -3,7 +3,7 @@
 // scene.cu).  Node format and conservativeness argument: wide.cu.
 //
 // Per node: the 8 child boxes are decoded to fp32 (fma(q, 2^e, p), exact
-// byte -> float via a PRMT-built 2^23 + q) and slab-tested with the
+// byte -> float via a PRMT-built 2^15 + q) and slab-tested with the
 // reference's formula (vlk/kernels/common.h:150-164), evaluating only the
 // near plane and the far plane of each axis (chosen by the sign of the
 // inverse direction, which yields exactly the reference's min/max result).
@@ -177,14 +177,17 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
 
     // Slab distances in quantised space.  For a plane at byte q of axis a the
     // reference evaluates fma(c, inv, oxi) on the child coordinate c; here
-    //   t = fma(2^23 + q, A, B -+ eps),  A = 2^e * inv (exact),
-    //   B = fma(p, inv, oxi) - 2^23 * A (rounded),
-    // with eps = 1.25 |A| + 2^-20 |B| on the near (-) and far (+) planes.  eps
-    // bounds the rounding of B, of B - 2^23 A and of B -+ eps (each at most
-    // |A| / 2 + 2^-24 |B|); as the decoded coordinate lies outside the exact
-    // child bound and rounding is monotone, the near distance never exceeds
-    // the reference's on the exact box and the far distance is never below it.
-    // A ray the reference's test admits is therefore always admitted.
+    //   t = fma(2^15 + q, A, B -+ eps),  A = 2^e * inv (exact),
+    //   B = fma(p, inv, oxi) - 2^15 * A (rounded),
+    // with eps = 2^-7 |A| + 2^-20 |B| on the near (-) and far (+) planes.  eps
+    // bounds the rounding of B, of B - 2^15 A and of B -+ eps (together at
+    // most 2^-8 |A| + 2^-22 |B|: the magic 2^15 + q, placed in the second
+    // mantissa byte, keeps B - 2^15 A within 2^15 |A| + |B|, where 2^23 + q
+    // cost half a quantisation step); as the decoded coordinate lies outside
+    // the exact child bound and rounding is monotone, the near distance never
+    // exceeds the reference's on the exact box and the far distance is never
+    // below it.  A ray the reference's test admits is therefore always
+    // admitted.  (The 2^23 form with eps = 1.25 |A| visited 7 % more nodes.)
     float An[3], Bn[3], Bf[3];
     {
         const float s3[3] = {sx, sy, sz}, p3[3] = {px, py, pz}, i3[3] = {inv.x, inv.y, inv.z},
@@ -194,8 +197,8 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
         {
             const float A   = s3[k] * i3[k];
             const float B   = fmaf(p3[k], i3[k], o3[k]);
-            const float eps = fmaf(fabsf(A), 1.25f, fabsf(B) * 9.5367431640625e-07f);
-            const float M   = fmaf(-8388608.0f, A, B);
+            const float eps = fmaf(fabsf(A), 0.0078125f, fabsf(B) * 9.5367431640625e-07f);
+            const float M   = fmaf(-32768.0f, A, B);
             An[k]           = A;
             Bn[k]           = M - eps;
             Bf[k]           = M + eps;
@@ -204,7 +207,7 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
     // Hit bits per visit position; empty slots are masked out below through
     // the meta bytes (internal: bit 7; leaf: bit 7 clear, count in bits 5-6).
     uint32_t hits = 0;
-#define RR_WIDE_Q(w, b) __int_as_float((int)__byte_perm((w), 0x4B000000u, 0x7540u | (b)))
+#define RR_WIDE_Q(w, b) __int_as_float((int)__byte_perm((w), 0x47000000u, 0x7504u | ((b) << 4)))
 #define RR_WIDE_CHILD(i, W)                                                                                         \
     {                                                                                                               \
         const float tnx = fmaf(RR_WIDE_Q(W##nx, (i) & 3), An[0], Bn[0]);                                            \
