@@ -187,7 +187,9 @@ __device__ __forceinline__ bool wide_step(WideRay& s, const WideNode* __restrict
     // the exact child bound and rounding is monotone, the near distance never
     // exceeds the reference's on the exact box and the far distance is never
     // below it.  A ray the reference's test admits is therefore always
-    // admitted.  (The 2^23 form with eps = 1.25 |A| visited 7 % more nodes.)
+    // admitted.  (The 2^23 form with eps = 1.25 |A| visited 7 % more nodes.
+    // Directed roundings instead of eps, as in the 4-wide kernel, were 1.6 %
+    // slower here.)
     float An[3], Bn[3], Bf[3];
     {
         const float s3[3] = {sx, sy, sz}, p3[3] = {px, py, pz}, i3[3] = {inv.x, inv.y, inv.z},
