@@ -150,11 +150,11 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
 // 2^-7 |A| + 2^-20 |B| took 6 more instructions per node, 0.4 % slower.)
 //
 // kRobust (the precise triangle test's traversal): `inv` is the exact
-// reciprocal and `oxi` the origin.  Each plane is decoded to p + q 2^e with
-// the fma rounded down (lo planes) or up (hi planes), so the decoded box
-// still contains the exact child box, and is then tested with the robust
-// slab distances of b4_children<true>: a child box the exact ray segment
-// touches is never culled.
+// reciprocal and `oxi` the origin.  Each plane is decoded to at most (lo
+// planes) or at least (hi planes) p + q 2^e by directed roundings, so the
+// decoded box still contains the exact child box, and is then tested with
+// the robust slab distances of b4_children<true>: a child box the exact ray
+// segment touches is never culled.
 template <bool kRobust = false>
 __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct)
 {
@@ -167,28 +167,41 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
     const uint32_t nzw = sz ? q1.y : q0.z, fzw = sz ? q0.z : q1.y;
     if (kRobust)
     {
-        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-        const float ex = __uint_as_float((w0.w & 0xffu) << 23), ey = __uint_as_float(((w0.w >> 8) & 0xffu) << 23),
-                    ez = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
-        // Byte c of a plane word as a float (exact: 2^23 + q - 2^23).
-        auto qf = [](uint32_t w, int c) {
-            return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | c)) - 8388608.0f;
-        };
-        // The near plane of an axis is lo for a non-negative direction.
-        auto plane = [](float q, float e, float o, bool is_lo) {
-            return is_lo ? __fmaf_rd(q, e, o) : __fmaf_ru(q, e, o);
-        };
+        // An axis with a negative direction is mirrored (x -> -x, o -> -o,
+        // inv -> -inv: the slab distances are the same fp32 operations), so
+        // that its near plane (the hi plane) is evaluated as a lo plane.  In
+        // mirrored coordinates every near plane is decoded rounded down and
+        // every far plane rounded up, each as one fma on 2^15 + q:
+        //   plane = fma(2^15 + q, g, P),  g = +-2^e,
+        //   P = p - 2^15 2^e rounded down (near) or up (far), mirrored,
+        // so the decoded box still contains the exact child box.
+        const float g[3] = {__uint_as_float((w0.w & 0xffu) << 23), __uint_as_float(((w0.w >> 8) & 0xffu) << 23),
+                            __uint_as_float(((w0.w >> 16) & 0xffu) << 23)};
+        const float p3[3] = {__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z)};
+        const bool  s3[3] = {sx, sy, sz};
+        const float o3[3] = {oxi.x, oxi.y, oxi.z}, i3[3] = {inv.x, inv.y, inv.z};
+        float       G[3], Pn[3], Pf[3], O[3], I[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const float lo = __fadd_rd(p3[k], -32768.0f * g[k]), hi = __fadd_ru(p3[k], -32768.0f * g[k]);
+            G[k]  = s3[k] ? -g[k] : g[k];
+            Pn[k] = s3[k] ? -hi : lo;
+            Pf[k] = s3[k] ? -lo : hi;
+            O[k]  = s3[k] ? -o3[k] : o3[k];
+            I[k]  = s3[k] ? -i3[k] : i3[k];
+        }
+#define RR_B4Q(w, c) __int_as_float((int)__byte_perm((w), 0x47000000u, 0x7504u | ((c) << 4)))
         auto key = [&](int c, uint32_t r) {
-            const float ax = plane(qf(nxw, c), ex, px, !sx), ay = plane(qf(nyw, c), ey, py, !sy),
-                        az = plane(qf(nzw, c), ez, pz, !sz);
-            const float bx = plane(qf(fxw, c), ex, px, sx), by = plane(qf(fyw, c), ey, py, sy),
-                        bz = plane(qf(fzw, c), ez, pz, sz);
-            const float t0 =
-                fmaxf(b4_max3((ax - oxi.x) * inv.x, (ay - oxi.y) * inv.y, (az - oxi.z) * inv.z), tmin);
-            const float t1 =
-                robust_far(fminf(b4_min3((bx - oxi.x) * inv.x, (by - oxi.y) * inv.y, (bz - oxi.z) * inv.z), ct));
+            const float ax = __fmaf_rd(RR_B4Q(nxw, c), G[0], Pn[0]), ay = __fmaf_rd(RR_B4Q(nyw, c), G[1], Pn[1]),
+                        az = __fmaf_rd(RR_B4Q(nzw, c), G[2], Pn[2]);
+            const float bx = __fmaf_ru(RR_B4Q(fxw, c), G[0], Pf[0]), by = __fmaf_ru(RR_B4Q(fyw, c), G[1], Pf[1]),
+                        bz = __fmaf_ru(RR_B4Q(fzw, c), G[2], Pf[2]);
+            const float t0 = fmaxf(b4_max3((ax - O[0]) * I[0], (ay - O[1]) * I[1], (az - O[2]) * I[2]), tmin);
+            const float t1 = robust_far(fminf(b4_min3((bx - O[0]) * I[0], (by - O[1]) * I[1], (bz - O[2]) * I[2]), ct));
             return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
         };
+#undef RR_B4Q
         float  k0 = key(0, cr.x), k1 = key(1, cr.y), k2 = key(2, cr.z), k3 = key(3, cr.w);
         B4Hits h;
         h.r0 = cr.x;
