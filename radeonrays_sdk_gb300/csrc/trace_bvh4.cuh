@@ -155,7 +155,7 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
 // decoded box still contains the exact child box, and is then tested with
 // the robust slab distances of b4_children<true>: a child box the exact ray
 // segment touches is never culled.
-template <bool kRobust = false>
+template <bool kRobust = false, bool kSort = true>
 __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct)
 {
     const uint4* p  = reinterpret_cast<const uint4*>(node);
@@ -247,6 +247,12 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
     h.r1 = cr.y;
     h.r2 = cr.z;
     h.r3 = cr.w;
+    if (!kSort)
+    {
+        // Hit mask in n, slots as stored (b4_descend_mask).
+        h.n = (k0 < INFINITY ? 1 : 0) | (k1 < INFINITY ? 2 : 0) | (k2 < INFINITY ? 4 : 0) | (k3 < INFINITY ? 8 : 0);
+        return h;
+    }
     h.n  = (k0 < INFINITY) + (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
     b4_cas(k0, h.r0, k1, h.r1);
     b4_cas(k2, h.r2, k3, h.r3);
@@ -266,6 +272,23 @@ __device__ __forceinline__ uint32_t b4_descend(const B4Hits& h, int& sp, uint32_
     if (h.n > 2) st.at(sp++) = h.r2;
     if (h.n > 1) st.at(sp++) = h.r1;
     return h.r0;
+}
+
+// Any-hit order over quantised nodes: the first hit slot is visited next, the
+// other hit slots are pushed (lowest slot on top); h.n holds the hit mask
+// (b4q_children with kSort = false).  An occlusion query stops at any hit, so
+// it skips the nearest-first sort: measured on the 16.8 M-ray heightfield
+// with tmax ~ U[0.01, 0.5], 1.3 % more node fetches and 2.5 % faster.
+__device__ __forceinline__ uint32_t b4_descend_mask(const B4Hits& h, int& sp, uint32_t& gsp, const PStack& st,
+                                                    DeviceWords* words)
+{
+    const uint32_t m     = (uint32_t)h.n;
+    const int      first = __ffs(m) - 1;
+    b4_reserve(sp, gsp, st, words, __popc(m) - 1);
+    if ((m & 8u) && first != 3) st.at(sp++) = h.r3;
+    if ((m & 4u) && first != 2) st.at(sp++) = h.r2;
+    if ((m & 2u) && first != 1) st.at(sp++) = h.r1;
+    return first == 0 ? h.r0 : first == 1 ? h.r1 : first == 2 ? h.r2 : h.r3;
 }
 
 // Traversal state of one ray of the 4-wide kernels (kept in registers between
@@ -351,13 +374,14 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        const B4Hits h = kQ8 ? b4q_children<kPrecise>(reinterpret_cast<const Bvh4QNode*>(wn) + idx, s.inv, s.oxi,
-                                                      s.ray.tmin, s.ct)
-                             : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
+        constexpr bool kMask = kAny && kQ8 && !kPrecise;
+        const B4Hits   h     = kQ8 ? b4q_children<kPrecise, !kMask>(reinterpret_cast<const Bvh4QNode*>(wn) + idx,
+                                                                  s.inv, s.oxi, s.ray.tmin, s.ct)
+                                   : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
         if (h.n)
         {
-            s.ref = b4_descend(h, s.sp, s.gsp, st, words);
+            s.ref = kMask ? b4_descend_mask(h, s.sp, s.gsp, st, words) : b4_descend(h, s.sp, s.gsp, st, words);
             pop   = false;
         }
     }
