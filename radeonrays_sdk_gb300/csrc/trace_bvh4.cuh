@@ -135,19 +135,19 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
 // The same test on a quantised node (Bvh4QNode, four 16-byte loads instead of
 // seven): each child plane decodes exactly to 2^15 + q (byte q permuted into
 // the second mantissa byte of 2^15, no conversion) and is evaluated as
-// fma(2^15 + q, A, B) with A = 2^e * inv (exact) and
-// B = fma(-2^15, A, fma(p, inv, oxi)), on the near and far planes picked by
-// the direction's signs.  On the near planes every fma rounds down, on the
-// far planes up.  The real value p + q 2^e of a decoded plane lies on the
-// outside of the exact child plane x, so the near distance is at most the
-// real (x - o) inv with the ray's oxi, and rounding down keeps it at most the
-// reference's fma(x, inv, oxi) rounded to nearest; the far distance is at
-// least the reference's likewise.  A child the reference's slab test admits
-// on its exact box is therefore always admitted, with no margin beyond the
-// directed roundings.  (The magic 2^23 + q, byte in the low mantissa byte,
-// with a margin of 1.25 |A| for rounding to nearest, visited 5 % more nodes
-// on the 16.8 M-ray heightfield and was 5 % slower; 2^15 + q with the margin
-// 2^-7 |A| + 2^-20 |B| took 6 more instructions per node, 0.4 % slower.)
+// fma(2^15 + q, A, B -+ eps) with A = 2^e * inv (exact) and
+// B = fma(p, inv, oxi) - 2^15 A, on the near (-) and far (+) planes picked by
+// the direction's signs.  eps = 2^-7 |A| + 2^-20 |B| bounds the roundings of
+// B, of B - 2^15 A and of B -+ eps (together at most 2^-8 |A| + 2^-22 |B|),
+// so the near distance is never above the reference's on the exact child box
+// and the far distance never below it (the argument of the 8-wide kernel,
+// trace_wide.cuh): a child the reference's slab test admits on its exact box
+// is always admitted.  The magic 2^23 + q (byte in the low mantissa byte)
+// would round B - 2^23 A to half a quantisation step and need eps = 1.25 |A|:
+// measured on the 16.8 M-ray heightfield, 5 % more node fetches and 5 %
+// slower.  Directed roundings instead of eps (every fma rounded down on the
+// near planes, up on the far ones) made the resident kernel 0.4 % faster but
+// its streamed variant 16 % slower (5.26 against 4.53 ms per e2e step).
 //
 // kRobust (the precise triangle test's traversal): `inv` is the exact
 // reciprocal and `oxi` the origin.  Each plane is decoded to at most (lo
@@ -155,8 +155,9 @@ __device__ __forceinline__ B4Hits b4_children(const Bvh4Node* node, F3 inv, F3 o
 // decoded box still contains the exact child box, and is then tested with
 // the robust slab distances of b4_children<true>: a child box the exact ray
 // segment touches is never culled.
-template <bool kRobust = false, bool kSort = true>
-__device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct)
+template <bool kRobust = false>
+__device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3 oxi, float tmin, float ct,
+                                               bool sort = true)
 {
     const uint4* p  = reinterpret_cast<const uint4*>(node);
     const uint4  w0 = __ldg(p), cr = __ldg(p + 1), q0 = __ldg(p + 2), q1 = __ldg(p + 3);
@@ -225,18 +226,21 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
         {
             const float sc  = __uint_as_float(((w0.w >> (8 * k)) & 0xffu) << 23);
             const float a   = sc * i3[k];
+            const float b   = fmaf(p3[k], i3[k], o3[k]);
+            const float eps = fmaf(fabsf(a), 0.0078125f, fabsf(b) * 9.5367431640625e-07f);
+            const float m   = fmaf(-32768.0f, a, b);
             A[k]            = a;
-            Bn[k]           = __fmaf_rd(-32768.0f, a, __fmaf_rd(p3[k], i3[k], o3[k]));
-            Bf[k]           = __fmaf_ru(-32768.0f, a, __fmaf_ru(p3[k], i3[k], o3[k]));
+            Bn[k]           = m - eps;
+            Bf[k]           = m + eps;
         }
     }
 #define RR_B4Q(w, c) __int_as_float((int)__byte_perm((w), 0x47000000u, 0x7504u | ((c) << 4)))
     auto key = [&](int c, uint32_t r) {
-        const float t0 = fmaxf(b4_max3(__fmaf_rd(RR_B4Q(nxw, c), A[0], Bn[0]), __fmaf_rd(RR_B4Q(nyw, c), A[1], Bn[1]),
-                                       __fmaf_rd(RR_B4Q(nzw, c), A[2], Bn[2])),
+        const float t0 = fmaxf(b4_max3(fmaf(RR_B4Q(nxw, c), A[0], Bn[0]), fmaf(RR_B4Q(nyw, c), A[1], Bn[1]),
+                                       fmaf(RR_B4Q(nzw, c), A[2], Bn[2])),
                                tmin);
-        const float t1 = fminf(b4_min3(__fmaf_ru(RR_B4Q(fxw, c), A[0], Bf[0]), __fmaf_ru(RR_B4Q(fyw, c), A[1], Bf[1]),
-                                       __fmaf_ru(RR_B4Q(fzw, c), A[2], Bf[2])),
+        const float t1 = fminf(b4_min3(fmaf(RR_B4Q(fxw, c), A[0], Bf[0]), fmaf(RR_B4Q(fyw, c), A[1], Bf[1]),
+                                       fmaf(RR_B4Q(fzw, c), A[2], Bf[2])),
                                ct);
         return (t0 <= t1 && r != kInvalid) ? t0 : INFINITY;
     };
@@ -247,7 +251,7 @@ __device__ __forceinline__ B4Hits b4q_children(const Bvh4QNode* node, F3 inv, F3
     h.r1 = cr.y;
     h.r2 = cr.z;
     h.r3 = cr.w;
-    if (!kSort)
+    if (!sort)
     {
         // Hit mask in n, slots as stored (b4_descend_mask).
         h.n = (k0 < INFINITY ? 1 : 0) | (k1 < INFINITY ? 2 : 0) | (k2 < INFINITY ? 4 : 0) | (k3 < INFINITY ? 8 : 0);
@@ -276,7 +280,7 @@ __device__ __forceinline__ uint32_t b4_descend(const B4Hits& h, int& sp, uint32_
 
 // Any-hit order over quantised nodes: the first hit slot is visited next, the
 // other hit slots are pushed (lowest slot on top); h.n holds the hit mask
-// (b4q_children with kSort = false).  An occlusion query stops at any hit, so
+// (b4q_children with sort = false).  An occlusion query stops at any hit, so
 // it skips the nearest-first sort: measured on the 16.8 M-ray heightfield
 // with tmax ~ U[0.01, 0.5], 1.3 % more node fetches and 2.5 % faster.
 __device__ __forceinline__ uint32_t b4_descend_mask(const B4Hits& h, int& sp, uint32_t& gsp, const PStack& st,
@@ -374,14 +378,17 @@ __device__ __forceinline__ bool b4_step(B4Ray& s, const Bvh4Node* __restrict__ w
     }
     else
     {
-        constexpr bool kMask = kAny && kQ8 && !kPrecise;
-        const B4Hits   h     = kQ8 ? b4q_children<kPrecise, !kMask>(reinterpret_cast<const Bvh4QNode*>(wn) + idx,
-                                                                  s.inv, s.oxi, s.ray.tmin, s.ct)
-                                   : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
+        // Any-hit queries over quantised nodes take the unsorted order (the
+        // multi-request kernel decides per ray, so that a request's hits
+        // equal its trace alone).
+        const bool   mask = kQ8 && !kPrecise && (kAny || (kRuntime && any));
+        const B4Hits h    = kQ8 ? b4q_children<kPrecise>(reinterpret_cast<const Bvh4QNode*>(wn) + idx, s.inv, s.oxi,
+                                                         s.ray.tmin, s.ct, !mask)
+                                : b4_children<kPrecise>(wn + idx, s.inv, s.oxi, s.ray.tmin, s.ct);
         ++nf;
         if (h.n)
         {
-            s.ref = kMask ? b4_descend_mask(h, s.sp, s.gsp, st, words) : b4_descend(h, s.sp, s.gsp, st, words);
+            s.ref = mask ? b4_descend_mask(h, s.sp, s.gsp, st, words) : b4_descend(h, s.sp, s.gsp, st, words);
             pop   = false;
         }
     }
