@@ -459,7 +459,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     build["update"] = {"ms": statistics.median(u_per), "mtris_s": ntri / statistics.median(u_per) / 1e3,
                        "operation": "RR_BUILD_OPERATION_UPDATE: leaves take the new vertices, atomic refit, "
-                                    "4-wide collapse again"}
+                                    "4-wide nodes requantised in place (topology kept)"}
     del v_up
     # The chosen path traces a quality build (flags without PREFER_FAST_BUILD:
     # LBVH + treelet restructure); the plain path the reference's fast LBVH.

@@ -14,7 +14,7 @@ namespace rr
 constexpr uint32_t kInvalid     = 0xffffffffu;  // vlk/kernels/common.h:20 RR_INVALID_ADDR
 constexpr uint32_t kSentinel    = 0xfffffffeu;  // vlk/kernels/isect_2l.comp:28
 constexpr uint32_t kMagic       = 0x52524742u;  // "RRGB": trailer tag of a result buffer
-constexpr uint32_t kVersion     = 1;
+constexpr uint32_t kVersion     = 2;  // 2: 4-wide nodes record their binary node (the update reads it)
 constexpr uint32_t kKindGeom    = 1;
 constexpr uint32_t kKindScene   = 2;
 constexpr size_t   kAlign       = 256;
@@ -447,6 +447,9 @@ size_t trace_scratch_bytes(uint32_t ray_count);
 // After a streamed trace: copies the hit records of the late-listed rays
 // (count at *late_count, at most cap) from dev_hits to host_hits (a
 // device-accessible pointer to the host buffer), rec_bytes (4 or 16) each.
+// RR_BUILD_OPERATION_UPDATE of a buffer with 4-wide nodes, after the binary
+// refit: each 4-wide node takes its children's new boxes (same topology).
+cudaError_t launch_refit_bvh4(uint8_t* result, const GeomLayout& L, DeviceWords* words, int sm_count, cudaStream_t s);
 cudaError_t launch_late_scatter(const uint32_t* late_count, const uint32_t* late, uint32_t cap,
                                 const uint8_t* dev_hits, uint8_t* host_hits, uint32_t rec_bytes, int sm_count,
                                 cudaStream_t s);

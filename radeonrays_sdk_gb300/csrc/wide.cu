@@ -135,6 +135,43 @@ __device__ __forceinline__ int pick_exp(float lo, float hi)
     return ex;
 }
 
+// The quantised 4-wide node of child boxes cb[0..nc-1] (slots nc..3 empty):
+// the frame of their union, bounds rounded outward.  The collapse and the
+// update's requantisation (k_refit_bvh4) both write nodes through it.
+__device__ __forceinline__ void quantize4(Bvh4QNode& o, const Bx* cb, int nc)
+{
+    Bx u = cb[0];
+#pragma unroll
+    for (int k = 1; k < 4; ++k)
+        if (k < nc)
+            for (int a = 0; a < 3; ++a)
+            {
+                u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+                u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+            }
+    float iv[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        o.p[a]  = u.lo[a];
+        int e   = pick_exp(u.lo[a], u.hi[a]);
+        o.e[a]  = (uint8_t)e;
+        iv[a]   = __uint_as_float((uint32_t)(254 - e) << 23);
+    }
+    o.pad0 = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const bool used = k < nc;
+        for (int a = 0; a < 3; ++a)
+        {
+            const float ql = used ? floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], o.p[a]), iv[a])) : 0.f;
+            const float qh = used ? ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], o.p[a]), iv[a])) : 0.f;
+            o.q[a][k]     = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
+            o.q[3 + a][k] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
+        }
+    }
+}
+
 // Per-geometry views of a fused build's collapse state.
 __device__ __forceinline__ CollapseCtl* ctl_of(const BuildItem& it)
 {
@@ -488,39 +525,16 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
         {
             // Quantised 4-wide node: the frame of the union of the child
             // boxes, bounds rounded outward as for the 8-wide node (below),
-            // children numbered as in the fp32 4-wide node.
+            // children numbered as in the fp32 4-wide node.  pad1[0] keeps
+            // the node's binary node, for the update's requantisation.
             Bvh4QNode o;
-            Bx        u = cb[0];
-#pragma unroll
-            for (int k = 1; k < W; ++k)
-                if (k < nc)
-                    for (int a = 0; a < 3; ++a)
-                    {
-                        u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
-                        u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
-                    }
-            float iv[3];
-            for (int a = 0; a < 3; ++a)
-            {
-                o.p[a]  = u.lo[a];
-                int e   = pick_exp(u.lo[a], u.hi[a]);
-                o.e[a]  = (uint8_t)e;
-                iv[a]   = __uint_as_float((uint32_t)(254 - e) << 23);
-            }
-            o.pad0    = 0;
-            o.pad1[0] = o.pad1[1] = 0;
+            quantize4(o, cb, nc);
+            o.pad1[0] = item.b;
+            o.pad1[1] = 0;
             uint32_t ri = 0;
             for (int k = 0; k < 4; ++k)
             {
-                const bool used = k < nc;
-                for (int a = 0; a < 3; ++a)
-                {
-                    const float ql = used ? floorf(__fmul_rd(__fsub_rd(cb[k].lo[a], o.p[a]), iv[a])) : 0.f;
-                    const float qh = used ? ceilf(__fmul_ru(__fsub_ru(cb[k].hi[a], o.p[a]), iv[a])) : 0.f;
-                    o.q[a][k]     = (uint8_t)fminf(fmaxf(ql, 0.f), 255.f);
-                    o.q[3 + a][k] = (uint8_t)fminf(fmaxf(qh, 0.f), 255.f);
-                }
-                if (!used)
+                if (k >= nc)
                     o.child[k] = kInvalid;
                 else if (cint[k])
                 {
@@ -559,7 +573,7 @@ __device__ __forceinline__ void collapse_pass(const BatchArgs& b, int level, Dev
                 }
                 else
                     o.child[k] = kBvh4Leaf | ch[k];
-                o.pad[k] = 0;
+                o.pad[k] = k == 0 ? item.b : 0u;  // pad[0]: the node's binary node (the update reads it)
             }
             reinterpret_cast<Bvh4Node*>(bi->result + bi->wide_off)[item.w] = o;
             continue;
@@ -722,6 +736,86 @@ __global__ void k_collapse_finish(BatchArgs b, DeviceWords* words)
     tr->wide_tri_count = ctl->tri_count;
 }
 
+// The update of a buffer with 4-wide nodes (RR_BUILD_OPERATION_UPDATE, after
+// the binary refit): the 4-wide topology stays, and every node takes its
+// children's new boxes.  One thread per 4-wide node: a leaf child's box is its
+// binary leaf's, an internal child's that of the binary node the child stands
+// for (recorded in the child's pad word by the collapse).  Written like the
+// collapse writes them (quantize4 for 8-bit bounds).  Indices out of range
+// raise NODE_RANGE and leave the node as it was.
+template <bool kQ8>
+__global__ void __launch_bounds__(256) k_refit_bvh4(uint8_t* wide, const BvhNode* nodes, uint32_t n,
+                                                     const Trailer* tr, uint32_t capacity, DeviceWords* words)
+{
+    const uint32_t count = min(tr->wide_count, capacity);
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < count; x += gridDim.x * blockDim.x)
+    {
+        uint32_t child[4];
+        if (kQ8)
+        {
+            const uint4 c = __ldcg(reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4QNode)) + 1);
+            child[0] = c.x, child[1] = c.y, child[2] = c.z, child[3] = c.w;
+        }
+        else
+        {
+            const uint4 c = __ldcg(reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4Node)) + 6);
+            child[0] = c.x, child[1] = c.y, child[2] = c.z, child[3] = c.w;
+        }
+        Bx   cb[4];
+        int  nc = 0;
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const uint32_t r = child[k];
+            if (r == kInvalid) break;  // the collapse packs the children into the first slots
+            uint32_t b;
+            if (r & kBvh4Leaf)
+                b = r & ~kBvh4Leaf;
+            else if (r < count)
+                b = kQ8 ? __ldcg(reinterpret_cast<const uint32_t*>(wide + (size_t)r * sizeof(Bvh4QNode) + 56))
+                        : __ldcg(reinterpret_cast<const uint32_t*>(wide + (size_t)r * sizeof(Bvh4Node) + 112));
+            else
+                b = kInvalid;
+            if (b >= 2 * n - 1)
+            {
+                ok = false;
+                continue;
+            }
+            cb[nc++] = node_union(load_node(nodes, b));
+        }
+        if (!ok || nc == 0)
+        {
+            atomicOr(&words->error_bits, (uint32_t)RR_CUDA_DEVICE_ERROR_NODE_RANGE);
+            continue;
+        }
+        if (kQ8)
+        {
+            Bvh4QNode* o = reinterpret_cast<Bvh4QNode*>(wide) + x;
+            Bvh4QNode  q;
+            quantize4(q, cb, nc);
+            // Frame and planes only: the references and the pad words stay.
+            float4* w = reinterpret_cast<float4*>(o);
+            w[0]      = *reinterpret_cast<const float4*>(&q);
+            uint4*  qw = reinterpret_cast<uint4*>(o) + 2;
+            const uint4 src = *(reinterpret_cast<const uint4*>(&q) + 2);
+            const uint2 tail = *reinterpret_cast<const uint2*>(reinterpret_cast<const uint8_t*>(&q) + 48);
+            *qw = src;
+            *reinterpret_cast<uint2*>(reinterpret_cast<uint8_t*>(o) + 48) = tail;
+        }
+        else
+        {
+            Bvh4Node* o = reinterpret_cast<Bvh4Node*>(wide) + x;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                for (int a = 0; a < 3; ++a)
+                {
+                    o->lo[a][k] = k < nc ? cb[k].lo[a] : 0.f;
+                    o->hi[a][k] = k < nc ? cb[k].hi[a] : 0.f;
+                }
+        }
+    }
+}
 }  // namespace
 
 cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm_count, cudaStream_t s)
@@ -779,4 +873,19 @@ cudaError_t launch_collapse_batch(const BatchArgs& b, DeviceWords* words, int sm
     return cudaGetLastError();
 }
 
+cudaError_t launch_refit_bvh4(uint8_t* result, const GeomLayout& L, DeviceWords* words, int sm_count, cudaStream_t s)
+{
+    if (L.n == 0 || !is_bvh4_format(L.format)) return cudaSuccess;
+    const BvhNode* nodes = reinterpret_cast<const BvhNode*>(result);
+    const Trailer* tr    = reinterpret_cast<const Trailer*>(result + L.trailer_off);
+    const uint32_t cap   = (uint32_t)L.wide_capacity;
+    const uint32_t grid  = (uint32_t)std::min<size_t>(((size_t)cap + 255) / 256, (size_t)sm_count * 16);
+    if (L.format == RR_CUDA_NODE_FORMAT_BVH4Q8)
+        k_refit_bvh4<true><<<grid, 256, 0, s>>>(result + L.wide_off, nodes, L.n, tr, cap, words);
+    else
+        k_refit_bvh4<false><<<grid, 256, 0, s>>>(result + L.wide_off, nodes, L.n, tr, cap, words);
+    return cudaGetLastError();
+}
+
 }  // namespace rr
+

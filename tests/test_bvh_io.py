@@ -23,7 +23,7 @@ def _host_buffer(orc, n, fmt=0):
     buf = np.zeros(toff + 256, np.uint8)
     buf[: nb.size] = nb
     tr = np.zeros(1, rr.TRAILER_DTYPE)
-    tr["magic"], tr["version"], tr["kind"], tr["node_format"] = 0x52524742, 1, 1, fmt
+    tr["magic"], tr["version"], tr["kind"], tr["node_format"] = 0x52524742, 2, 1, fmt
     tr["leaf_count"], tr["node_count"], tr["morton_bits"] = n, 2 * n - 1, 30
     buf[toff:] = tr.view(np.uint8)
     return buf, nodes

@@ -1,14 +1,27 @@
 """GPU RR_BUILD_OPERATION_UPDATE: new vertex positions on an existing tree.
 Binary nodes bit-identical to the oracle's refit of the same topology,
-traversal of the updated tree equal to the oracle's, wide nodes collapsed
-again, argument checks."""
+traversal of the updated tree equal to the oracle's, 8-wide nodes collapsed
+again, 4-wide nodes (either form) requantised in place with their topology,
+argument checks."""
 import numpy as np
 import pytest
 
-from gpu_util import INVALID, hits_np, nodes_of, to_dev, trace, trailer_of
+from gpu_util import INVALID, hits_np, nodes_of, tie_only_mismatch, to_dev, trace, trailer_of
 from test_gpu_build import same_nodes
 
 pytestmark = pytest.mark.gpu
+
+
+def _bvh4_children(res, n, fmt):
+    """The child references of the buffer's 4-wide nodes (fp32: 128-byte nodes, references at byte 96; 8-bit:
+    64-byte nodes, references at byte 16)."""
+    tr = trailer_of(res, n)
+    size, off = (128, 96) if fmt == 2 else (64, 16)
+    raw = res.cpu().numpy().view(np.uint8)
+    base = int(tr["wide_nodes_off"])
+    cnt = int(tr["wide_count"])
+    nodes = raw[base: base + cnt * size].reshape(cnt, size)
+    return nodes[:, off: off + 16].copy().view(np.uint32)
 
 
 def _moved(v, seed):
@@ -16,13 +29,14 @@ def _moved(v, seed):
     return (v * np.float32(1.5) + g.normal(0, 0.003, size=v.shape).astype(np.float32)).astype(np.float32)
 
 
-@pytest.mark.parametrize("fmt", [0, 1, 2])
+@pytest.mark.parametrize("fmt", [0, 1, 2, 4])
 @pytest.mark.parametrize("n", [1, 2, 3, 1000, 40000])
 def test_update_matches_oracle_refit(ctx, orc, fmt, n):
     from radeonrays_sdk_gb300 import scenes
     v, i = scenes.soup(n, scenes.rng(70, n))
     res = ctx.build_geometry(to_dev(v), to_dev(i), node_format=fmt)
     old = nodes_of(res, n).copy()
+    before4 = _bvh4_children(res, n, fmt) if fmt in (2, 4) and n > 3 else None
     v2 = _moved(v, n)
     ctx.update_geometry(to_dev(v2), to_dev(i), res)
     want = orc.fit(orc.build_mesh(v, i)[0], v2, i)
@@ -38,10 +52,16 @@ def test_update_matches_oracle_refit(ctx, orc, fmt, n):
     ref = orc.trace(want, rays)
     assert np.array_equal(trace(ctx, res, rays, traversal=1), ref)
     assert np.array_equal(trace(ctx, res, rays, traversal=3), ref)
-    if fmt in (1, 2):
-        # The re-collapsed wide nodes (8-wide or 4-wide) follow the new boxes.
+    if fmt in (1, 2, 4):
+        # The wide nodes follow the new boxes: 8-wide collapsed again, 4-wide
+        # requantised with their topology.  Hit flags are the reference's and
+        # primitive ids differ only at equal-t ties.
         wide = trace(ctx, res, rays, traversal=2 if fmt == 1 else 4)
         assert np.array_equal(wide[:, 2] != INVALID, ref[:, 2] != INVALID)
+        tie_only_mismatch(orc, rays, wide, ref, v2, i)
+    if fmt in (2, 4) and n > 3:
+        # The 4-wide topology is kept: child references unchanged.
+        assert np.array_equal(_bvh4_children(res, n, fmt), before4)
 
 
 def test_update_twice_back_to_original(ctx, orc):
