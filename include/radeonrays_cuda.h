@@ -259,8 +259,10 @@ RR_API RRError rrCudaAutotuneNodeFormat(RRContext                   context,
  * that rrCmdIntersect, rrCmdBuildScene and updates treat it like one built
  * here (no counterpart in the reference, whose buffers never leave their
  * context).  Reads the buffer's 256-byte trailer with a blocking copy and
- * checks magic, kind and counts against `triangle_count`; a mismatch returns
- * RR_ERROR_INVALID_PARAMETER.  Geometry buffers are position-independent
+ * checks magic, version, kind and counts against `triangle_count`; a mismatch
+ * returns RR_ERROR_INVALID_PARAMETER (a buffer written by an earlier version
+ * of the library, whose 4-wide nodes do not record their binary nodes for
+ * updates, is refused: build it again).  Geometry buffers are position-independent
  * (indices, not pointers), so their bytes can be stored and loaded as they
  * are; scene buffers hold BLAS addresses and are rebuilt instead. */
 RR_API RRError rrCudaRegisterGeometry(RRContext context, RRDevicePtr geometry_buffer, uint32_t triangle_count);
