@@ -751,16 +751,20 @@ __global__ void __launch_bounds__(256) k_refit_bvh4(uint8_t* wide, const BvhNode
     for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < count; x += gridDim.x * blockDim.x)
     {
         uint32_t child[4];
+        uint4    refs, pads;  // the node's reference and pad words, written back as they are
         if (kQ8)
         {
-            const uint4 c = __ldcg(reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4QNode)) + 1);
-            child[0] = c.x, child[1] = c.y, child[2] = c.z, child[3] = c.w;
+            const uint4* w = reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4QNode));
+            refs           = __ldcg(w + 1);
+            pads           = __ldcg(w + 3);
         }
         else
         {
-            const uint4 c = __ldcg(reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4Node)) + 6);
-            child[0] = c.x, child[1] = c.y, child[2] = c.z, child[3] = c.w;
+            const uint4* w = reinterpret_cast<const uint4*>(wide + (size_t)x * sizeof(Bvh4Node));
+            refs           = __ldcg(w + 6);
+            pads           = __ldcg(w + 7);
         }
+        child[0] = refs.x, child[1] = refs.y, child[2] = refs.z, child[3] = refs.w;
         Bx   cb[4];
         int  nc = 0;
         bool ok = true;
@@ -791,28 +795,36 @@ __global__ void __launch_bounds__(256) k_refit_bvh4(uint8_t* wide, const BvhNode
         }
         if (kQ8)
         {
-            Bvh4QNode* o = reinterpret_cast<Bvh4QNode*>(wide) + x;
-            Bvh4QNode  q;
+            // The whole node in four 16-byte stores (no partly written
+            // sector): frame and planes new, references and pads as read.
+            Bvh4QNode q;
             quantize4(q, cb, nc);
-            // Frame and planes only: the references and the pad words stay.
-            float4* w = reinterpret_cast<float4*>(o);
-            w[0]      = *reinterpret_cast<const float4*>(&q);
-            uint4*  qw = reinterpret_cast<uint4*>(o) + 2;
-            const uint4 src = *(reinterpret_cast<const uint4*>(&q) + 2);
-            const uint2 tail = *reinterpret_cast<const uint2*>(reinterpret_cast<const uint8_t*>(&q) + 48);
-            *qw = src;
-            *reinterpret_cast<uint2*>(reinterpret_cast<uint8_t*>(o) + 48) = tail;
+            const uint4* qs = reinterpret_cast<const uint4*>(&q);
+            uint4*       w  = reinterpret_cast<uint4*>(wide + (size_t)x * sizeof(Bvh4QNode));
+            uint4        w3 = qs[3];
+            w3.z            = pads.z;
+            w3.w            = pads.w;
+            w[0]            = qs[0];
+            w[1]            = refs;
+            w[2]            = qs[2];
+            w[3]            = w3;
         }
         else
         {
-            Bvh4Node* o = reinterpret_cast<Bvh4Node*>(wide) + x;
+            Bvh4Node o;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 for (int a = 0; a < 3; ++a)
                 {
-                    o->lo[a][k] = k < nc ? cb[k].lo[a] : 0.f;
-                    o->hi[a][k] = k < nc ? cb[k].hi[a] : 0.f;
+                    o.lo[a][k] = k < nc ? cb[k].lo[a] : 0.f;
+                    o.hi[a][k] = k < nc ? cb[k].hi[a] : 0.f;
                 }
+            const uint4* os = reinterpret_cast<const uint4*>(&o);
+            uint4*       w  = reinterpret_cast<uint4*>(wide + (size_t)x * sizeof(Bvh4Node));
+#pragma unroll
+            for (int j = 0; j < 6; ++j) w[j] = os[j];
+            w[6] = refs;
+            w[7] = pads;
         }
     }
 }
