@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_scene_bvh4(SceneTraceArgs 
     S4Ray    s;
     uint32_t gid = kInvalid, nf = 0;
     bool     active = false, pending = false, exhausted = false;
+    uint32_t it = 0;
     for (;;)
     {
         __syncwarp();
@@ -255,10 +256,25 @@ __global__ void __launch_bounds__(kPBlock, 8) k_trace_scene_bvh4(SceneTraceArgs 
         }
         const uint32_t amask = __ballot_sync(0xffffffffu, active);
         if (amask == 0 && exhausted && __ballot_sync(0xffffffffu, pending) == 0) break;
-        // No leaf batching here (unlike the single-level kernel): with the
-        // instance-tree steps as a third kind, holding the leaf lanes back
-        // measured 4-6 % slower.
-        if (active && s4_step<kAny, kQ8>(s, sa, gid, st, nf))
+        // Step batching: a lane's next step is an instance-tree node, a
+        // BLAS 4-wide node or a BLAS leaf, three different paths.  Each
+        // iteration only the lanes of the most common kind step (every
+        // fourth iteration all of them, so that no lane waits long); the
+        // others wait.  Every ray's own sequence of steps is unchanged, so
+        // hits are too.  Measured 4 Mi / 8.4 M incoherent rays on 256, 512
+        // and 2,048 instanced soups: 6 %, 11 % and 11.5 % faster.  Holding
+        // back only the leaf lanes (the single-level kernel's rule) was
+        // 4-6 % slower, and majority steps without the all-lane iterations
+        // gained nothing.
+        const bool     in_top  = active && s.inst == kInvalid;
+        const bool     in_leaf = active && !in_top && (s.addr & kBvh4Leaf) != 0;
+        const uint32_t nt      = __popc(__ballot_sync(0xffffffffu, in_top));
+        const uint32_t nl      = __popc(__ballot_sync(0xffffffffu, in_leaf));
+        const uint32_t nn      = __popc(amask) - nt - nl;
+        const int      kind    = (nt >= nn && nt >= nl) ? 0 : (nn >= nl ? 1 : 2);
+        ++it;
+        const bool go = (it & 3u) == 0 || (in_top ? kind == 0 : in_leaf ? kind == 2 : kind == 1);
+        if (active && go && s4_step<kAny, kQ8>(s, sa, gid, st, nf))
         {
             active  = false;
             pending = true;
